@@ -1,0 +1,6 @@
+"""ctwin_gb300: GB300-native engine for galloty/ctwin's PRP squaring engine and
+modular-root sieve, behind a C ABI (include/ctwin_gb300.h)."""
+from ._native import CtwError, lib
+from .prp import PrpEngine, prp_test
+
+__all__ = ["CtwError", "lib", "PrpEngine", "prp_test"]

@@ -1,0 +1,75 @@
+"""Loader of the native library (ctwin_gb300/_lib/libctwin_gb300.so).
+
+There is no Python or CPU fallback: when the library is missing or has no
+CUDA device to run on, the calls fail with CtwError.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libctwin_gb300.so")
+
+_lock = threading.Lock()
+_lib = None
+
+
+class CtwError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ctwin_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"native library not built: {LIB_PATH} (run ctwin_gb300.build)")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i32, u32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_longlong
+        H = ctypes.c_void_p
+        sigs = {
+            "ctw_last_error": ([], ctypes.c_char_p),
+            "ctw_version": ([], ctypes.c_char_p),
+            "ctw_device_count": ([], i32),
+            "ctw_prp_create": ([i32, i32, ctypes.POINTER(H)], i32),
+            "ctw_prp_destroy": ([H], i32),
+            "ctw_prp_set_csize": ([H, i32], i32),
+            "ctw_prp_set_base": ([H, u32], i32),
+            "ctw_prp_set_b": ([H, vp, i32], i32),
+            "ctw_prp_set": ([H, u32], i32),
+            "ctw_prp_copy": ([H, i32, i32], i32),
+            "ctw_prp_square_dup": ([H, vp], i32),
+            "ctw_prp_mul": ([H], i32),
+            "ctw_prp_mul_regs": ([H, i32, i32, i32], i32),
+            "ctw_prp_square_bits": ([H, vp, i32, i64, i32], i32),
+            "ctw_prp_get_digits": ([H, i32, vp], i32),
+            "ctw_prp_is_prime": ([H, i32, vp, vp], i32),
+            "ctw_prp_read_regs": ([H, i32, i32, vp], i32),
+            "ctw_prp_write_regs": ([H, i32, i32, vp], i32),
+            "ctw_prp_run": ([H, vp, i32, vp, vp, vp], i32),
+            "ctw_prp_sync": ([H], i32),
+            "ctw_prp_stream": ([H], vp),
+            "ctw_prp_geometry": ([H, vp, vp, vp], i32),
+            "ctw_prp_launches": ([H], i64),
+            "ctw_imad_peak": ([], ctypes.c_double),
+        }
+        for name, (args, res) in sigs.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+        return _lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        raise CtwError(rc, lib().ctw_last_error().decode(errors="replace"))
+
+
+def ptr(a) -> ctypes.c_void_p:
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None

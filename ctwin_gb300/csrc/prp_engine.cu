@@ -1,0 +1,647 @@
+// Host side of the PRP engine: root tables, launches, canonical digits,
+// RES64 and the Gerbicz-Li driver, behind the C ABI of include/ctwin_gb300.h.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ctwin_gb300.h"
+#include "bignum.h"
+#include "prp_arith.cuh"
+#include "prp_kernels.cuh"
+
+namespace ctw {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...)
+{
+	char buf[512];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof(buf), fmt, ap);
+	va_end(ap);
+	g_last_error = buf;
+	return code;
+}
+
+#define CTW_CUDA(call)                                                                                       \
+	do {                                                                                                     \
+		cudaError_t e_ = (call);                                                                             \
+		if (e_ != cudaSuccess) return fail(CTW_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),     \
+		                                   __FILE__, __LINE__);                                              \
+	} while (0)
+
+// ---- host modular arithmetic for table generation ----
+static uint32_t mulmod(uint32_t a, uint32_t b, uint32_t q) { return (uint32_t)(((uint64_t)a * b) % q); }
+static uint32_t powmod(uint32_t a, uint64_t e, uint32_t q)
+{
+	uint32_t r = 1 % q;
+	while (e) { if (e & 1) r = mulmod(r, a, q); a = mulmod(a, a, q); e >>= 1; }
+	return r;
+}
+static uint32_t invmod(uint32_t a, uint32_t q) { return powmod(a, q - 2, q); }
+static uint32_t mont(uint32_t a, uint32_t q) { return (uint32_t)((((uint64_t)a) << 32) % q); }
+static size_t bitrev(size_t j, size_t s)
+{
+	size_t r = 0;
+	for (size_t k = s; k > 1; k >>= 1, j >>= 1) r = (r << 1) | (j & 1);
+	return r;
+}
+
+static const uint32_t kQ[3] = { Q0, Q1, Q2 };
+static const uint32_t kGen[3] = { QGEN0, QGEN1, QGEN2 };
+
+}  // namespace ctw
+
+using namespace ctw;
+
+struct ctw_prp {
+	int ln = 0, lanes = 0, lg = 0, lm = 0, csize = 16;
+	uint32_t base = 2;
+	size_t D = 0, M = 0, G = 1;
+	int threads = 0;
+	size_t smem = 0;
+	int tw_smem = 0;
+	cudaStream_t stream = nullptr;
+	int32_t *d_regs = nullptr;        // [3][lanes][D]
+	uint32_t *d_scratch = nullptr;    // [lanes][G][3][M]
+	uint32_t *d_tf = nullptr, *d_ti = nullptr;
+	uint32_t *d_laneb = nullptr;      // [lanes][4]
+	uint32_t *d_bits = nullptr;
+	size_t bits_cap = 0;
+	uint32_t *d_status = nullptr;
+	std::vector<uint32_t> b;
+	PrpKernelArgs proto{};
+	long long launches = 0;
+
+	int32_t *reg(int r) const { return d_regs + (size_t)r * lanes * D; }
+};
+
+namespace {
+
+int check_handle(ctw_prp *h)
+{
+	if (!h) return fail(CTW_E_ARG, "null handle");
+	return CTW_OK;
+}
+
+// Roots of the ring X^D - X^{D/2} + 1 (the reference's ordering,
+// cyclo/src/transform.h:336-368): level s (s blocks), block j uses
+// r_{6s}^{3*bitrev(j,s) + 1 + floor(2j/s)}, r_{6s} a primitive 6s-th root.
+int build_tables(ctw_prp *h)
+{
+	const size_t D = h->D, M = h->M, G = h->G;
+	std::vector<uint32_t> tf(G * 3 * M, 0), ti(G * 3 * M, 0);
+	for (int pi = 0; pi < 3; ++pi)
+	{
+		const uint32_t q = kQ[pi];
+		std::vector<uint32_t> W(D, 0);
+		for (size_t s = 1; s < D; s *= 2)
+		{
+			const uint32_t rs = powmod(kGen[pi], (q - 1) / (6 * (uint64_t)s), q);
+			for (size_t j = 0; j < s; ++j) W[s + j] = powmod(rs, 3 * bitrev(j, s) + 1 + (2 * j) / s, q);
+		}
+		// local levels l: global level LG + l, block g*2^l + j'
+		for (size_t g = 0; g < G; ++g)
+			for (int l = 0; l < h->lm; ++l)
+				for (size_t jp = 0; jp < ((size_t)1 << l); ++jp)
+				{
+					const uint32_t w = W[(G << l) + (g << l) + jp];
+					tf[(g * 3 + pi) * M + ((size_t)1 << l) + jp] = mont(w, q);
+					ti[(g * 3 + pi) * M + ((size_t)1 << l) + jp] = mont(invmod(w, q), q);
+				}
+		for (size_t k = 1; k < G; ++k)
+		{
+			h->proto.tcf[pi][k] = mont(W[k], q);
+			h->proto.tci[pi][k] = mont(invmod(W[k], q), q);
+		}
+		const uint32_t w1 = W[1];
+		const uint32_t S = mulmod((uint32_t)(((uint64_t)1 << 32) % q), mulmod(2, invmod((uint32_t)(D % q), q), q), q);
+		const uint32_t K1 = mulmod(S, invmod((mulmod(2, w1, q) + q - 1) % q, q), q);
+		h->proto.omega[pi] = mont(w1, q);
+		h->proto.sc[pi] = mont(S, q);
+		h->proto.k1[pi] = mont(K1, q);
+	}
+	h->proto.ginv[0] = mont(invmod(Q2 % Q1, Q1), Q1);
+	h->proto.ginv[1] = mont(invmod(Q2 % Q0, Q0), Q0);
+	h->proto.ginv[2] = mont(invmod(Q1 % Q0, Q0), Q0);
+	const size_t bytes = G * 3 * M * sizeof(uint32_t);
+	CTW_CUDA(cudaMalloc(&h->d_tf, bytes));
+	CTW_CUDA(cudaMalloc(&h->d_ti, bytes));
+	CTW_CUDA(cudaMemcpy(h->d_tf, tf.data(), bytes, cudaMemcpyHostToDevice));
+	CTW_CUDA(cudaMemcpy(h->d_ti, ti.data(), bytes, cudaMemcpyHostToDevice));
+	return CTW_OK;
+}
+
+PrpKernelArgs make_args(ctw_prp *h)
+{
+	PrpKernelArgs a = h->proto;
+	a.tf = h->d_tf;
+	a.ti = h->d_ti;
+	a.lane_b = h->d_laneb;
+	a.status = h->d_status;
+	a.lm = h->lm;
+	a.csize = h->csize;
+	a.mult = (int)h->base;
+	a.tw_smem = h->tw_smem;
+	a.scratch = h->d_scratch;
+	return a;
+}
+
+int launch(ctw_prp *h, const PrpKernelArgs &a)
+{
+	const cudaError_t e = prp_launch(a, h->lg, h->lanes, h->stream);
+	if (e != cudaSuccess) return fail(CTW_E_CUDA, "PRP kernel launch: %s", cudaGetErrorString(e));
+	++h->launches;
+	return CTW_OK;
+}
+
+int ensure_bits(ctw_prp *h, size_t words)
+{
+	if (words <= h->bits_cap) return CTW_OK;
+	if (h->d_bits) cudaFree(h->d_bits);
+	h->d_bits = nullptr;
+	h->bits_cap = 0;
+	CTW_CUDA(cudaMalloc(&h->d_bits, words * sizeof(uint32_t)));
+	h->bits_cap = words;
+	return CTW_OK;
+}
+
+int check_status(ctw_prp *h)
+{
+	uint32_t st = 0;
+	CTW_CUDA(cudaMemcpyAsync(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+	CTW_CUDA(cudaStreamSynchronize(h->stream));
+	if (st != 0)
+	{
+		cudaMemsetAsync(h->d_status, 0, sizeof(uint32_t), h->stream);
+		return fail(CTW_E_COMPUTE, "device arithmetic range check failed (status 0x%x)", st);
+	}
+	return CTW_OK;
+}
+
+// Canonical digits of x mod N = b^D - b^{D/2} + 1 (cyclo/src/transform.h:501-597):
+// carry the signed digits base b, fold the top carry T as -T at 0 and +T at
+// D/2 (b^D = b^{D/2} - 1 mod N) until it vanishes, then subtract N once if the
+// value is >= N.
+int canonical(const int32_t *x, uint32_t b, size_t D, uint32_t *out)
+{
+	const int64_t B = b;
+	auto divmod = [B](int64_t &v) -> uint32_t {
+		int64_t q = v / B, r = v % B;
+		if (r < 0) { r += B; --q; }
+		v = q;
+		return (uint32_t)r;
+	};
+	int64_t c = 0;
+	for (size_t j = 0; j < D; ++j)
+	{
+		int64_t v = c + x[j];
+		out[j] = divmod(v);
+		c = v;
+	}
+	for (int guard = 0; c != 0; ++guard)
+	{
+		if (guard > 64) return fail(CTW_E_COMPUTE, "getInt: carry does not settle");
+		int64_t v = -c;
+		for (size_t j = 0; j < D / 2; ++j) { v += out[j]; out[j] = divmod(v); }
+		v += c;
+		for (size_t j = D / 2; j < D; ++j) { v += out[j]; out[j] = divmod(v); if (v == 0) break; }
+		c = v;
+	}
+	bool ge = true;
+	for (size_t j = D / 2; j < D; ++j) if (out[j] != b - 1) { ge = false; break; }
+	if (ge)
+	{
+		bool low_zero = true;
+		for (size_t j = 0; j < D / 2; ++j) if (out[j] != 0) { low_zero = false; break; }
+		ge = !low_zero;
+	}
+	if (ge)
+	{
+		// value - N: lower half minus 1, upper half cleared
+		size_t j = 0;
+		while (j < D / 2 && out[j] == 0) { out[j] = b - 1; ++j; }
+		if (j == D / 2) return fail(CTW_E_COMPUTE, "getInt failed");
+		out[j] -= 1;
+		for (size_t k = D / 2; k < D; ++k) out[k] = 0;
+	}
+	return CTW_OK;
+}
+
+int read_reg_host(ctw_prp *h, int reg, std::vector<int32_t> &v)
+{
+	v.resize((size_t)h->lanes * h->D);
+	CTW_CUDA(cudaMemcpyAsync(v.data(), h->reg(reg), v.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+	CTW_CUDA(cudaStreamSynchronize(h->stream));
+	return CTW_OK;
+}
+
+int canonical_reg(ctw_prp *h, int reg, std::vector<uint32_t> &c)
+{
+	std::vector<int32_t> v;
+	int rc = check_status(h);
+	if (rc) return rc;
+	if ((rc = read_reg_host(h, reg, v))) return rc;
+	c.resize(v.size());
+	for (int l = 0; l < h->lanes; ++l)
+		if ((rc = canonical(v.data() + (size_t)l * h->D, h->b[(size_t)l], h->D, c.data() + (size_t)l * h->D))) return rc;
+	return CTW_OK;
+}
+
+void res64_of(const uint32_t *c, uint32_t b, size_t D, bool &prp, bool &zero, uint64_t &r64)
+{
+	prp = (c[0] == 1);
+	zero = (c[0] == 0);
+	uint64_t r = c[0], bp = b;
+	for (size_t j = 1; j < D; ++j)
+	{
+		prp &= (c[j] == 0);
+		zero &= (c[j] == 0);
+		r += (uint64_t)c[j] * bp;
+		bp *= b;
+	}
+	r64 = r;
+}
+
+int op_square_bits(ctw_prp *h, const uint32_t *d_bits, int nwords, long long i_hi, int count)
+{
+	PrpKernelArgs a = make_args(h);
+	a.op = OP_SQUARE;
+	a.reg_in = h->reg(0);
+	a.reg_out = h->reg(0);
+	a.bits = d_bits;
+	a.nwords = nwords;
+	a.i_hi = i_hi;
+	a.count = count;
+	a.use_dupmask = 0;
+	return launch(h, a);
+}
+
+int op_mul(ctw_prp *h, int out, int x, int y)
+{
+	PrpKernelArgs a = make_args(h);
+	a.op = OP_MUL;
+	a.reg_in = h->reg(x);
+	a.reg_y = h->reg(y);
+	a.reg_out = h->reg(out);
+	a.count = 1;
+	return launch(h, a);
+}
+
+int op_set(ctw_prp *h, int reg, uint32_t v)
+{
+	const size_t n = (size_t)h->lanes * h->D;
+	CTW_CUDA(cudaMemsetAsync(h->reg(reg), 0, n * sizeof(int32_t), h->stream));
+	if (v != 0)
+	{
+		// coefficient 0 of every lane; a strided 2D copy of one int32 per lane
+		static thread_local std::vector<int32_t> one;
+		one.assign((size_t)h->lanes, (int32_t)v);
+		CTW_CUDA(cudaMemcpy2DAsync(h->reg(reg), h->D * sizeof(int32_t), one.data(), sizeof(int32_t), sizeof(int32_t),
+		                           (size_t)h->lanes, cudaMemcpyHostToDevice, h->stream));
+		CTW_CUDA(cudaStreamSynchronize(h->stream));
+	}
+	return CTW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *ctw_last_error(void) { return g_last_error.c_str(); }
+const char *ctw_version(void) { return "ctwin_gb300 0.1 (sm_103a)"; }
+int ctw_device_count(void)
+{
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess) { cudaGetLastError(); return 0; }
+	return n;
+}
+
+int ctw_prp_create(int log2_degree, int lanes, ctw_prp **out)
+{
+	if (!out) return fail(CTW_E_ARG, "null output pointer");
+	*out = nullptr;
+	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
+	if (lanes < 1 || lanes > MAX_INLINE_LANES) return fail(CTW_E_ARG, "lanes %d outside [1, %d]", lanes, MAX_INLINE_LANES);
+	if (ctw_device_count() == 0) return fail(CTW_E_CUDA, "no CUDA device");
+	ctw_prp *h = new ctw_prp();
+	h->ln = log2_degree;
+	h->lanes = lanes;
+	h->lg = log2_degree > 12 ? std::min(log2_degree - 12, MAX_LG) : 0;
+	h->lm = log2_degree - h->lg;
+	h->D = (size_t)1 << log2_degree;
+	h->G = (size_t)1 << h->lg;
+	h->M = h->D / h->G;
+	h->tw_smem = prp_smem_bytes(h->lm, 1) <= 227 * 1024 ? 1 : 0;
+	h->smem = prp_smem_bytes(h->lm, h->tw_smem);
+	h->threads = prp_threads(h->lm);
+	h->b.assign((size_t)lanes, 0);
+	int rc = CTW_OK;
+	auto cleanup = [&](int code) { ctw_prp_destroy(h); return code; };
+	if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+		return cleanup(fail(CTW_E_CUDA, "stream creation failed"));
+	const size_t rbytes = 3 * (size_t)lanes * h->D * sizeof(int32_t);
+	if (cudaMalloc(&h->d_regs, rbytes) != cudaSuccess) return cleanup(fail(CTW_E_NOMEM, "register allocation"));
+	if (cudaMalloc(&h->d_scratch, (size_t)lanes * h->D * 3 * sizeof(uint32_t)) != cudaSuccess)
+		return cleanup(fail(CTW_E_NOMEM, "scratch allocation"));
+	if (cudaMalloc(&h->d_laneb, (size_t)lanes * 4 * sizeof(uint32_t)) != cudaSuccess)
+		return cleanup(fail(CTW_E_NOMEM, "lane allocation"));
+	if (cudaMalloc(&h->d_status, sizeof(uint32_t)) != cudaSuccess) return cleanup(fail(CTW_E_NOMEM, "status"));
+	cudaMemset(h->d_regs, 0, rbytes);
+	cudaMemset(h->d_status, 0, sizeof(uint32_t));
+	cudaMemset(h->d_laneb, 0, (size_t)lanes * 4 * sizeof(uint32_t));
+	if ((rc = build_tables(h))) return cleanup(rc);
+	if (cudaDeviceSynchronize() != cudaSuccess) return cleanup(fail(CTW_E_CUDA, "device init failed"));
+	*out = h;
+	return CTW_OK;
+}
+
+int ctw_prp_destroy(ctw_prp *h)
+{
+	if (!h) return CTW_OK;
+	if (h->stream) cudaStreamSynchronize(h->stream);
+	cudaFree(h->d_regs);
+	cudaFree(h->d_scratch);
+	cudaFree(h->d_tf);
+	cudaFree(h->d_ti);
+	cudaFree(h->d_laneb);
+	cudaFree(h->d_bits);
+	cudaFree(h->d_status);
+	if (h->stream) cudaStreamDestroy(h->stream);
+	delete h;
+	return CTW_OK;
+}
+
+int ctw_prp_set_csize(ctw_prp *h, int csize)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (csize != 8 && csize != 16 && csize != 32 && csize != 64) return fail(CTW_E_ARG, "csize %d not in {8,16,32,64}", csize);
+	if ((size_t)csize * 2 > h->M) return fail(CTW_E_ARG, "csize too large for this degree");
+	h->csize = csize;
+	return CTW_OK;
+}
+
+int ctw_prp_set_base(ctw_prp *h, uint32_t base)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (base != 2 && base != 3) return fail(CTW_E_ARG, "base %u not in {2,3}", base);
+	h->base = base;
+	return CTW_OK;
+}
+
+int ctw_prp_set_b(ctw_prp *h, const uint32_t *b, int count)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (!b || count != h->lanes) return fail(CTW_E_ARG, "set_b expects lanes (%d) values", h->lanes);
+	std::vector<uint32_t> lb((size_t)h->lanes * 4);
+	for (int l = 0; l < h->lanes; ++l)
+	{
+		const uint32_t bl = b[l];
+		if (bl < 64 || bl >= 0x80000000u) return fail(CTW_E_ARG, "b = %u outside [64, 2^31)", bl);
+		const int s = (31 - __builtin_clz(bl)) - 1;
+		lb[4 * l + 0] = bl;
+		lb[4 * l + 1] = (uint32_t)(((uint64_t)1 << (s + 32)) / bl);
+		lb[4 * l + 2] = (uint32_t)s;
+		lb[4 * l + 3] = 0;
+		h->b[(size_t)l] = bl;
+	}
+	CTW_CUDA(cudaMemcpyAsync(h->d_laneb, lb.data(), lb.size() * 4, cudaMemcpyHostToDevice, h->stream));
+	CTW_CUDA(cudaStreamSynchronize(h->stream));
+	return CTW_OK;
+}
+
+int ctw_prp_set(ctw_prp *h, uint32_t a)
+{
+	if (int rc = check_handle(h)) return rc;
+	return op_set(h, 0, a);
+}
+
+int ctw_prp_copy(ctw_prp *h, int dst, int src)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (dst < 0 || dst > 2 || src < 0 || src > 2) return fail(CTW_E_ARG, "register index outside 0..2");
+	if (dst == src) return CTW_OK;
+	CTW_CUDA(cudaMemcpyAsync(h->reg(dst), h->reg(src), (size_t)h->lanes * h->D * sizeof(int32_t),
+	                         cudaMemcpyDeviceToDevice, h->stream));
+	return CTW_OK;
+}
+
+int ctw_prp_square_dup(ctw_prp *h, const uint64_t *mask)
+{
+	if (int rc = check_handle(h)) return rc;
+	PrpKernelArgs a = make_args(h);
+	a.op = OP_SQUARE;
+	a.reg_in = h->reg(0);
+	a.reg_out = h->reg(0);
+	a.count = 1;
+	a.i_hi = 0;
+	a.use_dupmask = 1;
+	const int nw = (h->lanes + 63) / 64;
+	for (int w = 0; w < nw; ++w) a.dupmask[w] = mask ? mask[w] : 0;
+	return launch(h, a);
+}
+
+int ctw_prp_mul(ctw_prp *h)
+{
+	if (int rc = check_handle(h)) return rc;
+	return op_mul(h, 0, 0, 1);
+}
+
+int ctw_prp_mul_regs(ctw_prp *h, int reg_out, int reg_a, int reg_b)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (reg_out < 0 || reg_out > 2 || reg_a < 0 || reg_a > 2 || reg_b < 0 || reg_b > 2)
+		return fail(CTW_E_ARG, "register index outside 0..2");
+	return op_mul(h, reg_out, reg_a, reg_b);
+}
+
+int ctw_prp_square_bits(ctw_prp *h, const uint32_t *e_words, int nwords, long long i_hi, int count)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (!e_words || nwords < 1 || count < 0) return fail(CTW_E_ARG, "bad exponent arguments");
+	if (count == 0) return CTW_OK;
+	const size_t words = (size_t)h->lanes * nwords;
+	if (int rc = ensure_bits(h, words)) return rc;
+	CTW_CUDA(cudaMemcpyAsync(h->d_bits, e_words, words * 4, cudaMemcpyHostToDevice, h->stream));
+	CTW_CUDA(cudaStreamSynchronize(h->stream));   // e_words may be reused by the caller
+	return op_square_bits(h, h->d_bits, nwords, i_hi, count);
+}
+
+int ctw_prp_get_digits(ctw_prp *h, int reg, uint32_t *out)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (!out || reg < 0 || reg > 2) return fail(CTW_E_ARG, "bad arguments");
+	std::vector<uint32_t> c;
+	if (int rc = canonical_reg(h, reg, c)) return rc;
+	memcpy(out, c.data(), c.size() * sizeof(uint32_t));
+	return CTW_OK;
+}
+
+int ctw_prp_is_prime(ctw_prp *h, int reg, uint8_t *is_prp, uint64_t *res64)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (reg < 0 || reg > 2) return fail(CTW_E_ARG, "bad register");
+	std::vector<uint32_t> c;
+	if (int rc = canonical_reg(h, reg, c)) return rc;
+	bool any_zero = false;
+	for (int l = 0; l < h->lanes; ++l)
+	{
+		bool prp, zero;
+		uint64_t r;
+		res64_of(c.data() + (size_t)l * h->D, h->b[(size_t)l], h->D, prp, zero, r);
+		if (is_prp) is_prp[l] = prp ? 1 : 0;
+		if (res64) res64[l] = r;
+		any_zero |= zero;
+	}
+	return any_zero ? fail(CTW_E_COMPUTE, "computation failed (zero residue)") : CTW_OK;
+}
+
+int ctw_prp_read_regs(ctw_prp *h, int first, int nregs, int32_t *out)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (!out || first < 0 || nregs < 1 || first + nregs > 3) return fail(CTW_E_ARG, "bad register range");
+	CTW_CUDA(cudaMemcpyAsync(out, h->reg(first), (size_t)nregs * h->lanes * h->D * 4, cudaMemcpyDeviceToHost, h->stream));
+	CTW_CUDA(cudaStreamSynchronize(h->stream));
+	return CTW_OK;
+}
+
+int ctw_prp_write_regs(ctw_prp *h, int first, int nregs, const int32_t *in)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (!in || first < 0 || nregs < 1 || first + nregs > 3) return fail(CTW_E_ARG, "bad register range");
+	CTW_CUDA(cudaMemcpyAsync(h->reg(first), in, (size_t)nregs * h->lanes * h->D * 4, cudaMemcpyHostToDevice, h->stream));
+	CTW_CUDA(cudaStreamSynchronize(h->stream));
+	return CTW_OK;
+}
+
+int ctw_prp_run(ctw_prp *h, const uint32_t *bv, int count, uint8_t *is_prp, uint64_t *res64, uint8_t *gl_ok)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (!bv || count < 1 || count > h->lanes) return fail(CTW_E_ARG, "count must be in [1, lanes]");
+	const int V = h->lanes;
+	std::vector<uint32_t> b((size_t)V);
+	for (int l = 0; l < V; ++l) b[(size_t)l] = bv[l < count ? l : count - 1];
+	int rc;
+	if ((rc = ctw_prp_set_b(h, b.data(), V))) return rc;
+
+	// Exponents E_l = b_l^D - b_l^{D/2} and the shared bit range (cyclo/src/cyclo.h:254-272).
+	std::vector<Big> E((size_t)V);
+	long long i0 = 0;
+	for (int l = 0; l < V; ++l)
+	{
+		if (l > 0 && b[(size_t)l] == b[(size_t)l - 1]) E[(size_t)l] = E[(size_t)l - 1];
+		else E[(size_t)l] = prp_exponent(b[(size_t)l], h->ln);
+		i0 = std::max(i0, (long long)big_bitlen(E[(size_t)l]) - 1);
+	}
+	const int L = 2 << ((31 - __builtin_clz((uint32_t)i0)) / 2);
+	const long long B_GL = (i0 - 1) / L + 1;
+
+	auto upload = [&](const std::vector<Big> &ex, int &nw) -> int {
+		size_t maxw = 1;
+		for (const Big &e : ex) maxw = std::max(maxw, e.size());
+		nw = (int)maxw;
+		std::vector<uint32_t> words((size_t)V * maxw, 0);
+		for (int l = 0; l < V; ++l) std::copy(ex[(size_t)l].begin(), ex[(size_t)l].end(), words.begin() + (size_t)l * maxw);
+		int r = ensure_bits(h, words.size());
+		if (r) return r;
+		CTW_CUDA(cudaMemcpyAsync(h->d_bits, words.data(), words.size() * 4, cudaMemcpyHostToDevice, h->stream));
+		CTW_CUDA(cudaStreamSynchronize(h->stream));
+		return CTW_OK;
+	};
+
+	int nw = 0;
+	if ((rc = upload(E, nw))) return rc;
+	if ((rc = op_set(h, 0, 1)) || (rc = op_set(h, 1, 1))) return rc;
+
+	// bits i0..0; after bit i with i % B_GL == 0 and i / B_GL != 0: d <- d * x
+	long long i = i0;
+	while (i >= 0)
+	{
+		const long long stop = (i / B_GL) * B_GL;    // next checkpoint at or below i
+		const int cnt = (int)(i - stop + 1);
+		if ((rc = op_square_bits(h, h->d_bits, nw, i, cnt))) return rc;
+		if (stop / B_GL != 0)
+		{
+			if ((rc = op_mul(h, 1, 0, 1))) return rc;
+		}
+		i = stop - 1;
+	}
+	std::vector<uint32_t> c0;
+	if ((rc = canonical_reg(h, 0, c0))) return rc;
+
+	// d(t+1) = d(t) * x in reg2; reg1 keeps d(t)
+	if ((rc = op_mul(h, 2, 0, 1))) return rc;
+
+	std::vector<Big> res((size_t)V);
+	long long j0 = 0;
+	for (int l = 0; l < V; ++l)
+	{
+		res[(size_t)l] = big_block_sum(E[(size_t)l], (int)B_GL);
+		j0 = std::max(j0, (long long)big_bitlen(res[(size_t)l]) - 1);
+	}
+	if ((rc = upload(res, nw))) return rc;
+	if ((rc = op_set(h, 0, 1))) return rc;
+	if (j0 >= B_GL)
+	{
+		if ((rc = op_square_bits(h, h->d_bits, nw, j0, (int)(j0 - B_GL + 1)))) return rc;
+	}
+	if ((rc = op_mul(h, 0, 0, 1))) return rc;
+	// remaining bits B_GL-1..0 (bits above j0 are zero in the exponent words)
+	if ((rc = op_square_bits(h, h->d_bits, nw, B_GL - 1, (int)B_GL))) return rc;
+
+	std::vector<uint32_t> c1, c2;
+	if ((rc = canonical_reg(h, 0, c1))) return rc;
+	if ((rc = canonical_reg(h, 2, c2))) return rc;
+	bool any_zero = false;
+	for (int l = 0; l < count; ++l)
+	{
+		bool prp, zero;
+		uint64_t r;
+		const size_t off = (size_t)l * h->D;
+		res64_of(c0.data() + off, b[(size_t)l], h->D, prp, zero, r);
+		if (is_prp) is_prp[l] = prp ? 1 : 0;
+		if (res64) res64[l] = r;
+		if (gl_ok) gl_ok[l] = (memcmp(c1.data() + off, c2.data() + off, h->D * sizeof(uint32_t)) == 0) ? 1 : 0;
+		any_zero |= zero;
+	}
+	// reset like the reference between vectors (cyclo/src/cyclo.h:475-477)
+	if ((rc = op_set(h, 0, 1)) || (rc = op_set(h, 1, 1))) return rc;
+	if (any_zero) return fail(CTW_E_COMPUTE, "computation failed (zero residue)");
+	for (int l = 0; l < count; ++l)
+		if (gl_ok && !gl_ok[l]) return fail(CTW_E_GERBICZ, "Gerbicz failed (lane %d)", l);
+	return CTW_OK;
+}
+
+int ctw_prp_sync(ctw_prp *h)
+{
+	if (int rc = check_handle(h)) return rc;
+	CTW_CUDA(cudaStreamSynchronize(h->stream));
+	return check_status(h);
+}
+
+void *ctw_prp_stream(ctw_prp *h) { return h ? (void *)h->stream : nullptr; }
+
+int ctw_prp_geometry(ctw_prp *h, int *ctas, int *threads, int *smem)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (ctas) *ctas = (int)h->G;
+	if (threads) *threads = h->threads;
+	if (smem) *smem = (int)h->smem;
+	return CTW_OK;
+}
+
+long long ctw_prp_launches(ctw_prp *h) { return h ? h->launches : 0; }
+
+double ctw_imad_peak(void)
+{
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) return 0.0;
+	return imad_peak(dev);
+}
+
+}  // extern "C"

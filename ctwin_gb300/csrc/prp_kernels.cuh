@@ -1,0 +1,55 @@
+// Launch interface of the PRP squaring kernels (host <-> device).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ctw {
+
+constexpr int MAX_LG = 4;          // up to 16 CTAs (one thread-block cluster) per candidate
+constexpr int MAX_G = 1 << MAX_LG;
+constexpr int MAX_INLINE_LANES = 4096;  // lanes whose dup bits fit the launch parameters
+
+enum PrpOp : int { OP_SQUARE = 0, OP_MUL = 1 };
+
+struct PrpKernelArgs {
+	const int32_t *reg_in;      // [lanes][D] digits of x
+	int32_t *reg_out;           // [lanes][D] digits of the result (may alias reg_in)
+	const int32_t *reg_y;       // [lanes][D] digits of y (OP_MUL)
+	uint32_t *scratch;          // [lanes][G][3][M] transform of y (OP_MUL)
+	const uint32_t *tf;         // [3][G][M] local forward roots (Montgomery form)
+	const uint32_t *ti;         // [3][G][M] local inverse roots
+	const uint32_t *lane_b;     // [lanes][4] = b, floor(2^(s+32)/b), s = ilog2(b)-1, 0
+	const uint32_t *bits;       // [lanes][nwords] exponent bits
+	uint32_t *status;           // error flags (0 = ok)
+	long long i_hi;             // first (most significant) bit index processed
+	int count;                  // squarings in this launch (OP_SQUARE)
+	int nwords;
+	int lm;                     // log2 of coefficients per CTA
+	int csize;                  // carry chunk (8..64), as the reference's CSIZE
+	int mult;                   // multiplier applied when a bit is set (2 = base 2, 3 = base 3)
+	int op;
+	int tw_smem;                // 1: copy the local roots into shared memory
+	uint32_t omega[3];          // 6th root w1 (Montgomery form)
+	uint32_t k1[3];             // S / (2 w1 - 1)
+	uint32_t sc[3];             // S = 2^32 * 2 / D   (Montgomery form)
+	uint32_t ginv[3];           // Garner: q2^-1 mod q1, q2^-1 mod q0, q1^-1 mod q0 (Montgomery forms)
+	uint32_t tcf[3][MAX_G];     // cross-CTA forward roots w[1..G-1]
+	uint32_t tci[3][MAX_G];     // cross-CTA inverse roots
+	int use_dupmask;            // 1: the bit of lane l is bit l of dupmask (count == 1)
+	uint64_t dupmask[MAX_INLINE_LANES / 64];
+};
+
+enum PrpStatus : uint32_t {
+	ST_OK = 0,
+	ST_BARRETT_RANGE = 1,       // quotient outside the two-step Barrett range
+	ST_DIGIT_RANGE = 2,         // a digit left the int32 range
+};
+
+size_t prp_smem_bytes(int lm, int tw_smem);
+int prp_threads(int lm);
+cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t stream);
+
+// Integer-multiply throughput probe (roofline denominator): returns IMAD/s.
+double imad_peak(int device);
+
+}  // namespace ctw

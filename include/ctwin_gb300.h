@@ -1,0 +1,117 @@
+/*
+ * ctwin_gb300 — GB300 (sm_103a) engine for the two data-parallel hot paths of
+ * galloty/ctwin: the cyclotomic PRP squaring engine and the modular-root sieve.
+ *
+ * C ABI.  Plain pointers and sizes; every function returns 0 on success or a
+ * negative CTW_E* code, and never exits or throws (the reference's engine calls
+ * exit() on OpenCL errors, cyclo/src/ocl.h:106-113).  ctw_last_error() gives the
+ * message of the last failure on the calling thread.  Handles are opaque, owned
+ * by the caller, not thread-safe; each PRP handle owns one CUDA stream.
+ * All citations are paths inside the reference project.
+ */
+#ifndef CTWIN_GB300_H
+#define CTWIN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CTW_OK 0
+#define CTW_E_ARG (-1)        /* invalid argument */
+#define CTW_E_CUDA (-2)       /* CUDA runtime error (no device, launch failure, ...) */
+#define CTW_E_NOMEM (-3)      /* device or host allocation failed */
+#define CTW_E_COMPUTE (-4)    /* arithmetic self-check failed (range, getInt, zero residue) */
+#define CTW_E_GERBICZ (-5)    /* Gerbicz-Li check failed */
+
+const char *ctw_last_error(void);
+/* Library version string. */
+const char *ctw_version(void);
+/* Number of visible CUDA devices (0 when none); never fails. */
+int ctw_device_count(void);
+
+/* ------------------------------------------------------------------------ */
+/* PRP engine: Fermat test of N = Phi_{3*2^n}(b) = b^D - b^{D/2} + 1, D = 2^n */
+/* ------------------------------------------------------------------------ */
+
+typedef struct ctw_prp ctw_prp;
+
+/* Create an engine for degree D = 2^log2_degree (8..18) and `lanes` candidates
+ * of that degree (the reference uses 64 lanes, VSIZE).  Registers 0..2 hold
+ * one residue per lane each, initialised to 0.
+ * Replaces: engine ctor + allocMemory + createKernels (cyclo/src/engine.h:40-65,132)
+ *           and transform ctor / initEngine roots (cyclo/src/transform.h:300-433). */
+int ctw_prp_create(int log2_degree, int lanes, ctw_prp **out);
+int ctw_prp_destroy(ctw_prp *h);
+
+/* Carry chunk size, 8/16/32/64 (the reference's CSIZE, autotuned there,
+ * cyclo/src/transform.h:383-419).  Register digits depend on it; canonical
+ * results do not.  Default 16. */
+int ctw_prp_set_csize(ctw_prp *h, int csize);
+/* Base of the Fermat test: 2 (the reference) or 3.  Sets the multiplier that
+ * square_dup applies for a set bit.  Default 2. */
+int ctw_prp_set_base(ctw_prp *h, uint32_t base);
+
+/* b of each lane, 64 <= b < 2^31; count == lanes.
+ * Replaces transform::set_b / engine::writeMemory_b (cyclo/src/transform.h:472-486). */
+int ctw_prp_set_b(ctw_prp *h, const uint32_t *b, int count);
+
+/* Register 0 of every lane <- a.   Replaces engine::set (cyclo/src/engine.h:231-237). */
+int ctw_prp_set(ctw_prp *h, uint32_t a);
+/* Register dst <- register src.    Replaces engine::copy (cyclo/src/engine.h:240-247). */
+int ctw_prp_copy(ctw_prp *h, int dst, int src);
+/* reg0 <- reg0^2 * base^{bit(lane)}, bit(lane) = bit (lane % 64) of
+ * lane_mask_words[lane / 64].  Asynchronous on the handle's stream.
+ * Replaces engine::squareDup(ln, dup) (cyclo/src/engine.h:387-419). */
+int ctw_prp_square_dup(ctw_prp *h, const uint64_t *lane_mask_words);
+/* reg0 <- reg0 * reg1.   Replaces engine::mul (cyclo/src/engine.h:421-433). */
+int ctw_prp_mul(ctw_prp *h);
+/* reg_out <- reg_a * reg_b (registers 0..2; reg_out may equal reg_a or reg_b). */
+int ctw_prp_mul_regs(ctw_prp *h, int reg_out, int reg_a, int reg_b);
+/* reg0 <- reg0^(2^count) * base^(bits of e), processing bit i_hi down to
+ * i_hi - count + 1 of each lane's exponent e (little-endian 32-bit words,
+ * nwords per lane, lanes * nwords words in total).  One launch, the residue
+ * stays in shared memory between squarings. */
+int ctw_prp_square_bits(ctw_prp *h, const uint32_t *e_words, int nwords, long long i_hi, int count);
+
+/* Canonical digits (each in [0, b)) of register reg for every lane: out has
+ * lanes * D entries, lane-major.  Blocks until the stream is idle.
+ * Replaces transform::getInt (cyclo/src/transform.h:501-597). */
+int ctw_prp_get_digits(ctw_prp *h, int reg, uint32_t *out);
+/* PRP flag and RES64 (sum x_j b^j mod 2^64) of register reg per lane; returns
+ * CTW_E_COMPUTE if a lane's residue is zero.
+ * Replaces transform::isPrime (cyclo/src/transform.h:600-636). */
+int ctw_prp_is_prime(ctw_prp *h, int reg, uint8_t *is_prp, uint64_t *res64);
+/* Raw register digits (signed, as the device keeps them), lanes * D int32 per
+ * register, registers first..first+nregs-1.  Context save/restore
+ * (cyclo/src/transform.h:445-468 keeps the same digits as RNS residues). */
+int ctw_prp_read_regs(ctw_prp *h, int first, int nregs, int32_t *out);
+int ctw_prp_write_regs(ctw_prp *h, int first, int nregs, const int32_t *in);
+
+/* Whole Fermat test of `count` (<= lanes) candidates of this degree, including
+ * the Gerbicz-Li check, as cyclo::check(b) (cyclo/src/cyclo.h:252-377).
+ * Lanes past count repeat the last b (cyclo/src/cyclo.h:233-236).
+ * Outputs per candidate: is_prp, res64, gl_ok (1 = Gerbicz-Li passed). */
+int ctw_prp_run(ctw_prp *h, const uint32_t *b, int count, uint8_t *is_prp, uint64_t *res64, uint8_t *gl_ok);
+
+/* Block until all work queued on the handle's stream is done. */
+int ctw_prp_sync(ctw_prp *h);
+/* The handle's cudaStream_t (as void *), for event timing by the caller. */
+void *ctw_prp_stream(ctw_prp *h);
+/* Launch geometry chosen for this degree: CTAs per lane (cluster size),
+ * threads per CTA, dynamic shared memory per CTA in bytes. */
+int ctw_prp_geometry(ctw_prp *h, int *ctas_per_lane, int *threads, int *smem_bytes);
+/* Kernel launches issued by this handle since creation. */
+long long ctw_prp_launches(ctw_prp *h);
+
+/* Measured 32-bit integer multiply-add throughput of the device (IMAD/s),
+ * from an in-library probe kernel; the roofline denominator. */
+double ctw_imad_peak(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CTWIN_GB300_H */

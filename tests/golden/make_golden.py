@@ -1,0 +1,124 @@
+"""Generate the golden fixtures under tests/golden/ (run once, in a container that
+has the reference source; the outputs are committed, the GPU tests only read them).
+
+  algo_kat.json     known-answer squares mod X^n - X^{n/2} + 1 for n = 8, 16, parsed
+                    from the reference's own check strings (cyclo/algo/algo.cpp:173-177)
+  sieve_ref.npz     survivor bitmaps + last p of the reference CPU sieve itself
+                    (sieve/CPU/ctsieve.cpp, compiled unchanged into oracle/_ref/)
+  sieve_files.json  md5 of cand_*.txt / sv_*.dat written by the reference's write(true)
+  prp_gmp.json      GMP Fermat residues (RES64, PRP flag) for base 2 and 3, N+ and N-
+
+Usage:  python tests/golden/make_golden.py [--skip-slow]
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import multiprocessing as mp
+import os
+import re
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+REF = os.environ.get("CTWIN_REFERENCE", "/root/reference")
+
+
+def algo_kat():
+    src = open(os.path.join(REF, "cyclo", "algo", "algo.cpp")).read()
+    out = {}
+    for n, rhs in re.findall(r'check\((\d+),\s*"\s*=\s*([^"]+)"\)', src):
+        n = int(n)
+        coeffs = [0] * n
+        for sign, mag, power in re.findall(r'([+-]?)\s*(\d+)(\*x(?:\^\d+)?)?', rhs.replace(" ", "")):
+            e = 0 if not power else (1 if power == "*x" else int(power.split("^")[1]))
+            coeffs[e] = -int(mag) if sign == "-" else int(mag)
+        out[str(n)] = coeffs
+    return out
+
+
+SIEVE_CASES = [
+    # name, n, b_min, b_max(inclusive), p_max_pos, p_max_neg, mode
+    ("cfg1_pos", 11, 100000, 299999, 2 ** 32, 11, 1),
+    ("cfg1_twin", 11, 100000, 299999, 2 ** 32, 2 ** 32, 0),
+    ("n8_small", 8, 2, 20000, 10 ** 7, 10 ** 6, 0),
+    ("n9_small", 9, 2, 3, 10 ** 6, 10 ** 6, 0),
+    ("n10_mid", 10, 50000, 70000, 2 ** 34, 2 ** 28, 0),
+    ("n12_pos", 12, 2, 200000, 2 ** 36, 11, 1),
+    ("n14_pos", 14, 123456, 223455, 2 ** 36, 11, 1),
+    ("n16_pos", 16, 2, 65537, 2 ** 36, 11, 1),
+    ("n20_pos_s0", 20, 2, 2 ** 16, 2 ** 36, 11, 1),
+]
+
+
+def run_sieve_case(case):
+    from oracle import oracle as O
+    name, n, bmin, bmax, pp, pn, mode = case
+    tmp = tempfile.mkdtemp()
+    r = O.ref_sieve(n, bmin, bmax, pp, pn, mode, write_dir=tmp)
+    files = {}
+    for f in os.listdir(tmp):
+        files[f] = hashlib.md5(open(os.path.join(tmp, f), "rb").read()).hexdigest()
+    return name, r, files
+
+
+def prp_case(args):
+    from oracle import oracle as O
+    b, ln, base, minus = args
+    r, r64, prp = O.fermat(b, ln, base, minus)
+    return {"b": b, "n": ln, "base": base, "form": "-" if minus else "+", "res64": f"{r64:016X}", "prp": bool(prp)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--skip-slow", action="store_true")
+    args = ap.parse_args()
+    from oracle import oracle as O
+    O.build()
+    O.build_ref()
+
+    json.dump(algo_kat(), open(os.path.join(HERE, "algo_kat.json"), "w"), indent=1)
+
+    cases = SIEVE_CASES if not args.skip_slow else [c for c in SIEVE_CASES if c[0] != "cfg1_twin"]
+    with mp.get_context("spawn").Pool(min(8, os.cpu_count() or 1)) as pool:
+        res = pool.map(run_sieve_case, cases)
+    arrays, meta, files = {}, {}, {}
+    for (name, r, fl), case in zip(res, cases):
+        bits, lp, ln_ = r
+        arrays[name] = np.packbits(bits, bitorder="little")
+        meta[name] = {"n": case[1], "b_min": case[2], "b_max": case[3], "p_max_pos": case[4], "p_max_neg": case[5],
+                      "mode": case[6], "p_last_pos": lp, "p_last_neg": ln_, "size": int(bits.size),
+                      "survivors": int((bits == 0).sum())}
+        files[name] = fl
+    np.savez_compressed(os.path.join(HERE, "sieve_ref.npz"), **arrays)
+    json.dump({"cases": meta, "files": files}, open(os.path.join(HERE, "sieve_files.json"), "w"), indent=1)
+
+    # PRP residues: survivors of config 1 (twin list), small-n PRP hunts, base 2 and 3, N+ and N-
+    twin = np.unpackbits(arrays["cfg1_twin"], bitorder="little")[: meta["cfg1_twin"]["size"]] if "cfg1_twin" in arrays else None
+    jobs = []
+    if twin is not None:
+        surv = [100000 + int(i) for i in np.flatnonzero(twin == 0)[:64]]
+        for b in surv:
+            for base in (2, 3):
+                jobs.append((b, 11, base, False))
+            jobs.append((b, 11, 2, True))
+    small = np.unpackbits(arrays["n8_small"], bitorder="little")[: meta["n8_small"]["size"]]
+    s8 = [2 + int(i) for i in np.flatnonzero(small == 0)]
+    for b in s8[:400]:
+        if b >= 64:
+            jobs.append((b, 8, 2, False))
+            jobs.append((b, 8, 3, False))
+            jobs.append((b, 8, 2, True))
+    with mp.get_context("spawn").Pool(min(8, os.cpu_count() or 1)) as pool:
+        prp = pool.map(prp_case, jobs)
+    json.dump(prp, open(os.path.join(HERE, "prp_gmp.json"), "w"), indent=0)
+    print("done", len(prp), "prp cases;", sum(p["prp"] for p in prp), "PRPs")
+
+
+if __name__ == "__main__":
+    main()
