@@ -2,5 +2,6 @@
 modular-root sieve, behind a C ABI (include/ctwin_gb300.h)."""
 from ._native import CtwError, lib
 from .prp import PrpEngine, prp_test
+from .sieve import Sieve, sieve_pass
 
-__all__ = ["CtwError", "lib", "PrpEngine", "prp_test"]
+__all__ = ["CtwError", "lib", "PrpEngine", "prp_test", "Sieve", "sieve_pass"]

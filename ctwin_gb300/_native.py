@@ -57,6 +57,10 @@ def lib() -> ctypes.CDLL:
             "ctw_prp_geometry": ([H, vp, vp, vp], i32),
             "ctw_prp_launches": ([H], i64),
             "ctw_imad_peak": ([], ctypes.c_double),
+            "ctw_sieve_run": ([i32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, i32, vp, vp], i32),
+            "ctw_sieve_write_files": ([i32, ctypes.c_uint64, ctypes.c_uint64, vp, ctypes.c_uint64, ctypes.c_uint64,
+                                       ctypes.c_char_p], i32),
+            "ctw_sieve_launches": ([], i64),
         }
         for name, (args, res) in sigs.items():
             fn = getattr(L, name)

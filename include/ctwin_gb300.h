@@ -110,6 +110,31 @@ long long ctw_prp_launches(ctw_prp *h);
  * from an in-library probe kernel; the roofline denominator. */
 double ctw_imad_peak(void);
 
+/* ------------------------------------------------------------------------ */
+/* Sieve: strike b in [b_min, b_max] with p | b^(2^n) - b^(2^(n-1)) +- 1      */
+/* ------------------------------------------------------------------------ */
+
+/* One sieve pass over the primes of one form:
+ *   mode +1: p = 3k*2^n + 1 (Sieve::check_pos, sieve/CPU/ctsieve.cpp:678-726;
+ *            GPU kernels sieve/GPU/ocl/kernel.cl:243-320),
+ *   mode -1: p = 10k +- 1   (Sieve::check_neg, sieve/CPU/ctsieve.cpp:728-787;
+ *            GPU kernels sieve/GPU/ocl/kernel.cl:328-479).
+ * The k range is the reference's: k from p_min/(3*2^n) (resp. p_min/10) up to
+ * the first k whose p reaches p_max (ctsieve.cpp:682-684, 733-735).
+ * struck_words: in/out bitmap, bit i (word i/32, bit i%32) set when b_min + i
+ * is struck; existing bits are kept (two calls, + then -, give the reference's
+ * "ini" list).  *p_last: in/out, raised to the last p the reference would have
+ * processed (its _p_min_pos / _p_min_neg, written to sv_*.dat).
+ * 8 <= n <= 24, 2 <= b_min <= b_max, p_max < 2^62. */
+int ctw_sieve_run(int n, uint64_t b_min, uint64_t b_max, uint64_t p_min, uint64_t p_max, int mode,
+                  uint32_t *struck_words, uint64_t *p_last);
+/* Write sv_<n>_<b_min>_<b_max>.dat and cand_<n>_<b_min>_<b_max>.txt into dir,
+ * byte-identical to Sieve::write(true) (sieve/CPU/ctsieve.cpp:591-626). */
+int ctw_sieve_write_files(int n, uint64_t b_min, uint64_t b_max, const uint32_t *struck_words,
+                          uint64_t p_min_pos, uint64_t p_min_neg, const char *dir);
+/* Sieve kernel launches issued by this process. */
+long long ctw_sieve_launches(void);
+
 #ifdef __cplusplus
 }
 #endif
