@@ -47,6 +47,8 @@ def lib() -> ctypes.CDLL:
             "ctw_prp_mul": ([H], i32),
             "ctw_prp_mul_regs": ([H, i32, i32, i32], i32),
             "ctw_prp_square_bits": ([H, vp, i32, i64, i32], i32),
+            "ctw_prp_load_exponent": ([H, vp, i32], i32),
+            "ctw_prp_square_resident": ([H, i64, i32], i32),
             "ctw_prp_get_digits": ([H, i32, vp], i32),
             "ctw_prp_is_prime": ([H, i32, vp, vp], i32),
             "ctw_prp_read_regs": ([H, i32, i32, vp], i32),

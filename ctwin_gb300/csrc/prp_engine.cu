@@ -73,6 +73,8 @@ struct ctw_prp {
 	uint32_t *d_laneb = nullptr;      // [lanes][4]
 	uint32_t *d_bits = nullptr;
 	size_t bits_cap = 0;
+	uint32_t *d_exp = nullptr;        // resident exponent words [lanes][exp_nwords]
+	int exp_nwords = 0;
 	uint32_t *d_status = nullptr;
 	std::vector<uint32_t> b;
 	PrpKernelArgs proto{};
@@ -371,6 +373,7 @@ int ctw_prp_destroy(ctw_prp *h)
 	cudaFree(h->d_ti);
 	cudaFree(h->d_laneb);
 	cudaFree(h->d_bits);
+	cudaFree(h->d_exp);
 	cudaFree(h->d_status);
 	if (h->stream) cudaStreamDestroy(h->stream);
 	delete h;
@@ -470,6 +473,30 @@ int ctw_prp_square_bits(ctw_prp *h, const uint32_t *e_words, int nwords, long lo
 	CTW_CUDA(cudaMemcpyAsync(h->d_bits, e_words, words * 4, cudaMemcpyHostToDevice, h->stream));
 	CTW_CUDA(cudaStreamSynchronize(h->stream));   // e_words may be reused by the caller
 	return op_square_bits(h, h->d_bits, nwords, i_hi, count);
+}
+
+int ctw_prp_load_exponent(ctw_prp *h, const uint32_t *e_words, int nwords)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (!e_words || nwords < 1) return fail(CTW_E_ARG, "bad exponent arguments");
+	const size_t words = (size_t)h->lanes * nwords;
+	CTW_CUDA(cudaStreamSynchronize(h->stream));
+	cudaFree(h->d_exp);
+	h->d_exp = nullptr;
+	h->exp_nwords = 0;
+	CTW_CUDA(cudaMalloc(&h->d_exp, words * 4));
+	CTW_CUDA(cudaMemcpy(h->d_exp, e_words, words * 4, cudaMemcpyHostToDevice));
+	h->exp_nwords = nwords;
+	return CTW_OK;
+}
+
+int ctw_prp_square_resident(ctw_prp *h, long long i_hi, int count)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (!h->d_exp) return fail(CTW_E_ARG, "no resident exponent (ctw_prp_load_exponent)");
+	if (count < 0) return fail(CTW_E_ARG, "negative count");
+	if (count == 0) return CTW_OK;
+	return op_square_bits(h, h->d_exp, h->exp_nwords, i_hi, count);
 }
 
 int ctw_prp_get_digits(ctw_prp *h, int reg, uint32_t *out)

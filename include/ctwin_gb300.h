@@ -75,6 +75,11 @@ int ctw_prp_mul_regs(ctw_prp *h, int reg_out, int reg_a, int reg_b);
  * nwords per lane, lanes * nwords words in total).  One launch, the residue
  * stays in shared memory between squarings. */
 int ctw_prp_square_bits(ctw_prp *h, const uint32_t *e_words, int nwords, long long i_hi, int count);
+/* Upload the per-lane exponents once (lanes * nwords words) and keep them in
+ * device memory; ctw_prp_square_resident then squares over bits i_hi down to
+ * i_hi - count + 1 of that resident copy without any host transfer. */
+int ctw_prp_load_exponent(ctw_prp *h, const uint32_t *e_words, int nwords);
+int ctw_prp_square_resident(ctw_prp *h, long long i_hi, int count);
 
 /* Canonical digits (each in [0, b)) of register reg for every lane: out has
  * lanes * D entries, lane-major.  Blocks until the stream is idle.
