@@ -111,6 +111,24 @@ int ctw_prp_geometry(ctw_prp *h, int *ctas_per_lane, int *threads, int *smem_byt
 /* Kernel launches issued by this handle since creation. */
 long long ctw_prp_launches(ctw_prp *h);
 
+/* z = x * y for `lanes` candidates of degree D = 2^log2_degree (8..14), with
+ * x, y, z caller-owned DEVICE buffers of lanes * D int32 digits (the register
+ * format of ctw_prp_read_regs) and b[lanes] on the host; the result is the one
+ * ctw_prp_mul_regs gives.  No counterpart in the reference.
+ * For callers that must not allocate device memory (a host that reserved the
+ * GPU's memory for itself, a pooling allocator that forbids cudaMalloc, a
+ * pipeline that cannot take cudaMalloc's device-wide synchronisation): it
+ * allocates nothing and uses fixed __device__ arrays the library holds on every
+ * GPU until exit (4 MiB scratch, so lanes * 12 * D <= 4 MiB and lanes <= 1024;
+ * larger requests fail with CTW_E_ARG).  Calls share those arrays: calls that
+ * overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller.  The first call on each device sets the arrays up
+ * (symbol addresses, root tables) and should come before any stream capture.
+ * Runs on `stream` (a cudaStream_t, NULL = default) and returns after it has
+ * synchronised the stream. */
+int ctw_prp_mul_noalloc(int log2_degree, int lanes, const uint32_t *b, const int32_t *x_dev,
+                        const int32_t *y_dev, int32_t *z_dev, int csize, void *stream);
+
 /* Measured 32-bit integer multiply-add throughput of the device (IMAD/s),
  * from an in-library probe kernel; the roofline denominator. */
 double ctw_imad_peak(void);
