@@ -12,6 +12,7 @@
 #include "bignum.h"
 #include "prp_arith.cuh"
 #include "prp_kernels.cuh"
+#include "prp_tables.h"
 
 namespace ctw {
 
@@ -35,41 +36,23 @@ int fail(int code, const char *fmt, ...)
 		                                   __FILE__, __LINE__);                                              \
 	} while (0)
 
-// ---- host modular arithmetic for table generation ----
-static uint32_t mulmod(uint32_t a, uint32_t b, uint32_t q) { return (uint32_t)(((uint64_t)a * b) % q); }
-static uint32_t powmod(uint32_t a, uint64_t e, uint32_t q)
-{
-	uint32_t r = 1 % q;
-	while (e) { if (e & 1) r = mulmod(r, a, q); a = mulmod(a, a, q); e >>= 1; }
-	return r;
-}
-static uint32_t invmod(uint32_t a, uint32_t q) { return powmod(a, q - 2, q); }
-static uint32_t mont(uint32_t a, uint32_t q) { return (uint32_t)((((uint64_t)a) << 32) % q); }
-static size_t bitrev(size_t j, size_t s)
-{
-	size_t r = 0;
-	for (size_t k = s; k > 1; k >>= 1, j >>= 1) r = (r << 1) | (j & 1);
-	return r;
-}
-
-static const uint32_t kQ[3] = { Q0, Q1, Q2 };
-static const uint32_t kGen[3] = { QGEN0, QGEN1, QGEN2 };
-
 }  // namespace ctw
 
 using namespace ctw;
 
 struct ctw_prp {
-	int ln = 0, lanes = 0, lg = 0, lm = 0, csize = 16;
+	int ln = 0, lanes = 0, lg = 0, lm = 0, csize = 8;
 	uint32_t base = 2;
 	size_t D = 0, M = 0, G = 1;
 	int threads = 0;
 	size_t smem = 0;
 	int tw_smem = 0;
+	int narrow = 0;                   // 64-bit carry arithmetic is exact for the current b
 	cudaStream_t stream = nullptr;
 	int32_t *d_regs = nullptr;        // [3][lanes][D]
 	uint32_t *d_scratch = nullptr;    // [lanes][G][3][M]
 	uint32_t *d_tf = nullptr, *d_ti = nullptr;
+	uint32_t *d_tfs = nullptr, *d_tis = nullptr;
 	uint32_t *d_laneb = nullptr;      // [lanes][4]
 	uint32_t *d_bits = nullptr;
 	size_t bits_cap = 0;
@@ -91,51 +74,24 @@ int check_handle(ctw_prp *h)
 	return CTW_OK;
 }
 
-// Roots of the ring X^D - X^{D/2} + 1 (the reference's ordering,
-// cyclo/src/transform.h:336-368): level s (s blocks), block j uses
-// r_{6s}^{3*bitrev(j,s) + 1 + floor(2j/s)}, r_{6s} a primitive 6s-th root.
+// Root tables and launch constants (prp_tables.h), uploaded once per handle.
 int build_tables(ctw_prp *h)
 {
-	const size_t D = h->D, M = h->M, G = h->G;
-	std::vector<uint32_t> tf(G * 3 * M, 0), ti(G * 3 * M, 0);
-	for (int pi = 0; pi < 3; ++pi)
-	{
-		const uint32_t q = kQ[pi];
-		std::vector<uint32_t> W(D, 0);
-		for (size_t s = 1; s < D; s *= 2)
-		{
-			const uint32_t rs = powmod(kGen[pi], (q - 1) / (6 * (uint64_t)s), q);
-			for (size_t j = 0; j < s; ++j) W[s + j] = powmod(rs, 3 * bitrev(j, s) + 1 + (2 * j) / s, q);
-		}
-		// local levels l: global level LG + l, block g*2^l + j'
-		for (size_t g = 0; g < G; ++g)
-			for (int l = 0; l < h->lm; ++l)
-				for (size_t jp = 0; jp < ((size_t)1 << l); ++jp)
-				{
-					const uint32_t w = W[(G << l) + (g << l) + jp];
-					tf[(g * 3 + pi) * M + ((size_t)1 << l) + jp] = mont(w, q);
-					ti[(g * 3 + pi) * M + ((size_t)1 << l) + jp] = mont(invmod(w, q), q);
-				}
-		for (size_t k = 1; k < G; ++k)
-		{
-			h->proto.tcf[pi][k] = mont(W[k], q);
-			h->proto.tci[pi][k] = mont(invmod(W[k], q), q);
-		}
-		const uint32_t w1 = W[1];
-		const uint32_t S = mulmod((uint32_t)(((uint64_t)1 << 32) % q), mulmod(2, invmod((uint32_t)(D % q), q), q), q);
-		const uint32_t K1 = mulmod(S, invmod((mulmod(2, w1, q) + q - 1) % q, q), q);
-		h->proto.omega[pi] = mont(w1, q);
-		h->proto.sc[pi] = mont(S, q);
-		h->proto.k1[pi] = mont(K1, q);
-	}
-	h->proto.ginv[0] = mont(invmod(Q2 % Q1, Q1), Q1);
-	h->proto.ginv[1] = mont(invmod(Q2 % Q0, Q0), Q0);
-	h->proto.ginv[2] = mont(invmod(Q1 % Q0, Q0), Q0);
-	const size_t bytes = G * 3 * M * sizeof(uint32_t);
+	const size_t words = h->G * 3 * h->M, swords = h->G * 3 * 256 * 2;
+	std::vector<uint32_t> tf(words), ti(words), tfs(swords), tis(swords);
+	prp_build_tables(h->ln, tf.data(), ti.data(), h->proto, tfs.data(), tis.data());
+	const size_t bytes = words * sizeof(uint32_t);
 	CTW_CUDA(cudaMalloc(&h->d_tf, bytes));
 	CTW_CUDA(cudaMalloc(&h->d_ti, bytes));
 	CTW_CUDA(cudaMemcpy(h->d_tf, tf.data(), bytes, cudaMemcpyHostToDevice));
 	CTW_CUDA(cudaMemcpy(h->d_ti, ti.data(), bytes, cudaMemcpyHostToDevice));
+	if (h->lm == 12)
+	{
+		CTW_CUDA(cudaMalloc(&h->d_tfs, swords * 4));
+		CTW_CUDA(cudaMalloc(&h->d_tis, swords * 4));
+		CTW_CUDA(cudaMemcpy(h->d_tfs, tfs.data(), swords * 4, cudaMemcpyHostToDevice));
+		CTW_CUDA(cudaMemcpy(h->d_tis, tis.data(), swords * 4, cudaMemcpyHostToDevice));
+	}
 	return CTW_OK;
 }
 
@@ -144,12 +100,15 @@ PrpKernelArgs make_args(ctw_prp *h)
 	PrpKernelArgs a = h->proto;
 	a.tf = h->d_tf;
 	a.ti = h->d_ti;
+	a.tfs = h->d_tfs;
+	a.tis = h->d_tis;
 	a.lane_b = h->d_laneb;
 	a.status = h->d_status;
 	a.lm = h->lm;
 	a.csize = h->csize;
 	a.mult = (int)h->base;
 	a.tw_smem = h->tw_smem;
+	a.narrow = h->narrow;
 	a.scratch = h->d_scratch;
 	return a;
 }
@@ -334,13 +293,13 @@ int ctw_prp_create(int log2_degree, int lanes, ctw_prp **out)
 	ctw_prp *h = new ctw_prp();
 	h->ln = log2_degree;
 	h->lanes = lanes;
-	h->lg = log2_degree > 12 ? std::min(log2_degree - 12, MAX_LG) : 0;
+	h->lg = prp_lg_for(log2_degree);
 	h->lm = log2_degree - h->lg;
 	h->D = (size_t)1 << log2_degree;
 	h->G = (size_t)1 << h->lg;
 	h->M = h->D / h->G;
-	h->tw_smem = prp_smem_bytes(h->lm, 1) <= 227 * 1024 ? 1 : 0;
-	h->smem = prp_smem_bytes(h->lm, h->tw_smem);
+	h->tw_smem = prp_smem_bytes(h->lm, h->lg, 1) <= 227 * 1024 ? 1 : 0;
+	h->smem = prp_smem_bytes(h->lm, h->lg, h->tw_smem);
 	h->threads = prp_threads(h->lm);
 	h->b.assign((size_t)lanes, 0);
 	int rc = CTW_OK;
@@ -371,6 +330,8 @@ int ctw_prp_destroy(ctw_prp *h)
 	cudaFree(h->d_scratch);
 	cudaFree(h->d_tf);
 	cudaFree(h->d_ti);
+	cudaFree(h->d_tfs);
+	cudaFree(h->d_tis);
 	cudaFree(h->d_laneb);
 	cudaFree(h->d_bits);
 	cudaFree(h->d_exp);
@@ -402,8 +363,10 @@ int ctw_prp_set_b(ctw_prp *h, const uint32_t *b, int count)
 	if (int rc = check_handle(h)) return rc;
 	if (!b || count != h->lanes) return fail(CTW_E_ARG, "set_b expects lanes (%d) values", h->lanes);
 	std::vector<uint32_t> lb((size_t)h->lanes * 4);
+	uint32_t bmax = 0;
 	for (int l = 0; l < h->lanes; ++l)
 	{
+		bmax = std::max(bmax, b[l]);
 		const uint32_t bl = b[l];
 		if (bl < 64 || bl >= 0x80000000u) return fail(CTW_E_ARG, "b = %u outside [64, 2^31)", bl);
 		const int s = (31 - __builtin_clz(bl)) - 1;
@@ -413,6 +376,8 @@ int ctw_prp_set_b(ctw_prp *h, const uint32_t *b, int count)
 		lb[4 * l + 3] = 0;
 		h->b[(size_t)l] = bl;
 	}
+	// |coefficient| <= 1.5 D b^2, accumulated x3 plus carries: 64-bit when 8 D b^2 < 2^62
+	h->narrow = (8.0 * (double)h->D * (double)bmax * (double)bmax < 4.611686018427388e18) ? 1 : 0;
 	CTW_CUDA(cudaMemcpyAsync(h->d_laneb, lb.data(), lb.size() * 4, cudaMemcpyHostToDevice, h->stream));
 	CTW_CUDA(cudaStreamSynchronize(h->stream));
 	return CTW_OK;

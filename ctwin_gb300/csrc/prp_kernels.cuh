@@ -18,6 +18,8 @@ struct PrpKernelArgs {
 	uint32_t *scratch;          // [lanes][G][3][M] transform of y (OP_MUL)
 	const uint32_t *tf;         // [3][G][M] local forward roots (Montgomery form)
 	const uint32_t *ti;         // [3][G][M] local inverse roots
+	const uint32_t *tfs;        // [G][3][256][2] (w, floor(w 2^32/q)) roots of local levels 0..7 (M = 4096 only)
+	const uint32_t *tis;        // the same for the inverse roots
 	const uint32_t *lane_b;     // [lanes][4] = b, floor(2^(s+32)/b), s = ilog2(b)-1, 0
 	const uint32_t *bits;       // [lanes][nwords] exponent bits
 	uint32_t *status;           // error flags (0 = ok)
@@ -29,12 +31,17 @@ struct PrpKernelArgs {
 	int mult;                   // multiplier applied when a bit is set (2 = base 2, 3 = base 3)
 	int op;
 	int tw_smem;                // 1: copy the local roots into shared memory
+	int swz_b;                  // swizzle selector of the shared planes (prp_swizzle_bit)
+	int scols;                  // columns per staging round of the cross-CTA levels
+	int narrow;                 // 1: |coefficients| * 3 + carries < 2^62, carry in 64-bit arithmetic
 	uint32_t omega[3];          // 6th root w1 (Montgomery form)
 	uint32_t k1[3];             // S / (2 w1 - 1)
 	uint32_t sc[3];             // S = 2^32 * 2 / D   (Montgomery form)
 	uint32_t ginv[3];           // Garner: q2^-1 mod q1, q2^-1 mod q0, q1^-1 mod q0 (Montgomery forms)
-	uint32_t tcf[3][MAX_G];     // cross-CTA forward roots w[1..G-1]
-	uint32_t tci[3][MAX_G];     // cross-CTA inverse roots
+	uint32_t tcf[3][MAX_G];     // cross-CTA forward roots w[1..G-1], plain
+	uint32_t tcfq[3][MAX_G];    // their Shoup quotients floor(w 2^32 / q)
+	uint32_t tci[3][MAX_G];     // cross-CTA inverse roots, plain
+	uint32_t tciq[3][MAX_G];
 	int use_dupmask;            // 1: the bit of lane l is bit l of dupmask (count == 1)
 	uint64_t dupmask[MAX_INLINE_LANES / 64];
 };
@@ -45,7 +52,9 @@ enum PrpStatus : uint32_t {
 	ST_DIGIT_RANGE = 2,         // a digit left the int32 range
 };
 
-size_t prp_smem_bytes(int lm, int tw_smem);
+size_t prp_smem_bytes(int lm, int lg, int tw_smem);
+// Words of the Shoup root tables of one CTA (both directions), 0 unless M = 4096.
+inline size_t prp_shoup_words(int lm) { return lm == 12 ? 2 * 3 * 256 * 2 : 0; }
 int prp_threads(int lm);
 cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t stream);
 

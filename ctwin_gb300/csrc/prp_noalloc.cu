@@ -10,7 +10,7 @@
 // engine's multiply without any allocation: the scratch, the root tables of
 // every supported degree, the per-lane parameters and the status word live in
 // the file-scope __device__ arrays below, which every GPU that loads the
-// library holds until the process exits (about 4.8 MiB in total).
+// library holds until the process exits (about 4.9 MiB in total).
 #include <cstring>
 #include <mutex>
 
@@ -19,6 +19,7 @@
 #include "../../include/ctwin_gb300.h"
 #include "prp_arith.cuh"
 #include "prp_kernels.cuh"
+#include "prp_tables.h"
 
 namespace ctw {
 int fail(int code, const char *fmt, ...);
@@ -31,8 +32,11 @@ namespace {
 constexpr int NA_MIN_LN = 8, NA_MAX_LN = 14;
 constexpr size_t NA_SCRATCH_BYTES = size_t(4) << 20;   // transform of the second operand
 constexpr int NA_MAX_LANES = 1024;
-// forward + inverse roots, [G][3][M] = 3*D words each, for every degree 2^8..2^14
-constexpr size_t NA_TABLE_WORDS = 6 * ((size_t(1) << (NA_MAX_LN + 1)) - (size_t(1) << NA_MIN_LN));
+// forward + inverse roots, [G][3][M] = 3*D words each, for every degree 2^8..2^14,
+// then the Shoup tables [G][3][256][2] of both directions for degrees 2^12..2^14
+constexpr size_t NA_MAIN_WORDS = 6 * ((size_t(1) << (NA_MAX_LN + 1)) - (size_t(1) << NA_MIN_LN));
+constexpr size_t NA_SHOUP_WORDS = (1 + 2 + 4) * 2 * 3 * 256 * 2;
+constexpr size_t NA_TABLE_WORDS = NA_MAIN_WORDS + NA_SHOUP_WORDS;
 constexpr int NA_MAX_DEVICES = 64;
 
 static __device__ __align__(256) uint32_t g_na_scratch[NA_SCRATCH_BYTES / 4];
@@ -56,70 +60,12 @@ size_t na_table_offset(int ln)
 	return off;
 }
 
-uint32_t na_mulmod(uint32_t a, uint32_t b, uint32_t q) { return (uint32_t)(((uint64_t)a * b) % q); }
-uint32_t na_pow(uint32_t a, uint64_t e, uint32_t q)
+// Shoup tables of degree 2^ln (12 <= ln <= 14): forward at the offset, inverse after it.
+size_t na_shoup_offset(int ln)
 {
-	uint32_t r = 1 % q;
-	while (e) { if (e & 1) r = na_mulmod(r, a, q); a = na_mulmod(a, a, q); e >>= 1; }
-	return r;
-}
-uint32_t na_inv(uint32_t a, uint32_t q) { return na_pow(a, q - 2, q); }
-uint32_t na_mont(uint32_t a, uint32_t q) { return (uint32_t)(((uint64_t)a << 32) % q); }
-size_t na_bitrev(size_t j, size_t s)
-{
-	size_t r = 0;
-	for (size_t k = s; k > 1; k >>= 1, j >>= 1) r = (r << 1) | (j & 1);
-	return r;
-}
-
-// Roots of X^D - X^{D/2} + 1 for one degree, written into the host staging
-// area, and the per-degree launch constants.  Same ring decomposition as the
-// handle-based engine: level s, block j uses r_{6s}^{3*bitrev(j,s)+1+floor(2j/s)}.
-void na_build_degree(int ln, PrpKernelArgs &proto)
-{
-	static const uint32_t kQ[3] = { Q0, Q1, Q2 };
-	static const uint32_t kG[3] = { QGEN0, QGEN1, QGEN2 };
-	const size_t D = size_t(1) << ln;
-	const int lg = ln > 12 ? (ln - 12 < MAX_LG ? ln - 12 : MAX_LG) : 0;
-	const size_t G = size_t(1) << lg, M = D / G;
-	const int lm = ln - lg;
-	uint32_t *tf = g_na_host_tables + na_table_offset(ln), *ti = tf + 3 * D;
-	memset(tf, 0, 6 * D * sizeof(uint32_t));
-	memset(&proto, 0, sizeof(proto));
-	for (int pi = 0; pi < 3; ++pi)
-	{
-		const uint32_t q = kQ[pi];
-		auto W = [&](size_t idx) -> uint32_t {   // root w[idx], idx = s + j
-			size_t s = 1;
-			while (s * 2 <= idx) s *= 2;
-			const size_t j = idx - s;
-			const uint32_t rs = na_pow(kG[pi], (q - 1) / (6 * (uint64_t)s), q);
-			return na_pow(rs, 3 * na_bitrev(j, s) + 1 + (2 * j) / s, q);
-		};
-		for (size_t g = 0; g < G; ++g)
-			for (int l = 0; l < lm; ++l)
-				for (size_t jp = 0; jp < (size_t(1) << l); ++jp)
-				{
-					const uint32_t w = W((G << l) + (g << l) + jp);
-					tf[(g * 3 + pi) * M + (size_t(1) << l) + jp] = na_mont(w, q);
-					ti[(g * 3 + pi) * M + (size_t(1) << l) + jp] = na_mont(na_inv(w, q), q);
-				}
-		for (size_t k = 1; k < G; ++k)
-		{
-			proto.tcf[pi][k] = na_mont(W(k), q);
-			proto.tci[pi][k] = na_mont(na_inv(W(k), q), q);
-		}
-		const uint32_t w1 = W(1);
-		const uint32_t S = na_mulmod((uint32_t)(((uint64_t)1 << 32) % q), na_mulmod(2, na_inv((uint32_t)(D % q), q), q), q);
-		const uint32_t K1 = na_mulmod(S, na_inv((na_mulmod(2, w1, q) + q - 1) % q, q), q);
-		proto.omega[pi] = na_mont(w1, q);
-		proto.sc[pi] = na_mont(S, q);
-		proto.k1[pi] = na_mont(K1, q);
-	}
-	proto.ginv[0] = na_mont(na_inv(Q2 % Q1, Q1), Q1);
-	proto.ginv[1] = na_mont(na_inv(Q2 % Q0, Q0), Q0);
-	proto.ginv[2] = na_mont(na_inv(Q1 % Q0, Q0), Q0);
-	proto.lm = lm;
+	size_t off = NA_MAIN_WORDS;
+	for (int k = 12; k < ln; ++k) off += (size_t(1) << (k - 12)) * 2 * 3 * 256 * 2;
+	return off;
 }
 
 // One-time set-up of the current device: device addresses of the file-scope
@@ -134,7 +80,19 @@ int na_setup(int dev)
 	    (e = cudaGetSymbolAddress((void **)&d.laneb, g_na_laneb)) != cudaSuccess ||
 	    (e = cudaGetSymbolAddress((void **)&d.status, g_na_status)) != cudaSuccess)
 		return fail(CTW_E_CUDA, "no-alloc set-up: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-	for (int ln = NA_MIN_LN; ln <= NA_MAX_LN; ++ln) na_build_degree(ln, d.proto[ln]);
+	for (int ln = NA_MIN_LN; ln <= NA_MAX_LN; ++ln)
+	{
+		uint32_t *tf = g_na_host_tables + na_table_offset(ln);
+		memset(&d.proto[ln], 0, sizeof(PrpKernelArgs));
+		uint32_t *tfs = nullptr, *tis = nullptr;
+		if (ln >= 12)
+		{
+			const size_t G = size_t(1) << (ln - 12);
+			tfs = g_na_host_tables + na_shoup_offset(ln);
+			tis = tfs + G * 3 * 256 * 2;
+		}
+		prp_build_tables(ln, tf, tf + 3 * (size_t(1) << ln), d.proto[ln], tfs, tis);
+	}
 	if ((e = cudaMemcpy(d.tables, g_na_host_tables, sizeof(g_na_host_tables), cudaMemcpyHostToDevice)) != cudaSuccess)
 		return fail(CTW_E_CUDA, "no-alloc set-up: table upload: %s", cudaGetErrorString(e));
 	d.ready = true;
@@ -155,8 +113,10 @@ extern "C" int ctw_prp_mul_noalloc(int log2_degree, int lanes, const uint32_t *b
 	if (csize != 8 && csize != 16 && csize != 32 && csize != 64) return fail(CTW_E_ARG, "csize %d not in {8,16,32,64}", csize);
 	if (!b || !x_dev || !y_dev || !z_dev) return fail(CTW_E_ARG, "ctw_prp_mul_noalloc: null pointer");
 	uint32_t lb[NA_MAX_LANES * 4];
+	uint32_t bmax = 0;
 	for (int l = 0; l < lanes; ++l)
 	{
+		if (b[l] > bmax) bmax = b[l];
 		if (b[l] < 64 || b[l] >= 0x80000000u) return fail(CTW_E_ARG, "b = %u outside [64, 2^31)", b[l]);
 		const int s = (31 - __builtin_clz(b[l])) - 1;
 		lb[4 * l + 0] = b[l];
@@ -180,12 +140,18 @@ extern "C" int ctw_prp_mul_noalloc(int log2_degree, int lanes, const uint32_t *b
 	PrpKernelArgs a = proto;
 	a.tf = d->tables + na_table_offset(log2_degree);
 	a.ti = a.tf + 3 * D;
+	if (log2_degree >= 12)
+	{
+		a.tfs = d->tables + na_shoup_offset(log2_degree);
+		a.tis = a.tfs + ((size_t)1 << (log2_degree - 12)) * 3 * 256 * 2;
+	}
 	a.lane_b = d->laneb;
 	a.status = d->status;
 	a.scratch = d->scratch;
 	a.csize = csize;
 	a.mult = 2;
-	a.tw_smem = prp_smem_bytes(proto.lm, 1) <= 227 * 1024 ? 1 : 0;
+	a.tw_smem = prp_smem_bytes(proto.lm, lg, 1) <= 227 * 1024 ? 1 : 0;
+	a.narrow = (8.0 * (double)D * (double)bmax * (double)bmax < 4.611686018427388e18) ? 1 : 0;
 	a.op = OP_MUL;
 	a.reg_in = x_dev;
 	a.reg_y = y_dev;

@@ -18,7 +18,7 @@ from ._native import check, lib, ptr
 class PrpEngine:
     """Fermat-test engine for `lanes` candidates of degree D = 2^log2_degree."""
 
-    def __init__(self, log2_degree: int, lanes: int = 1, csize: int = 16, base: int = 2):
+    def __init__(self, log2_degree: int, lanes: int = 1, csize: int = 8, base: int = 2):
         h = ctypes.c_void_p()
         check(lib().ctw_prp_create(log2_degree, lanes, ctypes.byref(h)))
         self._h = h
@@ -146,7 +146,7 @@ class PrpEngine:
         return int(lib().ctw_prp_launches(self._h))
 
 
-def prp_test(b_values, n: int, base: int = 2, lanes: int | None = None, csize: int = 16):
+def prp_test(b_values, n: int, base: int = 2, lanes: int | None = None, csize: int = 8):
     """Fermat-test b^(2^n) - b^(2^(n-1)) + 1 for every b: list of (b, is_prp, res64, gl_ok)."""
     b_values = [int(x) for x in b_values]
     lanes = lanes or min(64, max(1, len(b_values)))

@@ -48,7 +48,7 @@ int ctw_prp_destroy(ctw_prp *h);
 
 /* Carry chunk size, 8/16/32/64 (the reference's CSIZE, autotuned there,
  * cyclo/src/transform.h:383-419).  Register digits depend on it; canonical
- * results do not.  Default 16. */
+ * results do not.  Default 8. */
 int ctw_prp_set_csize(ctw_prp *h, int csize);
 /* Base of the Fermat test: 2 (the reference) or 3.  Sets the multiplier that
  * square_dup applies for a set bit.  Default 2. */
