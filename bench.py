@@ -15,7 +15,19 @@ work cyclo::check does between two checkpoints (cyclo/src/cyclo.h:277-308).
   cpu_baseline  the oracle's C restatement of the reference transform (the
          reference has no CPU PRP path), one candidate per host core
 
-python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Two more workloads print their own line (not the default):
+  --workload batch  4096 candidates of degree 2^k, k uniform in {12..15}, b uniform in
+         [2^16, 2^22) seed 3, resident in four pools (one per degree, autotuned split and
+         CSIZE); one step = one tick of every pool (B squarings + the Gerbicz-Li multiply
+         of every candidate), the pools' graphs running side by side on their streams;
+         compared per degree with the plain one-candidate-per-launch-sequence path
+  --workload serve  a seeded Poisson stream of full PRP tests, degree 2^k with k
+         log-uniform in [12, 15) (k = 12, 13, 14), b uniform in [2^16, 2^24), through the
+         server (continuous batching by degree, admission by pool bytes); tests/s and
+         p50/p99 latency, beside the plain path's, whose queue is replayed from its
+         measured per-degree service times
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload single|batch|serve]
 """
 from __future__ import annotations
 
@@ -185,6 +197,251 @@ def run_reference(args, rank, world):
 
 
 # ---------------------------------------------------------------------------
+# Batched and served workloads
+# ---------------------------------------------------------------------------
+
+def gl_block(i0: int) -> int:
+    L = 2 << ((i0.bit_length() - 1) // 2)
+    return (i0 - 1) // L + 1
+
+
+def plain_rate(ln: int, b: int, reps: int = 2):
+    """Plain path: one candidate per launch sequence, default split, CSIZE 8:
+    squarings/s over Gerbicz-Li blocks (B squarings + the multiply)."""
+    import torch
+    from ctwin_gb300 import PrpEngine
+    from ctwin_gb300._native import check, lib, ptr
+    L = lib()
+    E = exponent(b, ln)
+    i0 = E.bit_length() - 1
+    B = gl_block(((20 << ln) - 1))
+    words = np.frombuffer(E.to_bytes((E.bit_length() + 31) // 32 * 4, "little"), dtype=np.uint32).copy()
+    with PrpEngine(ln, 1) as eng:
+        eng.set_b([b])
+        eng.set(1)
+        eng.copy(1, 0)
+        check(L.ctw_prp_load_exponent(eng._h, ptr(words), words.size))
+        st = torch.cuda.ExternalStream(eng.stream)
+        i = i0
+        check(L.ctw_prp_square_resident(eng._h, i, B))
+        eng.sync()
+        ts = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            check(L.ctw_prp_square_resident(eng._h, i, B))
+            check(L.ctw_prp_mul_regs(eng._h, 1, 0, 1))
+            e1.record(st)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1000.0)
+            i -= B
+        eng.sync()
+    return (B + 1) / statistics.median(ts)
+
+
+def run_batch(args):
+    import torch
+    from ctwin_gb300 import Pool, autotune
+    from ctwin_gb300._native import lib
+    L = lib()
+    rng = random.Random(3)
+    N = args.candidates
+    ks = [rng.choice((12, 13, 14, 15)) for _ in range(N)]
+    bs = [rng.randrange(1 << 16, 1 << 22) for _ in range(N)]
+    groups = {k: [b for kk, b in zip(ks, bs) if kk == k] for k in (12, 13, 14, 15)}
+    pools, tune = {}, {}
+    t0 = time.perf_counter()
+    for k, bl in groups.items():
+        lg, cs, us = autotune(k, len(bl))
+        tune[k] = {"log2_ctas": lg, "csize": cs, "us_per_squaring_lane": us}
+        pools[k] = Pool(k, len(bl), log2_ctas=lg, csize=cs)
+    t_tune = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for k, bl in groups.items():
+        for j, b in enumerate(bl):
+            assert pools[k].admit(b, tag=j) == j
+    t_admit = time.perf_counter() - t0
+    info = {k: p.info() for k, p in pools.items()}
+    sq_per_step = {k: info[k]["slots"] * (info[k]["gl_block"] + 1) for k in pools}
+    streams = {k: torch.cuda.ExternalStream(p.stream) for k, p in pools.items()}
+    tl = torch.cuda.Stream()
+    peak_imad = L.ctw_imad_peak()
+
+    def step():
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(tl)
+        ends = []
+        for k, p in pools.items():
+            streams[k].wait_event(e0)
+            p.run(1)
+            ev = torch.cuda.Event()
+            ev.record(streams[k])
+            ends.append(ev)
+        for ev in ends:
+            tl.wait_event(ev)
+        e1.record(tl)
+        return e0, e1
+
+    for _ in range(args.warmup):
+        e0, e1 = step()
+        e1.synchronize()
+    for p in pools.values():
+        p.collect(wait=True)
+    times = []
+    launches_per_step = sum(2 + (info[k]["gl_block"] + 63) // 64 for k in pools)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            e0, e1 = step()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1000.0)
+        torch.cuda.synchronize()
+    t_dev = sum(times)
+    total_sq = sum(sq_per_step.values()) * args.steps
+    value = total_sq / t_dev
+    imad = sum(sq_per_step[k] * imad_per_squaring(1 << k) for k in pools) * args.steps / t_dev
+
+    # e2e through the public API: host planning + graph launch + collect per step (wall clock)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for p in pools.values():
+            p.run(1)
+        for p in pools.values():
+            p.collect(wait=True)
+    t_e2e = time.perf_counter() - t0
+    h2d = sum(3 * info[k]["slots"] * 16 for k in pools)
+
+    # per degree: the pool alone vs the plain path (one candidate per launch sequence)
+    per_degree = {}
+    for k, p in pools.items():
+        st = streams[k]
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        p.run(1)
+        e1.record(st)
+        e1.synchronize()
+        alone = sq_per_step[k] / (e0.elapsed_time(e1) / 1000.0)
+        plain = plain_rate(k, groups[k][0])
+        per_degree[str(k)] = {"candidates": info[k]["slots"], "gl_block": info[k]["gl_block"], **tune[k],
+                              "batched_alone_sq_per_s": alone, "plain_sq_per_s": plain,
+                              "batched_over_plain": alone / plain,
+                              "tests_per_s_projected": alone / ((1 << k) *
+                                                                statistics.mean(math.log2(b) for b in groups[k])),
+                              "plain_tests_per_s_projected": plain / ((1 << k) *
+                                                                      statistics.mean(math.log2(b) for b in groups[k]))}
+    for p in pools.values():
+        p.close()
+    clocks = clk.summary()
+    line = {
+        "metric": "PRP squarings/s (batched, uneven degrees)", "value": value, "unit": "squarings/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"{N} candidates, degree 2^k with k uniform in {{12..15}}, b uniform in [2^16, 2^22) "
+                               "seed 3, one pool per degree, one step = one tick of every pool",
+                   "l2": "inputs larger than L2 (registers of all candidates resident)",
+                   "setup_s": {"autotune": t_tune, "admit": t_admit}},
+        "per_degree": per_degree,
+        "e2e": {"value": total_sq / t_e2e, "unit": "squarings/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": 0},
+        "roofline": {"bound": "imad", "achieved": imad / 1e12, "peak": peak_imad / 1e12, "unit": "T IMAD/s",
+                     "frac": imad / peak_imad if peak_imad else None, "traffic": None,
+                     "peak_source": "32-bit IMAD probe kernel run on this GPU in this process"},
+        "cpu_baseline": None, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_serve(args):
+    import torch  # noqa: F401  (CUDA context for the library)
+    from ctwin_gb300 import Server, autotune
+    rng = random.Random(11)
+    degrees = (12, 13, 14)
+    lo, hi = math.log(12), math.log(15)
+    # service demand per degree from the tuned per-lane squaring time
+    us = {k: autotune(k, 64)[2] for k in degrees}
+    mean_bits = {k: (1 << k) * 20.0 for k in degrees}
+    w = {k: (math.log(k + 1) - math.log(k)) / (hi - lo) for k in degrees}
+    demand = sum(w[k] * mean_bits[k] * us[k] * 1e-6 for k in degrees)
+    lam = args.load / demand
+    n = args.requests or max(50, int(lam * args.serve_seconds))
+    reqs, t = [], 0.0
+    for i in range(n):
+        t += rng.expovariate(lam)
+        k = int(math.exp(rng.uniform(lo, hi)))
+        reqs.append((t, k, rng.randrange(1 << 16, 1 << 24)))
+    srv = Server(hbm_budget_bytes=args.hbm_budget << 30, max_slots=256, ticks_per_launch=1, autotune=True)
+    for k in degrees:
+        srv.prepare(k, 0)
+    last, still = -1, 0
+    while still < 10:                     # pools created and tuned: bytes stable for 1 s
+        nb = srv.stats()["pool_bytes"]
+        still = still + 1 if (nb == last and nb > 0) else 0
+        last = nb
+        time.sleep(0.1)
+    res = []
+    with ClockSampler(0) as clk:
+        t0 = srv.clock()
+        for i, (ta, k, b) in enumerate(reqs):
+            while srv.clock() - t0 < ta:
+                res += srv.poll(256, 0)
+                time.sleep(0.0005)
+            srv.submit(k, b, tag=i)
+        res += srv.drain(n - len(res), timeout_s=600)
+        t_end = srv.clock()
+    srv.close()
+    lat = sorted(r["t_done"] - r["t_submit"] for r in res)
+    bad = sum(1 for r in res if r["status"] != 0 or not r["gl_ok"])
+    span = max(r["t_done"] for r in res) - (t0 + reqs[0][0])
+    per = {}
+    for k in degrees:
+        lk = sorted(r["t_done"] - r["t_submit"] for r in res if r["log2_degree"] == k)
+        if lk:
+            per[str(k)] = {"count": len(lk), "p50_s": lk[len(lk) // 2], "p99_s": lk[min(len(lk) - 1, int(0.99 * len(lk)))]}
+    # plain path: one test at a time through PrpEngine.run; service time per degree
+    # measured on one full test each, then the same arrivals replayed through a FIFO queue
+    from ctwin_gb300 import PrpEngine
+    svc = {}
+    for k in degrees:
+        b = next(bb for (_, kk, bb) in reqs if kk == k) if any(kk == k for _, kk, _ in reqs) else 1 << 20
+        with PrpEngine(k, 1) as eng:
+            t1 = time.perf_counter()
+            eng.run([b])
+            svc[k] = (time.perf_counter() - t1) * (mean_bits[k] / ((1 << k) * math.log2(b)))
+    free, plat = 0.0, []
+    for ta, k, b in reqs:
+        start = max(ta, free)
+        free = start + svc[k] * ((1 << k) * math.log2(b)) / mean_bits[k]
+        plat.append(free - ta)
+    plat.sort()
+    line = {
+        "metric": "PRP tests/s (served, mixed degrees)", "value": len(res) / span, "unit": "tests/s",
+        "n_gpus": 1, "steps": n, "warmup": 0, "ms_per_step": 1000.0 * span / max(1, len(res)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"{n} Poisson arrivals (seed 11, rate {lam:.2f}/s = {args.load:.0%} of the tuned "
+                               "capacity), degree 2^k, k log-uniform in [12, 15), b uniform in [2^16, 2^24)",
+                   "hbm_budget_gib": args.hbm_budget, "ticks_per_launch": 1},
+        "latency_s": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                      "max": lat[-1]},
+        "per_degree": per, "failed": bad,
+        "plain_path": {"tests_per_s": n / free if free > 0 else None, "p50_s": plat[len(plat) // 2],
+                       "p99_s": plat[min(len(plat) - 1, int(0.99 * len(plat)))],
+                       "service_s": {str(k): v for k, v in svc.items()},
+                       "method": "one full test per degree through PrpEngine.run timed, the same arrivals "
+                                 "replayed through a FIFO queue with those service times (scaled by log2 b)"},
+        "wall_s": t_end,
+        "e2e": {"value": len(res) / span, "unit": "tests/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 
@@ -195,6 +452,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve"])
+    ap.add_argument("--candidates", type=int, default=4096, help="batch: candidates")
+    ap.add_argument("--requests", type=int, default=0, help="serve: requests (0: rate x --serve-seconds)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--load", type=float, default=0.8, help="serve: offered load / tuned capacity")
+    ap.add_argument("--hbm-budget", type=int, default=64, help="serve: pool budget in GiB")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -215,6 +478,10 @@ def main():
 
     import torch
     torch.cuda.set_device(local)
+    if args.workload == "batch":
+        return run_batch(args) if rank == 0 else 0
+    if args.workload == "serve":
+        return run_serve(args) if rank == 0 else 0
     import ctwin_gb300
     from ctwin_gb300 import PrpEngine
     from ctwin_gb300._native import lib

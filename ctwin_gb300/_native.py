@@ -16,6 +16,15 @@ _lock = threading.Lock()
 _lib = None
 
 
+class CtwResult(ctypes.Structure):
+    """struct ctw_result of include/ctwin_gb300.h."""
+    _fields_ = [("tag", ctypes.c_uint64), ("res64", ctypes.c_uint64), ("b", ctypes.c_uint32),
+                ("log2_degree", ctypes.c_int32), ("is_prp", ctypes.c_uint8), ("gl_ok", ctypes.c_uint8),
+                ("status", ctypes.c_int8), ("reserved", ctypes.c_uint8), ("slot", ctypes.c_int32),
+                ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double),
+                ("squarings", ctypes.c_longlong)]
+
+
 class CtwError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"ctwin_gb300 error {code}: {msg}")
@@ -64,6 +73,26 @@ def lib() -> ctypes.CDLL:
             "ctw_sieve_write_files": ([i32, ctypes.c_uint64, ctypes.c_uint64, vp, ctypes.c_uint64, ctypes.c_uint64,
                                        ctypes.c_char_p], i32),
             "ctw_sieve_launches": ([], i64),
+            "ctw_prp_create_split": ([i32, i32, i32, ctypes.POINTER(H)], i32),
+            "ctw_prp_autotune": ([i32, i32, vp, vp, vp], i32),
+            "ctw_pool_create": ([i32, i32, i32, i32, u32, i32, ctypes.POINTER(H)], i32),
+            "ctw_pool_destroy": ([H], i32),
+            "ctw_pool_slot_bytes": ([i32], ctypes.c_size_t),
+            "ctw_pool_admit": ([H, u32, ctypes.c_uint64], i32),
+            "ctw_pool_run": ([H, i32], i32),
+            "ctw_pool_collect": ([H, i32], i32),
+            "ctw_pool_results": ([H, vp, i32], i32),
+            "ctw_pool_info": ([H, vp, vp, vp, vp, vp, vp, vp], i32),
+            "ctw_pool_read_slot": ([H, i32, i32, vp], i32),
+            "ctw_pool_stream": ([H], vp),
+            "ctw_pool_schedule": ([i32, u32, i32, vp, i32, vp], i32),
+            "ctw_server_create": ([ctypes.c_size_t, i32, u32, i32, i32, ctypes.POINTER(H)], i32),
+            "ctw_server_submit": ([H, i32, u32, ctypes.c_uint64], i32),
+            "ctw_server_prepare": ([H, i32, i32], i32),
+            "ctw_server_poll": ([H, vp, i32, i32], i32),
+            "ctw_server_stats": ([H, vp, vp, vp, vp, vp], i32),
+            "ctw_server_clock": ([H], ctypes.c_double),
+            "ctw_server_destroy": ([H], i32),
         }
         for name, (args, res) in sigs.items():
             fn = getattr(L, name)

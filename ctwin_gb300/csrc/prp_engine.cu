@@ -12,6 +12,7 @@
 #include "bignum.h"
 #include "prp_arith.cuh"
 #include "prp_kernels.cuh"
+#include "prp_host.h"
 #include "prp_tables.h"
 
 namespace ctw {
@@ -35,6 +36,70 @@ int fail(int code, const char *fmt, ...)
 		if (e_ != cudaSuccess) return fail(CTW_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),     \
 		                                   __FILE__, __LINE__);                                              \
 	} while (0)
+
+// Canonical digits of x mod N = b^D - b^{D/2} + 1 (cyclo/src/transform.h:501-597):
+// carry the signed digits base b, fold the top carry T as -T at 0 and +T at
+// D/2 (b^D = b^{D/2} - 1 mod N) until it vanishes, then subtract N once if the
+// value is >= N.
+int canonical(const int32_t *x, uint32_t b, size_t D, uint32_t *out)
+{
+	const int64_t B = b;
+	auto divmod = [B](int64_t &v) -> uint32_t {
+		int64_t q = v / B, r = v % B;
+		if (r < 0) { r += B; --q; }
+		v = q;
+		return (uint32_t)r;
+	};
+	int64_t c = 0;
+	for (size_t j = 0; j < D; ++j)
+	{
+		int64_t v = c + x[j];
+		out[j] = divmod(v);
+		c = v;
+	}
+	for (int guard = 0; c != 0; ++guard)
+	{
+		if (guard > 64) return fail(CTW_E_COMPUTE, "getInt: carry does not settle");
+		int64_t v = -c;
+		for (size_t j = 0; j < D / 2; ++j) { v += out[j]; out[j] = divmod(v); }
+		v += c;
+		for (size_t j = D / 2; j < D; ++j) { v += out[j]; out[j] = divmod(v); if (v == 0) break; }
+		c = v;
+	}
+	bool ge = true;
+	for (size_t j = D / 2; j < D; ++j) if (out[j] != b - 1) { ge = false; break; }
+	if (ge)
+	{
+		bool low_zero = true;
+		for (size_t j = 0; j < D / 2; ++j) if (out[j] != 0) { low_zero = false; break; }
+		ge = !low_zero;
+	}
+	if (ge)
+	{
+		// value - N: lower half minus 1, upper half cleared
+		size_t j = 0;
+		while (j < D / 2 && out[j] == 0) { out[j] = b - 1; ++j; }
+		if (j == D / 2) return fail(CTW_E_COMPUTE, "getInt failed");
+		out[j] -= 1;
+		for (size_t k = D / 2; k < D; ++k) out[k] = 0;
+	}
+	return CTW_OK;
+}
+
+void res64_of(const uint32_t *c, uint32_t b, size_t D, bool &prp, bool &zero, uint64_t &r64)
+{
+	prp = (c[0] == 1);
+	zero = (c[0] == 0);
+	uint64_t r = c[0], bp = b;
+	for (size_t j = 1; j < D; ++j)
+	{
+		prp &= (c[j] == 0);
+		zero &= (c[j] == 0);
+		r += (uint64_t)c[j] * bp;
+		bp *= b;
+	}
+	r64 = r;
+}
 
 }  // namespace ctw
 
@@ -79,7 +144,7 @@ int build_tables(ctw_prp *h)
 {
 	const size_t words = h->G * 3 * h->M, swords = h->G * 3 * 256 * 2;
 	std::vector<uint32_t> tf(words), ti(words), tfs(swords), tis(swords);
-	prp_build_tables(h->ln, tf.data(), ti.data(), h->proto, tfs.data(), tis.data());
+	prp_build_tables(h->ln, h->lg, tf.data(), ti.data(), h->proto, tfs.data(), tis.data());
 	const size_t bytes = words * sizeof(uint32_t);
 	CTW_CUDA(cudaMalloc(&h->d_tf, bytes));
 	CTW_CUDA(cudaMalloc(&h->d_ti, bytes));
@@ -145,55 +210,6 @@ int check_status(ctw_prp *h)
 	return CTW_OK;
 }
 
-// Canonical digits of x mod N = b^D - b^{D/2} + 1 (cyclo/src/transform.h:501-597):
-// carry the signed digits base b, fold the top carry T as -T at 0 and +T at
-// D/2 (b^D = b^{D/2} - 1 mod N) until it vanishes, then subtract N once if the
-// value is >= N.
-int canonical(const int32_t *x, uint32_t b, size_t D, uint32_t *out)
-{
-	const int64_t B = b;
-	auto divmod = [B](int64_t &v) -> uint32_t {
-		int64_t q = v / B, r = v % B;
-		if (r < 0) { r += B; --q; }
-		v = q;
-		return (uint32_t)r;
-	};
-	int64_t c = 0;
-	for (size_t j = 0; j < D; ++j)
-	{
-		int64_t v = c + x[j];
-		out[j] = divmod(v);
-		c = v;
-	}
-	for (int guard = 0; c != 0; ++guard)
-	{
-		if (guard > 64) return fail(CTW_E_COMPUTE, "getInt: carry does not settle");
-		int64_t v = -c;
-		for (size_t j = 0; j < D / 2; ++j) { v += out[j]; out[j] = divmod(v); }
-		v += c;
-		for (size_t j = D / 2; j < D; ++j) { v += out[j]; out[j] = divmod(v); if (v == 0) break; }
-		c = v;
-	}
-	bool ge = true;
-	for (size_t j = D / 2; j < D; ++j) if (out[j] != b - 1) { ge = false; break; }
-	if (ge)
-	{
-		bool low_zero = true;
-		for (size_t j = 0; j < D / 2; ++j) if (out[j] != 0) { low_zero = false; break; }
-		ge = !low_zero;
-	}
-	if (ge)
-	{
-		// value - N: lower half minus 1, upper half cleared
-		size_t j = 0;
-		while (j < D / 2 && out[j] == 0) { out[j] = b - 1; ++j; }
-		if (j == D / 2) return fail(CTW_E_COMPUTE, "getInt failed");
-		out[j] -= 1;
-		for (size_t k = D / 2; k < D; ++k) out[k] = 0;
-	}
-	return CTW_OK;
-}
-
 int read_reg_host(ctw_prp *h, int reg, std::vector<int32_t> &v)
 {
 	v.resize((size_t)h->lanes * h->D);
@@ -212,21 +228,6 @@ int canonical_reg(ctw_prp *h, int reg, std::vector<uint32_t> &c)
 	for (int l = 0; l < h->lanes; ++l)
 		if ((rc = canonical(v.data() + (size_t)l * h->D, h->b[(size_t)l], h->D, c.data() + (size_t)l * h->D))) return rc;
 	return CTW_OK;
-}
-
-void res64_of(const uint32_t *c, uint32_t b, size_t D, bool &prp, bool &zero, uint64_t &r64)
-{
-	prp = (c[0] == 1);
-	zero = (c[0] == 0);
-	uint64_t r = c[0], bp = b;
-	for (size_t j = 1; j < D; ++j)
-	{
-		prp &= (c[j] == 0);
-		zero &= (c[j] == 0);
-		r += (uint64_t)c[j] * bp;
-		bp *= b;
-	}
-	r64 = r;
 }
 
 int op_square_bits(ctw_prp *h, const uint32_t *d_bits, int nwords, long long i_hi, int count)
@@ -285,15 +286,23 @@ int ctw_device_count(void)
 
 int ctw_prp_create(int log2_degree, int lanes, ctw_prp **out)
 {
+	return ctw_prp_create_split(log2_degree, lanes, -1, out);
+}
+
+int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **out)
+{
 	if (!out) return fail(CTW_E_ARG, "null output pointer");
 	*out = nullptr;
 	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
 	if (lanes < 1 || lanes > MAX_INLINE_LANES) return fail(CTW_E_ARG, "lanes %d outside [1, %d]", lanes, MAX_INLINE_LANES);
+	const int lg = log2_ctas < 0 ? prp_lg_for(log2_degree) : log2_ctas;
+	if (!prp_split_supported(log2_degree - lg, lg))
+		return fail(CTW_E_ARG, "no kernel for degree 2^%d on 2^%d CTAs", log2_degree, lg);
 	if (ctw_device_count() == 0) return fail(CTW_E_CUDA, "no CUDA device");
 	ctw_prp *h = new ctw_prp();
 	h->ln = log2_degree;
 	h->lanes = lanes;
-	h->lg = prp_lg_for(log2_degree);
+	h->lg = lg;
 	h->lm = log2_degree - h->lg;
 	h->D = (size_t)1 << log2_degree;
 	h->G = (size_t)1 << h->lg;
@@ -346,6 +355,8 @@ int ctw_prp_set_csize(ctw_prp *h, int csize)
 	if (int rc = check_handle(h)) return rc;
 	if (csize != 8 && csize != 16 && csize != 32 && csize != 64) return fail(CTW_E_ARG, "csize %d not in {8,16,32,64}", csize);
 	if ((size_t)csize * 2 > h->M) return fail(CTW_E_ARG, "csize too large for this degree");
+	if (h->lg > 0 && h->lm <= 13 && (size_t)csize > (h->M >> h->lg))
+		return fail(CTW_E_ARG, "csize %d longer than a column run of this split", csize);
 	h->csize = csize;
 	return CTW_OK;
 }

@@ -518,14 +518,13 @@ __device__ __forceinline__ int64_t load64(const uint32_t *X, int M, int p)
 // ---------------------------------------------------------------------------
 
 template <int LG>
-__device__ void cross_levels(uint32_t *X, uint32_t *ST, int M, int g, int dir, const PrpKernelArgs &a, int tid,
-                             int nt)
+__device__ void cross_levels(uint32_t *X, uint32_t *ST, int M, int g, int dir, const PrpKernelArgs &a, bool narrow,
+                             int tid, int nt)
 {
 	constexpr int G = 1 << LG;
 	cg::cluster_group cl = cg::this_cluster();
 	const int MG = M >> LG, SC = a.scols, nr = MG / SC, sb = a.swz_b;
 	const int SC4 = SC >> 2;
-	const bool narrow = a.narrow != 0;
 	uint32_t *SD = ST;                 // [G][SC] digits (forward)
 	uint32_t *SR = ST + G * SC;        // [3][G][SC] residues
 	for (int rnd = 0; rnd < nr; ++rnd)
@@ -662,6 +661,38 @@ __device__ __forceinline__ int64_t carry_chunk(uint32_t *X, int M, int c, int cs
 
 // Shared memory (words): planes [3][M], stage (cross levels) or chunk carries,
 // carry exchange, then the CTA's roots [3][M] forward and inverse when they fit.
+// Operands of one lane: from the launch, or from the lane's command.
+struct LaneView {
+	const int32_t *rin, *ry;
+	int32_t *rout;
+	long long i_hi;
+	int count;
+};
+
+__device__ __forceinline__ bool lane_view(const PrpKernelArgs &a, int lane, LaneView &v)
+{
+	if (!a.cmd)
+	{
+		v.rin = a.reg_in;
+		v.ry = a.reg_y;
+		v.rout = a.reg_out;
+		v.i_hi = a.i_hi;
+		v.count = a.count;
+		return true;
+	}
+	// a.i_hi / a.count cut the lane's squarings into launches: this launch runs
+	// squarings a.i_hi .. a.i_hi + a.count - 1 of the command
+	const PrpLaneCmd c = a.cmd[lane];
+	const int count = min(c.count - (int)a.i_hi, a.count);
+	if (count <= 0) return false;
+	v.rin = a.regs + c.r_in * a.reg_stride;
+	v.ry = a.regs + c.r_y * a.reg_stride;
+	v.rout = a.regs + c.r_out * a.reg_stride;
+	v.i_hi = (long long)c.i_hi - a.i_hi;
+	v.count = count;
+	return true;
+}
+
 __host__ __device__ __forceinline__ size_t smem_stage_words(int lm, int lg, int scols)
 {
 	const size_t stage = lg > 0 ? (size_t)4 * ((size_t)1 << lg) * scols : 0;
@@ -679,8 +710,9 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 	int g = 0;
 	if constexpr (LG > 0) g = (int)cg::this_cluster().block_rank();
 	const int lane = blockIdx.x / G;
+	LaneView lv;
+	if (!lane_view(a, lane, lv)) return;   // idle lane: the whole cluster leaves
 	const int ncl = M / a.csize, sb = a.swz_b;
-	const bool narrow = a.narrow != 0;
 
 	uint32_t *X = sm;                                           // [3][M] swizzled planes
 	uint32_t *ST = sm + 3 * M;                                  // stage / chunk carries
@@ -692,6 +724,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
 	const int b_s = (int)a.lane_b[4 * lane + 2];
+	const bool narrow = (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;   // launch-wide or per-lane 64-bit carries
 	uint32_t err = 0;
 
 	// Root tables are laid out [G][3][M]: the slice of CTA g is contiguous.
@@ -702,7 +735,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 	}
 	const uint32_t *TFl = a.tw_smem ? TF : tfg;
 	const uint32_t *TIl = a.tw_smem ? TI : tig;
-	uint32_t *SF = TI + 3 * M, *SI = SF + 3 * 256 * 2;         // Shoup roots of levels 0..7 (M12)
+	uint32_t *SF = a.tw_smem ? TI + 3 * M : TF, *SI = SF + 3 * 256 * 2;   // Shoup roots of levels 0..7 (M12)
 	if constexpr (M12)
 	{
 		const uint32_t *sfg = a.tfs + (size_t)g * 3 * 256 * 2, *sig = a.tis + (size_t)g * 3 * 256 * 2;
@@ -722,7 +755,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 		if constexpr (LG > 0)
 		{
 			csync<LG>();
-			cross_levels<LG>(X, ST, M, g, 0, a, tid, nt);
+			cross_levels<LG>(X, ST, M, g, 0, a, narrow, tid, nt);
 			csync<LG>();
 		}
 		else
@@ -744,7 +777,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 		if constexpr (LG > 0)
 		{
 			csync<LG>();
-			cross_levels<LG>(X, ST, M, g, 1, a, tid, nt);   // includes Garner
+			cross_levels<LG>(X, ST, M, g, 1, a, narrow, tid, nt);   // includes Garner
 			csync<LG>();
 		}
 		else
@@ -812,18 +845,18 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 
 	if (a.op == OP_MUL)
 	{
-		load_digits(a.reg_y);
+		load_digits(lv.ry);
 		transform_and_normalize(LM_FWD_ONLY, 1);
 		__syncthreads();
-		load_digits(a.reg_in);
+		load_digits(lv.rin);
 		transform_and_normalize(LM_MUL, 1);
 	}
 	else
 	{
-		load_digits(a.reg_in);
-		for (int it = 0; it < a.count; ++it)
+		load_digits(lv.rin);
+		for (int it = 0; it < lv.count; ++it)
 		{
-			const long long i = a.i_hi - it;
+			const long long i = lv.i_hi - it;
 			int bit = 0;
 			if (a.use_dupmask) bit = (int)((a.dupmask[lane >> 6] >> (lane & 63)) & 1);
 			else if (i >= 0 && (i >> 5) < a.nwords) bit = (a.bits[(size_t)lane * a.nwords + (i >> 5)] >> (i & 31)) & 1;
@@ -831,7 +864,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 		}
 	}
 	// digits -> global
-	for (int t = tid; t < M; t += nt) a.reg_out[lane_off + t] = (int32_t)X[swz(t, sb)];
+	for (int t = tid; t < M; t += nt) lv.rout[lane_off + t] = (int32_t)X[swz(t, sb)];
 	if (err) atomicOr(a.status, err);
 	// No CTA may leave while another can still read its shared memory.
 	csync<LG>();
@@ -865,11 +898,12 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 	cg::cluster_group cl = cg::this_cluster();
 	const int g = (int)cl.block_rank();
 	const int lane = blockIdx.x / G;
+	LaneView lv;
+	if (!lane_view(a, lane, lv)) return;   // idle lane: the whole cluster leaves
 	const int csz = a.csize, sb = a.swz_b;
 	const int runc = MG / csz;                                  // chunks per run
 	const int ncl = G * runc;                                   // chunks held by this CTA
 	const int cb = g * MG;                                      // first column of this CTA
-	const bool narrow = a.narrow != 0;
 
 	uint32_t *XC = sm;                                          // [3][G][MG] column runs
 	uint32_t *XR = sm + 3 * M;                                  // [3][M] row block g
@@ -880,6 +914,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
 	const int b_s = (int)a.lane_b[4 * lane + 2];
+	const bool narrow = (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;   // launch-wide or per-lane 64-bit carries
 	uint32_t err = 0;
 
 	const uint32_t *tfg = a.tf + (size_t)g * 3 * M, *tig = a.ti + (size_t)g * 3 * M;
@@ -889,7 +924,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 	}
 	const uint32_t *TFl = a.tw_smem ? TF : tfg;
 	const uint32_t *TIl = a.tw_smem ? TI : tig;
-	uint32_t *SF = TI + 3 * M, *SI = SF + 3 * 256 * 2;         // Shoup roots of levels 0..7 (M12)
+	uint32_t *SF = a.tw_smem ? TI + 3 * M : TF, *SI = SF + 3 * 256 * 2;   // Shoup roots of levels 0..7 (M12)
 	if constexpr (M12)
 	{
 		const uint32_t *sfg = a.tfs + (size_t)g * 3 * 256 * 2, *sig = a.tis + (size_t)g * 3 * 256 * 2;
@@ -1096,18 +1131,18 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 
 	if (a.op == OP_MUL)
 	{
-		load_digits(a.reg_y);
+		load_digits(lv.ry);
 		transform_and_normalize(LM_FWD_ONLY, 1);
 		cl.sync();                // peers may still be pulling y's columns
-		load_digits(a.reg_in);
+		load_digits(lv.rin);
 		transform_and_normalize(LM_MUL, 1);
 	}
 	else
 	{
-		load_digits(a.reg_in);
-		for (int it = 0; it < a.count; ++it)
+		load_digits(lv.rin);
+		for (int it = 0; it < lv.count; ++it)
 		{
-			const long long i = a.i_hi - it;
+			const long long i = lv.i_hi - it;
 			int bit = 0;
 			if (a.use_dupmask) bit = (int)((a.dupmask[lane >> 6] >> (lane & 63)) & 1);
 			else if (i >= 0 && (i >> 5) < a.nwords) bit = (a.bits[(size_t)lane * a.nwords + (i >> 5)] >> (i & 31)) & 1;
@@ -1117,7 +1152,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 	for (int e = tid; e < M; e += nt)
 	{
 		const int h = e / MG, tt = e - h * MG;
-		a.reg_out[lane_base + (size_t)h * M + cb + tt] = (int32_t)XC[pc(h, tt)];
+		lv.rout[lane_base + (size_t)h * M + cb + tt] = (int32_t)XC[pc(h, tt)];
 	}
 	if (err) atomicOr(a.status, err);
 	cl.sync();                    // peers may still read this CTA's carries
@@ -1175,12 +1210,22 @@ static cudaError_t launch_lg(const PrpKernelArgs &a, int lanes, cudaStream_t str
 	return cudaLaunchKernelEx(&cfg, kern, a);
 }
 
-// Degrees 2^12..2^16 use the 4096-coefficient local path (one CTA for 2^12,
-// column-layout clusters of 2..16 CTAs above); 2^8..2^11 the generic path on
-// one CTA; 2^17 a 16-CTA column-layout cluster with the generic local path;
-// 2^18 a 16-CTA cluster with staged cross levels.
+// Cluster splits with a kernel: one CTA for M = 2^8..2^14 (the 4096-coefficient
+// path for M = 2^12); column-layout clusters of 2..16 CTAs for M = 2^8..2^13
+// with runs of at least 32 columns (M / G >= 32, so the swizzle stays inside a
+// run); staged cross levels for M = 2^14 on 16 CTAs.  The default split of each
+// degree is prp_lg_for (prp_tables.h); the others are autotuning choices.
+bool prp_split_supported(int lm, int lg)
+{
+	if (lm < 8 || lm > 14 || lg < 0 || lg > MAX_LG) return false;
+	if (lg == 0) return true;
+	if (lm <= 13) return lm - lg >= 5;
+	return lg == 4;
+}
+
 cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t stream)
 {
+	if (!prp_split_supported(a.lm, lg)) return cudaErrorInvalidValue;
 	if (a.lm == 12)
 	{
 		switch (lg)
@@ -1189,14 +1234,45 @@ cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t s
 		case 1: return launch_lg<1, true, true>(a, lanes, stream);
 		case 2: return launch_lg<2, true, true>(a, lanes, stream);
 		case 3: return launch_lg<3, true, true>(a, lanes, stream);
-		case 4: return launch_lg<4, true, true>(a, lanes, stream);
-		default: return cudaErrorInvalidValue;
+		default: return launch_lg<4, true, true>(a, lanes, stream);
 		}
 	}
 	if (lg == 0) return launch_lg<0, false, false>(a, lanes, stream);
-	if (lg == 4 && a.lm == 13) return launch_lg<4, false, true>(a, lanes, stream);
-	if (lg == 4 && a.lm == 14) return launch_lg<4, false, false>(a, lanes, stream);
-	return cudaErrorInvalidValue;
+	if (a.lm == 14) return launch_lg<4, false, false>(a, lanes, stream);
+	switch (lg)
+	{
+	case 1: return launch_lg<1, false, true>(a, lanes, stream);
+	case 2: return launch_lg<2, false, true>(a, lanes, stream);
+	case 3: return launch_lg<3, false, true>(a, lanes, stream);
+	default: return launch_lg<4, false, true>(a, lanes, stream);
+	}
+}
+
+// Per-lane register set-up of a pool tick, ahead of its squarings: bit 0 of
+// aux saves register 0 in register 3, bit 1 sets register 0 to aux_arg, bit 2
+// sets register 1 to aux_arg (the value 1 of the reference's engine::set).
+__global__ void prp_aux_kernel(const PrpLaneCmd *cmd, int32_t *regs, long long stride, int D)
+{
+	const int lane = blockIdx.y;
+	const PrpLaneCmd c = cmd[lane];
+	if (c.aux == 0) return;
+	int32_t *r0 = regs + (size_t)lane * D, *r1 = r0 + stride, *r3 = r0 + 3 * stride;
+	for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < D; j += gridDim.x * blockDim.x)
+	{
+		const int32_t v = (j == 0) ? (int32_t)c.aux_arg : 0;
+		if (c.aux & 1) r3[j] = r0[j];
+		if (c.aux & 2) r0[j] = v;
+		if (c.aux & 4) r1[j] = v;
+	}
+}
+
+cudaError_t prp_aux_launch(const PrpLaneCmd *cmd, int32_t *regs, long long reg_stride, int ln, int lanes,
+                           cudaStream_t stream)
+{
+	const int D = 1 << ln, threads = 256;
+	const int gx = D / (threads * 4) > 0 ? D / (threads * 4) : 1;
+	prp_aux_kernel<<<dim3(gx, lanes), threads, 0, stream>>>(cmd, regs, reg_stride, D);
+	return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

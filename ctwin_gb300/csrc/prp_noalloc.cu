@@ -91,7 +91,7 @@ int na_setup(int dev)
 			tfs = g_na_host_tables + na_shoup_offset(ln);
 			tis = tfs + G * 3 * 256 * 2;
 		}
-		prp_build_tables(ln, tf, tf + 3 * (size_t(1) << ln), d.proto[ln], tfs, tis);
+		prp_build_tables(ln, prp_lg_for(ln), tf, tf + 3 * (size_t(1) << ln), d.proto[ln], tfs, tis);
 	}
 	if ((e = cudaMemcpy(d.tables, g_na_host_tables, sizeof(g_na_host_tables), cudaMemcpyHostToDevice)) != cudaSuccess)
 		return fail(CTW_E_CUDA, "no-alloc set-up: table upload: %s", cudaGetErrorString(e));

@@ -1,0 +1,401 @@
+// Request loop over pools of every degree: continuous batching by size class
+// with admission by device-memory footprint.
+//
+// Threads: the caller submits requests; a preparation thread computes each
+// request's exponent and Gerbicz-Li block sum on the host; the worker thread
+// owns the CUDA work.  Each worker iteration admits prepared requests into
+// free slots of the pool of their degree (allocating a new pool only while
+// the pools' bytes stay within the budget, and releasing idle pools when a
+// request is blocked by the budget), keeps at most two graph launches queued
+// per pool, and retires finished tests.  Pools run on their own streams, so
+// ticks of different degrees overlap on the device.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ctwin_gb300.h"
+#include "prp_host.h"
+#include "prp_pool.h"
+#include "prp_tables.h"
+
+using namespace ctw;
+
+namespace {
+
+struct Request {
+	int ln = 0;
+	uint32_t b = 0;
+	uint64_t tag = 0;
+	double t_submit = 0;
+};
+
+struct Prepared {
+	Request r;
+	PreparedTest t;
+};
+
+}  // namespace
+
+struct ctw_server {
+	size_t budget = 0;
+	int max_slots = 256, tpl = 2, autotune = 0, device = 0;
+	uint32_t base = 2;
+	double t0 = 0;
+
+	std::mutex mu;
+	std::condition_variable cv_in, cv_ready, cv_done;
+	std::deque<Request> incoming;
+	std::deque<Prepared> ready;
+	std::deque<ctw_result> done;
+	std::deque<std::pair<int, int>> prepare_req;   // (degree, slots) pools to create ahead
+	bool stop = false;
+	std::string error;
+	long long submitted = 0, finished = 0, active = 0, pending = 0;
+	size_t bytes = 0;
+
+	std::thread prep, worker;
+	// worker-owned
+	std::map<int, std::vector<ctw_pool *>> pools;
+	std::map<int, std::pair<int, int>> split;      // degree -> (log2 CTAs, csize)
+	std::vector<Prepared> waiting;
+};
+
+namespace {
+
+int pool_slots_for(ctw_server *s, int ln)
+{
+	const size_t sb = pool_slot_bytes(ln, default_gl_block(ln));
+	const size_t cap = std::max<size_t>(1, (s->budget / 4) / sb);
+	return (int)std::min<size_t>((size_t)s->max_slots, cap);
+}
+
+// Split and carry chunk of a degree: tuned once on first use, else the defaults.
+std::pair<int, int> split_for(ctw_server *s, int ln, int slots)
+{
+	auto it = s->split.find(ln);
+	if (it != s->split.end()) return it->second;
+	int lg = prp_lg_for(ln), cs = 8;
+	if (s->autotune)
+	{
+		double us = 0;
+		int tlg = 0, tcs = 0;
+		if (ctw_prp_autotune(ln, slots, &tlg, &tcs, &us) == CTW_OK) { lg = tlg; cs = tcs; }
+	}
+	return s->split[ln] = std::make_pair(lg, cs);
+}
+
+size_t new_pool_bytes(ctw_server *s, int ln, int slots)
+{
+	return pool_bytes_estimate(ln, split_for(s, ln, slots).first, slots, default_gl_block(ln));
+}
+
+int new_pool(ctw_server *s, int ln, int slots, ctw_pool **out)
+{
+	const std::pair<int, int> sp = split_for(s, ln, slots);
+	return ctw_pool_create(ln, slots, sp.first, sp.second, s->base, 0, out);
+}
+
+void prep_loop(ctw_server *s)
+{
+	for (;;)
+	{
+		Request r;
+		{
+			std::unique_lock<std::mutex> lk(s->mu);
+			s->cv_in.wait(lk, [&] { return s->stop || !s->incoming.empty(); });
+			if (s->stop) return;
+			r = s->incoming.front();
+			s->incoming.pop_front();
+		}
+		Prepared p;
+		p.r = r;
+		p.t.b = r.b;
+		slot_prepare(p.t, r.ln, default_gl_block(r.ln));
+		{
+			std::lock_guard<std::mutex> lk(s->mu);
+			s->ready.push_back(std::move(p));
+		}
+		s->cv_ready.notify_one();
+	}
+}
+
+void set_error(ctw_server *s, const char *where)
+{
+	std::lock_guard<std::mutex> lk(s->mu);
+	if (s->error.empty()) s->error = std::string(where) + ": " + ctw_last_error();
+}
+
+void worker_loop(ctw_server *s)
+{
+	cudaSetDevice(s->device);
+	std::vector<ctw_result> buf(256);
+	for (;;)
+	{
+		std::vector<std::pair<int, int>> ahead;
+		{
+			std::unique_lock<std::mutex> lk(s->mu);
+			bool busy = !s->waiting.empty();
+			for (auto &kv : s->pools)
+				for (ctw_pool *p : kv.second)
+					if (pool_active(p) > 0 || pool_in_flight(p) > 0) busy = true;
+			if (!busy)
+				s->cv_ready.wait_for(lk, std::chrono::milliseconds(2),
+				                     [&] { return s->stop || !s->ready.empty() || !s->prepare_req.empty(); });
+			if (s->stop) break;
+			while (!s->ready.empty())
+			{
+				s->waiting.push_back(std::move(s->ready.front()));
+				s->ready.pop_front();
+			}
+			while (!s->prepare_req.empty())
+			{
+				ahead.push_back(s->prepare_req.front());
+				s->prepare_req.pop_front();
+			}
+		}
+		for (auto &pr : ahead)
+		{
+			if (!s->pools[pr.first].empty()) continue;
+			ctw_pool *p = nullptr;
+			const int slots = pr.second > 0 ? std::min(pr.second, s->max_slots) : pool_slots_for(s, pr.first);
+			if (new_pool(s, pr.first, slots, &p) == CTW_OK)
+			{
+				s->pools[pr.first].push_back(p);
+				std::lock_guard<std::mutex> lk(s->mu);
+				s->bytes += pool_bytes(p);
+			}
+			else
+				set_error(s, "prepare");
+		}
+
+		// admission, first come first served within each degree
+		long long admitted = 0;
+		bool blocked_by_budget = false;
+		std::vector<Prepared> still;
+		std::vector<ctw_result> out;
+		for (Prepared &w : s->waiting)
+		{
+			if (new_pool_bytes(s, w.r.ln, 1) > s->budget)
+			{
+				// not even a one-slot pool fits: the request fails instead of waiting forever
+				ctw_result r{};
+				r.tag = w.r.tag;
+				r.b = w.r.b;
+				r.log2_degree = w.r.ln;
+				r.status = (int8_t)CTW_E_NOMEM;
+				r.slot = -1;
+				r.t_submit = w.r.t_submit;
+				r.t_admit = r.t_done = mono_seconds();
+				out.push_back(r);
+				continue;
+			}
+			auto &vec = s->pools[w.r.ln];
+			ctw_pool *target = nullptr;
+			for (ctw_pool *p : vec)
+				if (pool_free_slots(p) > 0) { target = p; break; }
+			if (!target)
+			{
+				const int slots = pool_slots_for(s, w.r.ln);
+				if (s->bytes + new_pool_bytes(s, w.r.ln, slots) <= s->budget)
+				{
+					ctw_pool *p = nullptr;
+					if (new_pool(s, w.r.ln, slots, &p) == CTW_OK)
+					{
+						vec.push_back(p);
+						std::lock_guard<std::mutex> lk(s->mu);
+						s->bytes += pool_bytes(p);
+						target = p;
+					}
+					else
+						set_error(s, "pool");
+				}
+				else
+					blocked_by_budget = true;
+			}
+			if (target && pool_admit_prepared(target, w.t, w.r.tag, w.r.t_submit) >= 0)
+				++admitted;
+			else
+				still.push_back(std::move(w));
+		}
+		s->waiting.swap(still);
+		if (blocked_by_budget)
+		{
+			// give back pools with nothing to do
+			for (auto &kv : s->pools)
+				for (auto it = kv.second.begin(); it != kv.second.end();)
+				{
+					ctw_pool *p = *it;
+					if (pool_active(p) == 0 && pool_in_flight(p) == 0 && ctw_pool_collect(p, 0) == 0)
+					{
+						const size_t pb = pool_bytes(p);
+						ctw_pool_destroy(p);
+						it = kv.second.erase(it);
+						std::lock_guard<std::mutex> lk(s->mu);
+						s->bytes -= pb;
+					}
+					else
+						++it;
+				}
+		}
+
+		// keep two launches queued per busy pool; retire finished tests
+		long long act = 0;
+		for (auto &kv : s->pools)
+			for (ctw_pool *p : kv.second)
+			{
+				if (pool_active(p) > 0 && pool_in_flight(p) < 2)
+					if (ctw_pool_run(p, s->tpl) != CTW_OK) set_error(s, "run");
+				const int n = ctw_pool_collect(p, 0);
+				if (n < 0) set_error(s, "collect");
+				for (int got; n > 0 && (got = ctw_pool_results(p, buf.data(), (int)buf.size())) > 0;)
+					for (int i = 0; i < got; ++i) out.push_back(buf[(size_t)i]);
+				act += pool_active(p);
+			}
+		{
+			std::lock_guard<std::mutex> lk(s->mu);
+			for (ctw_result &r : out)
+			{
+				r.t_submit -= s->t0;
+				r.t_admit -= s->t0;
+				r.t_done -= s->t0;
+				s->done.push_back(r);
+			}
+			s->finished += (long long)out.size();
+			s->active = act;
+			s->pending = (long long)s->waiting.size() + (long long)s->ready.size() + (long long)s->incoming.size();
+		}
+		if (!out.empty()) s->cv_done.notify_all();
+		if (admitted == 0 && out.empty()) std::this_thread::sleep_for(std::chrono::microseconds(100));
+	}
+	for (auto &kv : s->pools)
+		for (ctw_pool *p : kv.second) ctw_pool_destroy(p);
+	s->pools.clear();
+}
+
+}  // namespace
+
+extern "C" {
+
+int ctw_server_create(size_t hbm_budget_bytes, int max_slots, uint32_t base, int ticks_per_launch, int autotune,
+                      ctw_server **out)
+{
+	if (!out) return fail(CTW_E_ARG, "null output pointer");
+	*out = nullptr;
+	if (base != 2 && base != 3) return fail(CTW_E_ARG, "base %u not in {2,3}", base);
+	if (max_slots < 1 || max_slots > 65535) return fail(CTW_E_ARG, "max_slots %d outside [1, 65535]", max_slots);
+	if (ticks_per_launch < 1 || ticks_per_launch > POOL_TMAX)
+		return fail(CTW_E_ARG, "ticks_per_launch %d outside [1, %d]", ticks_per_launch, POOL_TMAX);
+	if (ctw_device_count() == 0) return fail(CTW_E_CUDA, "no CUDA device");
+	ctw_server *s = new ctw_server();
+	cudaGetDevice(&s->device);
+	if (hbm_budget_bytes == 0)
+	{
+		size_t fr = 0, tot = 0;
+		if (cudaMemGetInfo(&fr, &tot) != cudaSuccess)
+		{
+			delete s;
+			return fail(CTW_E_CUDA, "cudaMemGetInfo failed");
+		}
+		hbm_budget_bytes = fr / 10 * 8;
+	}
+	s->budget = hbm_budget_bytes;
+	s->max_slots = max_slots;
+	s->base = base;
+	s->tpl = ticks_per_launch;
+	s->autotune = autotune;
+	s->t0 = mono_seconds();
+	s->prep = std::thread(prep_loop, s);
+	s->worker = std::thread(worker_loop, s);
+	*out = s;
+	return CTW_OK;
+}
+
+int ctw_server_submit(ctw_server *s, int log2_degree, uint32_t b, uint64_t tag)
+{
+	if (!s) return fail(CTW_E_ARG, "null server");
+	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
+	if (b < 64 || b >= 0x80000000u) return fail(CTW_E_ARG, "b = %u outside [64, 2^31)", b);
+	{
+		std::lock_guard<std::mutex> lk(s->mu);
+		if (!s->error.empty()) return fail(CTW_E_CUDA, "server failed: %s", s->error.c_str());
+		Request r;
+		r.ln = log2_degree;
+		r.b = b;
+		r.tag = tag;
+		r.t_submit = mono_seconds();
+		s->incoming.push_back(r);
+		++s->submitted;
+		++s->pending;
+	}
+	s->cv_in.notify_one();
+	return CTW_OK;
+}
+
+int ctw_server_prepare(ctw_server *s, int log2_degree, int slots)
+{
+	if (!s) return fail(CTW_E_ARG, "null server");
+	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
+	{
+		std::lock_guard<std::mutex> lk(s->mu);
+		s->prepare_req.emplace_back(log2_degree, slots);
+	}
+	s->cv_ready.notify_one();
+	return CTW_OK;
+}
+
+int ctw_server_poll(ctw_server *s, ctw_result *out, int max, int timeout_ms)
+{
+	if (!s || (!out && max > 0)) return fail(CTW_E_ARG, "bad arguments");
+	std::unique_lock<std::mutex> lk(s->mu);
+	if (s->done.empty() && timeout_ms > 0)
+		s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms),
+		                    [&] { return !s->done.empty() || !s->error.empty(); });
+	if (!s->error.empty() && s->done.empty()) return fail(CTW_E_CUDA, "server failed: %s", s->error.c_str());
+	int n = 0;
+	while (n < max && !s->done.empty())
+	{
+		out[n++] = s->done.front();
+		s->done.pop_front();
+	}
+	return n;
+}
+
+int ctw_server_stats(ctw_server *s, long long *submitted, long long *pending, long long *active, long long *finished,
+                     size_t *pool_bytes_out)
+{
+	if (!s) return fail(CTW_E_ARG, "null server");
+	std::lock_guard<std::mutex> lk(s->mu);
+	if (submitted) *submitted = s->submitted;
+	if (pending) *pending = s->pending;
+	if (active) *active = s->active;
+	if (finished) *finished = s->finished;
+	if (pool_bytes_out) *pool_bytes_out = s->bytes;
+	return CTW_OK;
+}
+
+double ctw_server_clock(ctw_server *s) { return s ? mono_seconds() - s->t0 : 0.0; }
+
+int ctw_server_destroy(ctw_server *s)
+{
+	if (!s) return CTW_OK;
+	{
+		std::lock_guard<std::mutex> lk(s->mu);
+		s->stop = true;
+	}
+	s->cv_in.notify_all();
+	s->cv_ready.notify_all();
+	if (s->prep.joinable()) s->prep.join();
+	if (s->worker.joinable()) s->worker.join();
+	delete s;
+	return CTW_OK;
+}
+
+}  // extern "C"

@@ -64,13 +64,14 @@ inline int prp_stage_cols(int lm, int lg)
 // consecutive threads read consecutive words.
 // tfs/tis (lm == 12 only, else may be null): [G][3][256][2] Shoup pairs
 // (w, floor(w 2^32 / q)) of the plain roots at indices 1..255 (local levels 0..7).
-inline void prp_build_tables(int ln, uint32_t *tf, uint32_t *ti, PrpKernelArgs &proto, uint32_t *tfs = nullptr,
+// lg is the cluster split (2^lg CTAs per candidate; prp_lg_for(ln) by default).
+inline void prp_build_tables(int ln, int lg, uint32_t *tf, uint32_t *ti, PrpKernelArgs &proto, uint32_t *tfs = nullptr,
                              uint32_t *tis = nullptr)
 {
 	using namespace tables_detail;
 	static const uint32_t kQ[3] = { Q0, Q1, Q2 };
 	static const uint32_t kG[3] = { QGEN0, QGEN1, QGEN2 };
-	const int lg = prp_lg_for(ln), lm = ln - lg;
+	const int lm = ln - lg;
 	const size_t D = size_t(1) << ln, G = size_t(1) << lg, M = D / G;
 	// last local pass (same split as the kernel: passes of <= 4 levels, larger first)
 	const int np = (lm + 3) / 4, base = lm / np, extra = lm % np;

@@ -1,0 +1,200 @@
+"""Pools and the request server: many resident PRP tests at once.
+
+Neither has a counterpart in the reference, whose cyclog runs one vector of
+64 candidates of one degree to completion (cyclo/src/cyclo.h:457-478); both
+return, per test, the same verdict and RES64 as PrpEngine.run.  Every call goes
+through the C ABI of libctwin_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._native import CtwError, CtwResult, check, lib, ptr
+
+CTW_E_FULL = -6
+
+
+def result_dict(r: CtwResult) -> dict:
+    return {"tag": int(r.tag), "b": int(r.b), "log2_degree": int(r.log2_degree), "is_prp": bool(r.is_prp),
+            "res64": int(r.res64), "gl_ok": bool(r.gl_ok), "status": int(r.status), "slot": int(r.slot),
+            "t_submit": r.t_submit, "t_admit": r.t_admit, "t_done": r.t_done, "squarings": int(r.squarings)}
+
+
+def autotune(log2_degree: int, lanes: int):
+    """(log2_ctas, csize, us_per_squaring) the device picks for `lanes` candidates of degree 2^log2_degree."""
+    lg, cs, us = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+    check(lib().ctw_prp_autotune(log2_degree, lanes, ctypes.byref(lg), ctypes.byref(cs), ctypes.byref(us)))
+    return lg.value, cs.value, us.value
+
+
+def schedule(log2_degree: int, b: int, gl_block: int = 0):
+    """Tick program of one test (host only): (int32 array [ticks, 8], bit offset of the block sum)."""
+    L = lib()
+    r0 = ctypes.c_int()
+    n = L.ctw_pool_schedule(log2_degree, b, gl_block, None, 0, ctypes.byref(r0))
+    if n < 0:
+        check(n)
+    out = np.zeros((n, 8), dtype=np.int32)
+    check(0 if L.ctw_pool_schedule(log2_degree, b, gl_block, ptr(out), n, ctypes.byref(r0)) == n else -1)
+    return out, r0.value
+
+
+def slot_bytes(log2_degree: int) -> int:
+    return int(lib().ctw_pool_slot_bytes(log2_degree))
+
+
+class Pool:
+    """`slots` resident tests of degree 2^log2_degree (continuous batching)."""
+
+    def __init__(self, log2_degree: int, slots: int, log2_ctas: int = -1, csize: int = 0, base: int = 2,
+                 gl_block: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().ctw_pool_create(log2_degree, slots, log2_ctas, csize, base, gl_block, ctypes.byref(h)))
+        self._h = h
+        self.ln = log2_degree
+        self.D = 1 << log2_degree
+        self.slots = slots
+
+    def close(self):
+        if self._h:
+            lib().ctw_pool_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def admit(self, b: int, tag: int = 0) -> int | None:
+        """Slot of the new test, or None when the pool is full."""
+        rc = lib().ctw_pool_admit(self._h, int(b), int(tag))
+        if rc == CTW_E_FULL:
+            return None
+        if rc < 0:
+            check(rc)
+        return rc
+
+    def run(self, ticks: int = 1):
+        check(lib().ctw_pool_run(self._h, ticks))
+
+    def collect(self, wait: bool = False) -> int:
+        n = lib().ctw_pool_collect(self._h, 1 if wait else 0)
+        if n < 0:
+            check(n)
+        return n
+
+    def results(self) -> list[dict]:
+        out = []
+        buf = (CtwResult * 256)()
+        while True:
+            n = lib().ctw_pool_results(self._h, ctypes.cast(buf, ctypes.c_void_p), 256)
+            if n < 0:
+                check(n)
+            out += [result_dict(buf[i]) for i in range(n)]
+            if n < 256:
+                return out
+
+    def info(self) -> dict:
+        v = [ctypes.c_int() for _ in range(6)]
+        sq = ctypes.c_longlong()
+        check(lib().ctw_pool_info(self._h, *[ctypes.byref(x) for x in v], ctypes.byref(sq)))
+        keys = ["slots", "active", "in_flight", "gl_block", "log2_ctas", "csize"]
+        d = {k: x.value for k, x in zip(keys, v)}
+        d["squarings"] = sq.value
+        return d
+
+    def read_slot(self, slot: int, reg: int) -> np.ndarray:
+        out = np.zeros(self.D, dtype=np.int32)
+        check(lib().ctw_pool_read_slot(self._h, slot, reg, ptr(out)))
+        return out
+
+    @property
+    def stream(self) -> int:
+        return lib().ctw_pool_stream(self._h) or 0
+
+    def run_to_completion(self, ticks_per_call: int = 8) -> list[dict]:
+        """Run until every admitted test has finished; return their results."""
+        res = []
+        while True:
+            self.collect(wait=False)
+            res += self.results()
+            if self.info()["active"] == 0:
+                return res
+            self.run(ticks_per_call)
+            self.collect(wait=True)
+            res += self.results()
+
+
+class Server:
+    """Request loop over pools of every degree (continuous batching by size class)."""
+
+    def __init__(self, hbm_budget_bytes: int = 0, max_slots: int = 256, base: int = 2, ticks_per_launch: int = 2,
+                 autotune: bool = False):
+        h = ctypes.c_void_p()
+        check(lib().ctw_server_create(hbm_budget_bytes, max_slots, base, ticks_per_launch, 1 if autotune else 0,
+                                      ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().ctw_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, log2_degree: int, b: int, tag: int = 0):
+        check(lib().ctw_server_submit(self._h, log2_degree, int(b), int(tag)))
+
+    def prepare(self, log2_degree: int, slots: int = 0):
+        check(lib().ctw_server_prepare(self._h, log2_degree, slots))
+
+    def poll(self, max_results: int = 256, timeout_ms: int = 0) -> list[dict]:
+        buf = (CtwResult * max_results)()
+        n = lib().ctw_server_poll(self._h, ctypes.cast(buf, ctypes.c_void_p), max_results, timeout_ms)
+        if n < 0:
+            check(n)
+        return [result_dict(buf[i]) for i in range(n)]
+
+    def stats(self) -> dict:
+        v = [ctypes.c_longlong() for _ in range(4)]
+        nb = ctypes.c_size_t()
+        check(lib().ctw_server_stats(self._h, *[ctypes.byref(x) for x in v], ctypes.byref(nb)))
+        d = dict(zip(["submitted", "pending", "active", "finished"], [x.value for x in v]))
+        d["pool_bytes"] = nb.value
+        return d
+
+    def clock(self) -> float:
+        return float(lib().ctw_server_clock(self._h))
+
+    def drain(self, count: int, timeout_s: float = 600.0) -> list[dict]:
+        """Wait for `count` results (or raise after timeout_s of no progress)."""
+        import time
+        out: list[dict] = []
+        last = time.monotonic()
+        while len(out) < count:
+            got = self.poll(256, 50)
+            if got:
+                out += got
+                last = time.monotonic()
+            elif time.monotonic() - last > timeout_s:
+                raise CtwError(-2, f"server drain: {len(out)} of {count} results after {timeout_s} s without progress")
+        return out

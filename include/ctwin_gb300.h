@@ -44,6 +44,11 @@ typedef struct ctw_prp ctw_prp;
  * Replaces: engine ctor + allocMemory + createKernels (cyclo/src/engine.h:40-65,132)
  *           and transform ctor / initEngine roots (cyclo/src/transform.h:300-433). */
 int ctw_prp_create(int log2_degree, int lanes, ctw_prp **out);
+/* The same with an explicit cluster split: 2^log2_ctas CTAs per candidate
+ * (-1: the default split).  Registers and results do not depend on the split;
+ * it is an autotuning choice (ctw_prp_autotune).  CTW_E_ARG when the degree
+ * has no kernel for that split. */
+int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **out);
 int ctw_prp_destroy(ctw_prp *h);
 
 /* Carry chunk size, 8/16/32/64 (the reference's CSIZE, autotuned there,
@@ -128,6 +133,105 @@ long long ctw_prp_launches(ctw_prp *h);
  * synchronised the stream. */
 int ctw_prp_mul_noalloc(int log2_degree, int lanes, const uint32_t *b, const int32_t *x_dev,
                         const int32_t *y_dev, int32_t *z_dev, int csize, void *stream);
+
+/* Pick the cluster split and carry chunk of degree 2^log2_degree for `lanes`
+ * resident candidates by timing every supported (split, csize) pair on the
+ * device (the reference times its CSIZE candidates the same way,
+ * cyclo/src/transform.h:383-419).  Results are cached per (degree, lanes) for
+ * the life of the process.  Outputs may be NULL. */
+int ctw_prp_autotune(int log2_degree, int lanes, int *log2_ctas, int *csize, double *us_per_squaring);
+
+/* ------------------------------------------------------------------------ */
+/* Pools: many resident tests of one degree, each at its own bit position.  */
+/* No counterpart in the reference, which runs one vector of 64 candidates   */
+/* of one degree to completion (cyclo/src/cyclo.h:457-478).                  */
+/* ------------------------------------------------------------------------ */
+
+#define CTW_E_FULL (-6)       /* no free slot */
+
+/* One finished test (pool or server).  Times are seconds on the owner's clock
+ * (CLOCK_MONOTONIC of the process for pools, the server's clock for servers). */
+typedef struct ctw_result {
+	uint64_t tag;             /* caller's tag */
+	uint64_t res64;           /* RES64 of 2^(N-1) mod N (base 3: 3^(N-1)) */
+	uint32_t b;
+	int32_t log2_degree;
+	uint8_t is_prp;           /* residue == 1 */
+	uint8_t gl_ok;            /* Gerbicz-Li check passed */
+	int8_t status;            /* 0, or the CTW_E_* code of a failed test */
+	uint8_t reserved;
+	int32_t slot;
+	double t_submit, t_admit, t_done;
+	long long squarings;      /* squarings and multiplies run for this test */
+} ctw_result;
+
+typedef struct ctw_pool ctw_pool;
+
+/* A pool of `slots` tests of degree 2^log2_degree kept in HBM (registers,
+ * exponent bits, the multiply's scratch).  Every tick runs, for each active
+ * slot, gl_block squarings of its own exponent from its own bit position and
+ * its Gerbicz-Li multiply, so tests admitted at different times share each
+ * launch (continuous batching).  Ticks are queued as CUDA graphs on the pool's
+ * stream.  log2_ctas -1 and csize 0 take the default split and CSIZE 8;
+ * gl_block 0 takes the reference's rule (cyclo/src/cyclo.h:272) for a
+ * 20-bit b.  Results are bit-identical to ctw_prp_run's. */
+int ctw_pool_create(int log2_degree, int slots, int log2_ctas, int csize, uint32_t base, int gl_block,
+                    ctw_pool **out);
+int ctw_pool_destroy(ctw_pool *p);
+/* Device bytes a pool holds per slot at this degree (admission by footprint). */
+size_t ctw_pool_slot_bytes(int log2_degree);
+/* Admit a test of b (64 <= b < 2^31) into the lowest free slot; returns the
+ * slot (>= 0) or CTW_E_FULL.  The test starts with the next queued tick. */
+int ctw_pool_admit(ctw_pool *p, uint32_t b, uint64_t tag);
+/* Queue `ticks` ticks (asynchronous; blocks only while two graph launches of
+ * this pool are already in flight). */
+int ctw_pool_run(ctw_pool *p, int ticks);
+/* Retire the tests whose last tick has completed (wait != 0: wait for every
+ * queued tick first); returns the number of results waiting to be taken. */
+int ctw_pool_collect(ctw_pool *p, int wait);
+/* Take up to max results; returns the count. */
+int ctw_pool_results(ctw_pool *p, ctw_result *out, int max);
+/* Slots, active tests, queued-but-unfinished graph launches, the Gerbicz-Li
+ * block, split and csize in use, and squarings issued so far (any may be NULL). */
+int ctw_pool_info(ctw_pool *p, int *slots, int *active, int *in_flight, int *gl_block, int *log2_ctas, int *csize,
+                  long long *squarings);
+/* Copy register reg (0..3) of one slot to the host (after ctw_pool_collect
+ * with wait); for tests. */
+int ctw_pool_read_slot(ctw_pool *p, int slot, int reg, int32_t *out);
+void *ctw_pool_stream(ctw_pool *p);
+/* The tick program of one test, without a device: per tick 8 int32 words
+ * {aux, sq_count, sq_i_hi, mul_count, mul_in, mul_y, mul_out, 0}; sq_i_hi >=
+ * *r0 addresses the Gerbicz-Li block sum at bit *r0.  Returns the tick count
+ * (or the count needed when max_ticks is too small). */
+int ctw_pool_schedule(int log2_degree, uint32_t b, int gl_block, int32_t *ticks_out, int max_ticks, int *r0);
+
+/* ------------------------------------------------------------------------ */
+/* Server: a request loop over pools of every degree.  No counterpart in the */
+/* reference.                                                                */
+/* ------------------------------------------------------------------------ */
+
+typedef struct ctw_server ctw_server;
+
+/* Start a server thread.  hbm_budget_bytes bounds the pools' device memory
+ * (0: 80 % of the free memory); a request waits until its degree has a free
+ * slot, and a new pool is allocated only while the budget allows.
+ * max_slots caps one pool; ticks_per_launch sets the graph length (1..8);
+ * autotune != 0 picks split and csize per degree on first use. */
+int ctw_server_create(size_t hbm_budget_bytes, int max_slots, uint32_t base, int ticks_per_launch, int autotune,
+                      ctw_server **out);
+/* Queue a test (thread-safe).  8 <= log2_degree <= 18. */
+int ctw_server_submit(ctw_server *s, int log2_degree, uint32_t b, uint64_t tag);
+/* Create (and tune) the pool of a degree ahead of its first request. */
+int ctw_server_prepare(ctw_server *s, int log2_degree, int slots);
+/* Take up to max finished tests, waiting up to timeout_ms for the first. */
+int ctw_server_poll(ctw_server *s, ctw_result *out, int max, int timeout_ms);
+/* Submitted, pending (not admitted), active, finished counts; pool bytes allocated. */
+int ctw_server_stats(ctw_server *s, long long *submitted, long long *pending, long long *active, long long *finished,
+                     size_t *pool_bytes);
+/* Seconds since the server started (the clock of ctw_result times). */
+double ctw_server_clock(ctw_server *s);
+/* Stop the thread and free the pools. */
+int ctw_server_destroy(ctw_server *s);
 
 /* Measured 32-bit integer multiply-add throughput of the device (IMAD/s),
  * from an in-library probe kernel; the roofline denominator. */

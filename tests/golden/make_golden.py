@@ -7,8 +7,9 @@ has the reference source; the outputs are committed, the GPU tests only read the
                     (sieve/CPU/ctsieve.cpp, compiled unchanged into oracle/_ref/)
   sieve_files.json  md5 of cand_*.txt / sv_*.dat written by the reference's write(true)
   prp_gmp.json      GMP Fermat residues (RES64, PRP flag) for base 2 and 3, N+ and N-
+  pool_gmp.json     GMP Fermat residues of the pool / server cases (degrees 2^9..2^15)
 
-Usage:  python tests/golden/make_golden.py [--skip-slow]
+Usage:  python tests/golden/make_golden.py [--skip-slow] [--only pool]
 """
 from __future__ import annotations
 
@@ -74,12 +75,35 @@ def prp_case(args):
     return {"b": b, "n": ln, "base": base, "form": "-" if minus else "+", "res64": f"{r64:016X}", "prp": bool(prp)}
 
 
+def pool_jobs():
+    import random
+    jobs = []
+    # split / csize coverage at degrees 2^12..2^15 (small b keeps GMP and the GPU quick)
+    for ln in (12, 13, 14, 15):
+        for b in (64, 65, 100, 1000):
+            jobs.append((b, ln, 2, False))
+    jobs.append((77, 12, 3, False))
+    # server mixes: seeded b in [2^16, 2^20) at degrees 2^9..2^11
+    rng = random.Random(5)
+    for ln in (9, 10, 11):
+        for _ in range(24):
+            jobs.append((rng.randrange(1 << 16, 1 << 20), ln, 2, False))
+    return jobs
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-slow", action="store_true")
+    ap.add_argument("--only", choices=["pool"], default=None)
     args = ap.parse_args()
     from oracle import oracle as O
     O.build()
+    if args.only == "pool":
+        with mp.get_context("spawn").Pool(min(8, os.cpu_count() or 1)) as pool:
+            res = pool.map(prp_case, pool_jobs())
+        json.dump(res, open(os.path.join(HERE, "pool_gmp.json"), "w"), indent=0)
+        print("done", len(res), "pool cases")
+        return
     O.build_ref()
 
     json.dump(algo_kat(), open(os.path.join(HERE, "algo_kat.json"), "w"), indent=1)

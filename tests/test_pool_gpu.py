@@ -1,0 +1,156 @@
+"""Pools and the server on the GPU: every test's verdict and RES64 equal GMP's
+(tests/golden/pool_gmp.json), whatever the cluster split, carry chunk, slot
+or admission time, and a test's result is the same alone and in a mix."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = None
+
+
+def gold():
+    global GOLD
+    if GOLD is None:
+        here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pool_gmp.json")
+        GOLD = {(d["b"], d["n"], d["base"]): d for d in json.load(open(here)) if d["form"] == "+"}
+    return GOLD
+
+
+def expect(b, ln, base=2):
+    d = gold()[(b, ln, base)]
+    return d["prp"], int(d["res64"], 16)
+
+
+def check_results(res, ln, base=2):
+    for r in res:
+        assert r["status"] == 0, r
+        assert r["gl_ok"], r
+        assert (r["is_prp"], r["res64"]) == expect(r["b"], ln, base), r
+
+
+def server_cases(ln):
+    return sorted(b for (b, n, base) in gold() if n == ln and base == 2 and b >= 1 << 16)
+
+
+@pytest.mark.parametrize("ln,lg", [(12, 0), (12, 1), (12, 2), (12, 3), (13, 0), (13, 1), (13, 2), (13, 3), (13, 4),
+                                   (14, 0), (14, 1), (14, 2), (14, 4), (15, 3)])
+def test_pool_splits_match_gmp(native, ln, lg):
+    from ctwin_gb300 import Pool
+    bs = [64, 65, 100, 1000]
+    csize = 8 if lg % 2 == 0 else 16
+    with Pool(ln, 4, log2_ctas=lg, csize=csize) as p:
+        for i, b in enumerate(bs):
+            assert p.admit(b, tag=i) == i
+        res = p.run_to_completion()
+    assert sorted(r["b"] for r in res) == bs
+    check_results(res, ln)
+
+
+def test_pool_base3(native):
+    from ctwin_gb300 import Pool
+    with Pool(12, 2, base=3) as p:
+        p.admit(77, 1)
+        res = p.run_to_completion()
+    check_results(res, 12, base=3)
+
+
+def test_pool_continuous_admission(native):
+    """Tests admitted while others run, into slots freed by finished tests."""
+    from ctwin_gb300 import Pool
+    bs = server_cases(10)[:12]
+    got = []
+    with Pool(10, 4) as p:
+        queue = list(bs)
+        for _ in range(2):
+            p.admit(queue.pop(0))
+        while queue or p.info()["active"]:
+            p.run(3)
+            p.collect(wait=True)
+            got += p.results()
+            if queue and p.info()["active"] < 4:
+                assert p.admit(queue.pop(0)) is not None
+        got += p.results()
+    assert sorted(r["b"] for r in got) == sorted(bs)
+    check_results(got, 10)
+    assert max(r["slot"] for r in got) < 4
+
+
+def test_pool_full_and_args(native):
+    from ctwin_gb300 import Pool, CtwError
+    with Pool(9, 2) as p:
+        assert p.admit(100000) == 0 and p.admit(100001) == 1
+        assert p.admit(100002) is None
+        with pytest.raises(CtwError):
+            p.admit(63)
+    with pytest.raises(CtwError):
+        Pool(12, 2, log2_ctas=4)          # 256 coefficients per CTA on 16 CTAs: no kernel
+    with pytest.raises(CtwError):
+        Pool(13, 2, log2_ctas=4, csize=64)  # run of 32 columns shorter than the chunk
+
+
+def test_autotune(native):
+    from ctwin_gb300 import Pool, autotune
+    lg, cs, us = autotune(12, 64)
+    assert 0 <= lg <= 3 and cs in (8, 16, 32, 64) and us > 0
+    assert autotune(12, 64) == (lg, cs, us)           # cached
+    with Pool(12, 2, log2_ctas=lg, csize=cs) as p:
+        p.admit(100)
+        p.admit(1000)
+        check_results(p.run_to_completion(), 12)
+
+
+def test_server_mix_and_alone(native):
+    """Requests of degrees 2^9..2^11 interleaved; each result equals GMP and
+    equals the same request served alone."""
+    from ctwin_gb300 import Server
+    reqs = [(ln, b) for ln in (9, 10, 11) for b in server_cases(ln)]
+    rng = np.random.default_rng(3)
+    order = rng.permutation(len(reqs))
+    with Server(hbm_budget_bytes=1 << 30, max_slots=16, ticks_per_launch=2) as s:
+        for i in order:
+            ln, b = reqs[i]
+            s.submit(ln, b, tag=int(i))
+        res = s.drain(len(reqs), timeout_s=300)
+        st = s.stats()
+    assert st["finished"] == len(reqs) and st["pending"] == 0
+    by_tag = {r["tag"]: r for r in res}
+    assert sorted(by_tag) == list(range(len(reqs)))
+    for t, r in by_tag.items():
+        ln, b = reqs[t]
+        assert (r["log2_degree"], r["b"]) == (ln, b)
+        check_results([r], ln)
+        assert r["t_submit"] <= r["t_admit"] <= r["t_done"]
+    alone = {}
+    with Server(hbm_budget_bytes=1 << 30, max_slots=16) as s:
+        for t in (0, len(reqs) // 2, len(reqs) - 1):
+            ln, b = reqs[t]
+            s.submit(ln, b, tag=t)
+            r = s.drain(1, timeout_s=120)[0]
+            alone[t] = (r["is_prp"], r["res64"], r["gl_ok"])
+    for t, v in alone.items():
+        assert v == (by_tag[t]["is_prp"], by_tag[t]["res64"], by_tag[t]["gl_ok"])
+
+
+def test_server_budget_admission(native):
+    """A budget that holds one pool at a time: degrees take turns, all finish."""
+    from ctwin_gb300 import Server
+    from ctwin_gb300.pool import slot_bytes
+    # one one-slot pool of degree 2^10 (its slot plus 2 x 3 x 1024 words of
+    # root tables) fits, a second pool next to it does not
+    budget = slot_bytes(10) + 24 * 1024 + 1024
+    reqs = [(9, b) for b in server_cases(9)[:4]] + [(10, b) for b in server_cases(10)[:4]]
+    with Server(hbm_budget_bytes=budget, max_slots=4) as s:
+        for i, (ln, b) in enumerate(reqs):
+            s.submit(ln, b, tag=i)
+        res = s.drain(len(reqs), timeout_s=300)
+        assert s.stats()["pool_bytes"] <= budget
+    for r in res:
+        check_results([r], reqs[r["tag"]][0])
+    with Server(hbm_budget_bytes=1 << 16, max_slots=4) as s:
+        s.submit(12, 100003, tag=7)                 # no pool of degree 2^12 fits in 64 KiB
+        r = s.drain(1, timeout_s=60)[0]
+        assert r["status"] == -3 and r["tag"] == 7
