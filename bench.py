@@ -290,7 +290,7 @@ def run_batch(args):
     for p in pools.values():
         p.collect(wait=True)
     times = []
-    launches_per_step = sum(2 + (info[k]["gl_block"] + 63) // 64 for k in pools)
+    launches_per_step = sum(3 + (info[k]["gl_block"] + 63) // 64 for k in pools)   # moves x2, multiply, squarings
     with ClockSampler(0) as clk:
         torch.cuda.synchronize()
         for _ in range(args.steps):

@@ -661,38 +661,6 @@ __device__ __forceinline__ int64_t carry_chunk(uint32_t *X, int M, int c, int cs
 
 // Shared memory (words): planes [3][M], stage (cross levels) or chunk carries,
 // carry exchange, then the CTA's roots [3][M] forward and inverse when they fit.
-// Operands of one lane: from the launch, or from the lane's command.
-struct LaneView {
-	const int32_t *rin, *ry;
-	int32_t *rout;
-	long long i_hi;
-	int count;
-};
-
-__device__ __forceinline__ bool lane_view(const PrpKernelArgs &a, int lane, LaneView &v)
-{
-	if (!a.cmd)
-	{
-		v.rin = a.reg_in;
-		v.ry = a.reg_y;
-		v.rout = a.reg_out;
-		v.i_hi = a.i_hi;
-		v.count = a.count;
-		return true;
-	}
-	// a.i_hi / a.count cut the lane's squarings into launches: this launch runs
-	// squarings a.i_hi .. a.i_hi + a.count - 1 of the command
-	const PrpLaneCmd c = a.cmd[lane];
-	const int count = min(c.count - (int)a.i_hi, a.count);
-	if (count <= 0) return false;
-	v.rin = a.regs + c.r_in * a.reg_stride;
-	v.ry = a.regs + c.r_y * a.reg_stride;
-	v.rout = a.regs + c.r_out * a.reg_stride;
-	v.i_hi = (long long)c.i_hi - a.i_hi;
-	v.count = count;
-	return true;
-}
-
 __host__ __device__ __forceinline__ size_t smem_stage_words(int lm, int lg, int scols)
 {
 	const size_t stage = lg > 0 ? (size_t)4 * ((size_t)1 << lg) * scols : 0;
@@ -710,8 +678,6 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 	int g = 0;
 	if constexpr (LG > 0) g = (int)cg::this_cluster().block_rank();
 	const int lane = blockIdx.x / G;
-	LaneView lv;
-	if (!lane_view(a, lane, lv)) return;   // idle lane: the whole cluster leaves
 	const int ncl = M / a.csize, sb = a.swz_b;
 
 	uint32_t *X = sm;                                           // [3][M] swizzled planes
@@ -845,18 +811,18 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 
 	if (a.op == OP_MUL)
 	{
-		load_digits(lv.ry);
+		load_digits(a.reg_y);
 		transform_and_normalize(LM_FWD_ONLY, 1);
 		__syncthreads();
-		load_digits(lv.rin);
+		load_digits(a.reg_in);
 		transform_and_normalize(LM_MUL, 1);
 	}
 	else
 	{
-		load_digits(lv.rin);
-		for (int it = 0; it < lv.count; ++it)
+		load_digits(a.reg_in);
+		for (int it = 0; it < a.count; ++it)
 		{
-			const long long i = lv.i_hi - it;
+			const long long i = a.i_hi - it;
 			int bit = 0;
 			if (a.use_dupmask) bit = (int)((a.dupmask[lane >> 6] >> (lane & 63)) & 1);
 			else if (i >= 0 && (i >> 5) < a.nwords) bit = (a.bits[(size_t)lane * a.nwords + (i >> 5)] >> (i & 31)) & 1;
@@ -864,7 +830,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 		}
 	}
 	// digits -> global
-	for (int t = tid; t < M; t += nt) lv.rout[lane_off + t] = (int32_t)X[swz(t, sb)];
+	for (int t = tid; t < M; t += nt) a.reg_out[lane_off + t] = (int32_t)X[swz(t, sb)];
 	if (err) atomicOr(a.status, err);
 	// No CTA may leave while another can still read its shared memory.
 	csync<LG>();
@@ -898,8 +864,6 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 	cg::cluster_group cl = cg::this_cluster();
 	const int g = (int)cl.block_rank();
 	const int lane = blockIdx.x / G;
-	LaneView lv;
-	if (!lane_view(a, lane, lv)) return;   // idle lane: the whole cluster leaves
 	const int csz = a.csize, sb = a.swz_b;
 	const int runc = MG / csz;                                  // chunks per run
 	const int ncl = G * runc;                                   // chunks held by this CTA
@@ -1131,18 +1095,18 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 
 	if (a.op == OP_MUL)
 	{
-		load_digits(lv.ry);
+		load_digits(a.reg_y);
 		transform_and_normalize(LM_FWD_ONLY, 1);
 		cl.sync();                // peers may still be pulling y's columns
-		load_digits(lv.rin);
+		load_digits(a.reg_in);
 		transform_and_normalize(LM_MUL, 1);
 	}
 	else
 	{
-		load_digits(lv.rin);
-		for (int it = 0; it < lv.count; ++it)
+		load_digits(a.reg_in);
+		for (int it = 0; it < a.count; ++it)
 		{
-			const long long i = lv.i_hi - it;
+			const long long i = a.i_hi - it;
 			int bit = 0;
 			if (a.use_dupmask) bit = (int)((a.dupmask[lane >> 6] >> (lane & 63)) & 1);
 			else if (i >= 0 && (i >> 5) < a.nwords) bit = (a.bits[(size_t)lane * a.nwords + (i >> 5)] >> (i & 31)) & 1;
@@ -1152,7 +1116,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 	for (int e = tid; e < M; e += nt)
 	{
 		const int h = e / MG, tt = e - h * MG;
-		lv.rout[lane_base + (size_t)h * M + cb + tt] = (int32_t)XC[pc(h, tt)];
+		a.reg_out[lane_base + (size_t)h * M + cb + tt] = (int32_t)XC[pc(h, tt)];
 	}
 	if (err) atomicOr(a.status, err);
 	cl.sync();                    // peers may still read this CTA's carries
@@ -1248,30 +1212,40 @@ cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t s
 	}
 }
 
-// Per-lane register set-up of a pool tick, ahead of its squarings: bit 0 of
-// aux saves register 0 in register 3, bit 1 sets register 0 to aux_arg, bit 2
-// sets register 1 to aux_arg (the value 1 of the reference's engine::set).
-__global__ void prp_aux_kernel(const PrpLaneCmd *cmd, int32_t *regs, long long stride, int D)
+// Per-lane register moves of a pool tick (PrpLaneAux::ops), in bit order:
+// bit 0 r0 = r1 = arg; bit 1 r3 = r1; bit 2 r2 = r0; bit 3 r4 = r1;
+// bit 4 r0 = arg; bit 5 r1 = r3; bit 6 r0 = r1; bit 7 r5 = r0.
+// (arg is the value 1 of the reference's engine::set.)  Registers are planes
+// of `stride` words; lane l's register r starts at regs + r * stride + l * D.
+__global__ void prp_aux_kernel(const PrpLaneAux *aux, int32_t *regs, long long stride, int D)
 {
 	const int lane = blockIdx.y;
-	const PrpLaneCmd c = cmd[lane];
-	if (c.aux == 0) return;
-	int32_t *r0 = regs + (size_t)lane * D, *r1 = r0 + stride, *r3 = r0 + 3 * stride;
+	const PrpLaneAux c = aux[lane];
+	if (c.ops == 0) return;
+	int32_t *r[6];
+#pragma unroll
+	for (int k = 0; k < 6; ++k) r[k] = regs + k * stride + (size_t)lane * D;
 	for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < D; j += gridDim.x * blockDim.x)
 	{
-		const int32_t v = (j == 0) ? (int32_t)c.aux_arg : 0;
-		if (c.aux & 1) r3[j] = r0[j];
-		if (c.aux & 2) r0[j] = v;
-		if (c.aux & 4) r1[j] = v;
+		const int32_t v = (j == 0) ? (int32_t)c.arg : 0;
+		int32_t x0 = r[0][j], x1 = r[1][j], x3 = r[3][j];
+		if (c.ops & 1) { x0 = v; x1 = v; r[0][j] = v; r[1][j] = v; }
+		if (c.ops & 2) { x3 = x1; r[3][j] = x1; }
+		if (c.ops & 4) r[2][j] = x0;
+		if (c.ops & 8) r[4][j] = x1;
+		if (c.ops & 16) { x0 = v; r[0][j] = v; }
+		if (c.ops & 32) { x1 = x3; r[1][j] = x3; }
+		if (c.ops & 64) { x0 = x1; r[0][j] = x1; }
+		if (c.ops & 128) r[5][j] = x0;
 	}
 }
 
-cudaError_t prp_aux_launch(const PrpLaneCmd *cmd, int32_t *regs, long long reg_stride, int ln, int lanes,
+cudaError_t prp_aux_launch(const PrpLaneAux *aux, int32_t *regs, long long reg_stride, int ln, int lanes,
                            cudaStream_t stream)
 {
 	const int D = 1 << ln, threads = 256;
 	const int gx = D / (threads * 4) > 0 ? D / (threads * 4) : 1;
-	prp_aux_kernel<<<dim3(gx, lanes), threads, 0, stream>>>(cmd, regs, reg_stride, D);
+	prp_aux_kernel<<<dim3(gx, lanes), threads, 0, stream>>>(aux, regs, reg_stride, D);
 	return cudaGetLastError();
 }
 

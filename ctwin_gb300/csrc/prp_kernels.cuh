@@ -11,18 +11,22 @@ constexpr int MAX_INLINE_LANES = 4096;  // lanes whose dup bits fit the launch p
 
 enum PrpOp : int { OP_SQUARE = 0, OP_MUL = 1 };
 
-// Per-lane command of a pool launch (PrpKernelArgs::cmd != null).  Every lane
-// of one launch runs the same operation, but from its own registers and, for
-// squarings, its own exponent position and count; a lane with count <= 0 is
-// idle (all CTAs of its cluster return at once).
-struct PrpLaneCmd {
-	int32_t count;              // OP_SQUARE: squarings; OP_MUL: > 0 to take part
-	int32_t i_hi;               // OP_SQUARE: index of the first bit in this lane's exponent words
-	uint8_t r_in, r_y, r_out;   // register indices into regs (reg_stride words apart)
-	uint8_t aux;                // prp_aux_launch: bit 0 copy r0 -> r3, bit 1 r0 <- aux_arg, bit 2 r1 <- aux_arg
-	uint32_t aux_arg;
+// Per-lane register moves of a pool tick (prp_aux_launch): ops is a bit mask
+// executed in bit order, arg the value written by the set operations.
+struct PrpLaneAux {
+	uint32_t ops;
+	uint32_t arg;
 };
-static_assert(sizeof(PrpLaneCmd) == 16, "PrpLaneCmd is one 16-byte load");
+enum PrpAuxOp : uint32_t {
+	AUX_INIT = 1,          // r0 = r1 = arg
+	AUX_SAVE_D = 2,        // r3 = r1          d(t)
+	AUX_SAVE_X = 4,        // r2 = r0          the result
+	AUX_SAVE_D1 = 8,       // r4 = r1          d(t+1)
+	AUX_SET_Y = 16,        // r0 = arg         verify accumulator
+	AUX_LOAD_D = 32,       // r1 = r3          d(t) as multiply operand
+	AUX_TAKE_PRODUCT = 64, // r0 = r1          y <- y * d(t)
+	AUX_SAVE_Y = 128,      // r5 = r0          verify result
+};
 
 struct PrpKernelArgs {
 	const int32_t *reg_in;      // [lanes][D] digits of x
@@ -36,9 +40,8 @@ struct PrpKernelArgs {
 	const uint32_t *lane_b;     // [lanes][4] = b, floor(2^(s+32)/b), s = ilog2(b)-1, 1 if 64-bit carries are exact for b
 	const uint32_t *bits;       // [lanes][nwords] exponent bits
 	uint32_t *status;           // error flags (0 = ok)
-	long long i_hi;             // first (most significant) bit index processed; with cmd: squarings of
-	                            // the lane's command skipped by earlier launches of the same tick
-	int count;                  // squarings in this launch (OP_SQUARE); with cmd: the most per lane
+	long long i_hi;             // first (most significant) bit index processed
+	int count;                  // squarings in this launch (OP_SQUARE)
 	int nwords;
 	int lm;                     // log2 of coefficients per CTA
 	int csize;                  // carry chunk (8..64), as the reference's CSIZE
@@ -56,9 +59,6 @@ struct PrpKernelArgs {
 	uint32_t tcfq[3][MAX_G];    // their Shoup quotients floor(w 2^32 / q)
 	uint32_t tci[3][MAX_G];     // cross-CTA inverse roots, plain
 	uint32_t tciq[3][MAX_G];
-	const PrpLaneCmd *cmd;      // per-lane commands, or null for a uniform launch
-	int32_t *regs;              // register file [r][lanes][D] addressed by cmd
-	long long reg_stride;       // words between two registers of regs
 	int use_dupmask;            // 1: the bit of lane l is bit l of dupmask (count == 1)
 	uint64_t dupmask[MAX_INLINE_LANES / 64];
 };
@@ -76,8 +76,9 @@ int prp_threads(int lm);
 // Whether a cluster split D = 2^lg CTAs x 2^lm coefficients has a kernel.
 bool prp_split_supported(int lm, int lg);
 cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t stream);
-// Register set-up of a pool tick (PrpLaneCmd::aux) for lanes of degree 2^ln.
-cudaError_t prp_aux_launch(const PrpLaneCmd *cmd, int32_t *regs, long long reg_stride, int ln, int lanes,
+// Register moves of a pool tick (PrpLaneAux) for lanes of degree 2^ln; six
+// register planes `reg_stride` words apart.
+cudaError_t prp_aux_launch(const PrpLaneAux *aux, int32_t *regs, long long reg_stride, int ln, int lanes,
                            cudaStream_t stream);
 
 // Integer-multiply throughput probe (roofline denominator): returns IMAD/s.

@@ -1,24 +1,27 @@
 // Pools of resident PRP tests of one degree (continuous batching) and the
 // autotuner of the cluster split and carry chunk.
 //
-// A pool keeps, for each of its slots, four registers, the exponent bits, the
-// Gerbicz-Li block sum and the multiply's scratch in HBM.  Each slot runs the
-// program of cyclo::check (cyclo/src/cyclo.h:252-377) as a sequence of ticks:
+// A pool keeps six registers and the multiply's scratch per slot in HBM.  Each
+// slot runs the program of cyclo::check (cyclo/src/cyclo.h:252-377) as ticks
+// of B squarings (B = the Gerbicz-Li block):
 //
-//   main      B squarings of x = reg0 over bits pos .. pos-B+1 of E, then
-//             d <- d * x (reg1) at every block boundary but the last, where
-//             reg2 <- d * x (d(t+1)) instead;
-//   verify 1  reg3 <- reg0 (the result), reg0 <- 1, squarings over the bits of
-//             the block sum above B, reg0 <- reg0 * d(t);
-//   verify 2  B squarings over the low B bits of the block sum.
+//   main      nb ticks over E padded with leading zero bits to nb * B bits
+//             (x stays 1 over the padding, so every checkpoint is where the
+//             reference puts it); after each, d <- d * x; before the last,
+//             d(t) is saved, so the last multiply leaves d(t+1);
+//   verify    kh ticks over the bits of the block sum above B (zero-padded),
+//             from y = 1, then y <- y * d(t); one tick over its low B bits.
 //
-// E is padded with leading zero bits to a multiple of B, so every block, and
-// every Gerbicz-Li checkpoint, is where the reference puts it (x stays 1 over
-// the padding).  One tick is three launches over all slots (register set-up,
-// squarings, multiply) driven by per-slot commands, so slots admitted at
-// different times share every launch.  Ticks are replayed from CUDA graphs.
+// Every launch of a tick is uniform over the pool's lanes (the engine's own
+// squaring and multiply launches): the B exponent bits of each slot's tick are
+// cut on the host into a per-tick staging row, and the per-slot register
+// moves run in a small kernel before the squarings and after the multiply.
+// Idle and finished slots square and multiply values nobody reads.  Ticks are
+// replayed from CUDA graphs; the host uploads each launch's staging rows and
+// register moves with the graph.
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -54,21 +57,13 @@ int gl_block_for(long long i0)
 
 int default_gl_block(int ln) { return gl_block_for(((long long)20 << ln) - 1); }
 
-// Exponent words of one slot: E (b < 2^31, so below 2^(31 D)) padded to a
-// multiple of B, then the block sum at word ewE.
-void slot_words(int ln, int B, int &ewE, int &ewR)
-{
-	const long long D = 1LL << ln;
-	ewE = (int)((31 * D + B + 31) / 32) + 1;
-	ewR = (B + 64 + 31) / 32 + 1;
-}
+static int stage_words(int B) { return (B + 31) / 32; }
 
 size_t pool_slot_bytes(int ln, int B)
 {
-	int ewE, ewR;
-	slot_words(ln, B, ewE, ewR);
 	const size_t D = (size_t)1 << ln;
-	return 4 * D * 4 + 3 * D * 4 + (size_t)(ewE + ewR) * 4 + 16 + 2 * (size_t)POOL_TMAX * 3 * sizeof(PrpLaneCmd);
+	return (size_t)POOL_REGS * D * 4 + 3 * D * 4 + 16 +
+	       2 * (size_t)POOL_TMAX * ((size_t)stage_words(B) * 4 + 2 * sizeof(PrpLaneAux));
 }
 
 size_t pool_bytes_estimate(int ln, int lg, int slots, int B)
@@ -85,78 +80,64 @@ void slot_prepare(PreparedTest &t, int ln, int B)
 	t.B = B;
 }
 
-void slot_start(PoolSlot &s, const PreparedTest &t, uint64_t tag)
+void slot_start(PoolSlot &s, PreparedTest &&t, uint64_t tag)
 {
-	const long long L = (long long)big_bitlen(t.E);
-	const long long P = ((L + t.B - 1) / t.B) * t.B;
-	s.state = SLOT_MAIN;
-	s.fresh = true;
-	s.pos = (P > 0 ? P : t.B) - 1;
-	s.j0 = (int)big_bitlen(t.res) - 1;
+	const int B = t.B;
+	const long long L = std::max<long long>(1, (long long)big_bitlen(t.E));
+	const long long rl = (long long)big_bitlen(t.res);
+	s.state = SLOT_ACTIVE;
+	s.tk = 0;
+	s.nb = (int)((L + B - 1) / B);
+	s.P = (long long)s.nb * B;
+	s.kh = (int)std::max<long long>(1, (rl - B + B - 1) / B);
 	s.tag = tag;
 	s.b = t.b;
 	s.squarings = 0;
 	s.done_seq = -1;
+	s.t = std::move(t);
 }
 
-// Commands of one slot for one tick; returns true when this tick finishes the test.
-bool slot_tick(PoolSlot &s, int B, int r0, PrpLaneCmd &aux, PrpLaneCmd &sq, PrpLaneCmd &mul)
+SlotTick slot_tick(PoolSlot &s, int B)
 {
-	aux = PrpLaneCmd{};
-	sq = PrpLaneCmd{};
-	mul = PrpLaneCmd{};
-	switch (s.state)
+	SlotTick k;
+	const int t = s.tk++;
+	if (t < s.nb)
 	{
-	case SLOT_MAIN:
-		if (s.fresh)
-		{
-			aux.aux = 2 | 4;   // x = 1, d = 1
-			aux.aux_arg = 1;
-			s.fresh = false;
-		}
-		sq.count = B;
-		sq.i_hi = (int32_t)s.pos;
-		sq.r_in = sq.r_out = 0;
-		mul.count = 1;
-		mul.r_in = 0;
-		mul.r_y = 1;
-		if (s.pos - B + 1 > 0)
-		{
-			mul.r_out = 1;                 // d <- d * x at a block boundary
-			s.pos -= B;
-		}
-		else
-		{
-			mul.r_out = 2;                 // d(t+1) = d(t) * x
-			s.state = SLOT_VERIFY1;
-		}
-		s.squarings += B + 1;
-		return false;
-	case SLOT_VERIFY1:
-		aux.aux = 1 | 2;                   // reg3 <- result, reg0 <- 1
-		aux.aux_arg = 1;
-		if (s.j0 >= B)
-		{
-			sq.count = s.j0 - B + 1;
-			sq.i_hi = r0 + s.j0;
-			s.squarings += sq.count;
-		}
-		mul.count = 1;
-		mul.r_in = 0;
-		mul.r_y = 1;
-		mul.r_out = 0;
-		s.squarings += 1;
-		s.state = SLOT_VERIFY2;
-		return false;
-	case SLOT_VERIFY2:
-		sq.count = B;
-		sq.i_hi = r0 + B - 1;
-		s.squarings += B;
-		s.state = SLOT_FINISHED;
-		return true;
-	default:
-		return false;
+		k.source = 0;
+		k.lo = s.P - (long long)(t + 1) * B;
+		if (t == 0) k.before |= AUX_INIT;
+		if (t == s.nb - 1) k.before |= AUX_SAVE_D;
 	}
+	else if (t < s.nb + s.kh)
+	{
+		const int j = t - s.nb;
+		k.source = 1;
+		k.lo = (long long)(s.kh - j) * B;
+		if (j == 0) k.before |= AUX_SAVE_X | AUX_SAVE_D1 | AUX_SET_Y;
+		if (j == s.kh - 1)
+		{
+			k.before |= AUX_LOAD_D;
+			k.after |= AUX_TAKE_PRODUCT;
+		}
+	}
+	else
+	{
+		k.source = 1;
+		k.lo = 0;
+		k.after |= AUX_SAVE_Y;
+		k.last = true;
+		s.state = SLOT_FINISHED;
+	}
+	s.squarings += B + 1;
+	return k;
+}
+
+// Bits [lo, lo + B) of v into nw words (bit 0 of word 0 = bit lo).
+static void bit_slice(const Big &v, long long lo, int B, uint32_t *out, int nw)
+{
+	memset(out, 0, (size_t)nw * 4);
+	for (int k = 0; k < B; ++k)
+		if (big_bit(v, lo + k)) out[k >> 5] |= 1u << (k & 31);
 }
 
 }  // namespace ctw
@@ -164,18 +145,19 @@ bool slot_tick(PoolSlot &s, int B, int r0, PrpLaneCmd &aux, PrpLaneCmd &sq, PrpL
 using namespace ctw;
 
 struct ctw_pool {
-	int ln = 0, lg = 0, lm = 0, slots = 0, csize = 8, B = 0;
+	int ln = 0, lg = 0, lm = 0, slots = 0, csize = 8, B = 0, nws = 0;
 	uint32_t base = 2;
 	size_t D = 0, M = 0, G = 1;
 	int tw_smem = 0;
-	int ewE = 0, ewR = 0, nwords = 0, r0 = 0;
 	cudaStream_t stream = nullptr, cap_stream = nullptr, rb_stream = nullptr;
-	int32_t *d_regs = nullptr;                 // [4][slots][D]
+	int32_t *d_regs = nullptr;                 // [POOL_REGS][slots][D]
 	uint32_t *d_scratch = nullptr, *d_tf = nullptr, *d_ti = nullptr, *d_tfs = nullptr, *d_tis = nullptr;
-	uint32_t *d_laneb = nullptr, *d_exp = nullptr, *d_status = nullptr;
-	PrpLaneCmd *d_cmd[2] = { nullptr, nullptr };
-	PrpLaneCmd *h_cmd[2] = { nullptr, nullptr };   // pinned [POOL_TMAX][3][slots]
-	uint32_t *h_stage = nullptr;                    // pinned [slots][4 + nwords]
+	uint32_t *d_laneb = nullptr, *d_status = nullptr;
+	uint32_t *d_stage[2] = { nullptr, nullptr };    // [POOL_TMAX][slots][nws] exponent bits per tick
+	PrpLaneAux *d_aux[2] = { nullptr, nullptr };    // [POOL_TMAX][2][slots] moves before / after
+	uint32_t *h_stage[2] = { nullptr, nullptr };    // pinned mirrors
+	PrpLaneAux *h_aux[2] = { nullptr, nullptr };
+	uint32_t *h_laneb = nullptr;                    // pinned [slots][4]
 	int32_t *h_read = nullptr;                      // pinned [3][D]
 	cudaEvent_t ev[2] = { nullptr, nullptr };
 	bool ev_pending[2] = { false, false };
@@ -189,6 +171,7 @@ struct ctw_pool {
 	int active = 0;
 	long long squarings = 0;
 	size_t bytes = 0;
+	bool direct = false;     // CTW_POOL_DIRECT=1: direct launches, each checked (diagnostics)
 };
 
 namespace {
@@ -206,27 +189,40 @@ cudaError_t dmalloc(T **p, size_t bytes, size_t &total)
 	return cudaMalloc((void **)p, bytes);
 }
 
+void lane_params(uint32_t b, size_t D, uint32_t *lb)
+{
+	const int sh = (31 - __builtin_clz(b)) - 1;
+	lb[0] = b;
+	lb[1] = (uint32_t)(((uint64_t)1 << (sh + 32)) / b);
+	lb[2] = (uint32_t)sh;
+	lb[3] = (8.0 * (double)D * (double)b * (double)b < 4.611686018427388e18) ? 1u : 0u;
+}
+
 int pool_init(ctw_pool *p)
 {
-	const size_t D = p->D, S = (size_t)p->slots;
+	const size_t D = p->D, S = (size_t)p->slots, nws = (size_t)p->nws;
 	size_t &tot = p->bytes;
 	if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
 	    cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
 	    cudaStreamCreateWithFlags(&p->rb_stream, cudaStreamNonBlocking) != cudaSuccess)
 		return fail(CTW_E_CUDA, "pool stream creation failed");
-	if (dmalloc(&p->d_regs, 4 * S * D * 4, tot) != cudaSuccess || dmalloc(&p->d_scratch, S * 3 * D * 4, tot) != cudaSuccess ||
-	    dmalloc(&p->d_laneb, S * 16, tot) != cudaSuccess || dmalloc(&p->d_exp, S * (size_t)p->nwords * 4, tot) != cudaSuccess ||
-	    dmalloc(&p->d_status, 4, tot) != cudaSuccess ||
-	    dmalloc(&p->d_cmd[0], (size_t)POOL_TMAX * 3 * S * sizeof(PrpLaneCmd), tot) != cudaSuccess ||
-	    dmalloc(&p->d_cmd[1], (size_t)POOL_TMAX * 3 * S * sizeof(PrpLaneCmd), tot) != cudaSuccess)
+	const size_t stage_bytes = (size_t)POOL_TMAX * S * nws * 4, aux_bytes = (size_t)POOL_TMAX * 2 * S * sizeof(PrpLaneAux);
+	if (dmalloc(&p->d_regs, POOL_REGS * S * D * 4, tot) != cudaSuccess ||
+	    dmalloc(&p->d_scratch, S * 3 * D * 4, tot) != cudaSuccess || dmalloc(&p->d_laneb, S * 16, tot) != cudaSuccess ||
+	    dmalloc(&p->d_status, 4, tot) != cudaSuccess || dmalloc(&p->d_stage[0], stage_bytes, tot) != cudaSuccess ||
+	    dmalloc(&p->d_stage[1], stage_bytes, tot) != cudaSuccess || dmalloc(&p->d_aux[0], aux_bytes, tot) != cudaSuccess ||
+	    dmalloc(&p->d_aux[1], aux_bytes, tot) != cudaSuccess)
 		return fail(CTW_E_NOMEM, "pool of %d slots at degree 2^%d: device allocation failed", p->slots, p->ln);
-	if (cudaMallocHost(&p->h_cmd[0], (size_t)POOL_TMAX * 3 * S * sizeof(PrpLaneCmd)) != cudaSuccess ||
-	    cudaMallocHost(&p->h_cmd[1], (size_t)POOL_TMAX * 3 * S * sizeof(PrpLaneCmd)) != cudaSuccess ||
-	    cudaMallocHost(&p->h_stage, S * (4 + (size_t)p->nwords) * 4) != cudaSuccess ||
-	    cudaMallocHost(&p->h_read, 3 * D * 4) != cudaSuccess)
+	if (cudaMallocHost(&p->h_stage[0], stage_bytes) != cudaSuccess ||
+	    cudaMallocHost(&p->h_stage[1], stage_bytes) != cudaSuccess ||
+	    cudaMallocHost(&p->h_aux[0], aux_bytes) != cudaSuccess || cudaMallocHost(&p->h_aux[1], aux_bytes) != cudaSuccess ||
+	    cudaMallocHost(&p->h_laneb, S * 16) != cudaSuccess || cudaMallocHost(&p->h_read, 3 * D * 4) != cudaSuccess)
 		return fail(CTW_E_NOMEM, "pool pinned host allocation failed");
-	POOL_CUDA(cudaMemset(p->d_regs, 0, 4 * S * D * 4));
-	POOL_CUDA(cudaMemset(p->d_laneb, 0, S * 16));
+	// every slot holds valid numbers from the start: registers 0, b = 2^16 + 1
+	for (size_t s = 0; s < S; ++s) lane_params(65537u, D, p->h_laneb + 4 * s);
+	POOL_CUDA(cudaMemcpy(p->d_laneb, p->h_laneb, S * 16, cudaMemcpyHostToDevice));
+	POOL_CUDA(cudaMemset(p->d_regs, 0, POOL_REGS * S * D * 4));
+	POOL_CUDA(cudaMemset(p->d_scratch, 0, S * 3 * D * 4));
 	POOL_CUDA(cudaMemset(p->d_status, 0, 4));
 	POOL_CUDA(cudaEventCreateWithFlags(&p->ev[0], cudaEventDisableTiming));
 	POOL_CUDA(cudaEventCreateWithFlags(&p->ev[1], cudaEventDisableTiming));
@@ -258,13 +254,68 @@ int pool_init(ctw_pool *p)
 	a.tw_smem = p->tw_smem;
 	a.narrow = 0;                 // per lane (lane_b[3])
 	a.scratch = p->d_scratch;
-	a.bits = p->d_exp;
-	a.nwords = p->nwords;
-	a.regs = p->d_regs;
-	a.reg_stride = (long long)S * (long long)D;
 	a.use_dupmask = 0;
 	POOL_CUDA(cudaDeviceSynchronize());
 	return CTW_OK;
+}
+
+int32_t *reg_plane(ctw_pool *p, int r) { return p->d_regs + (size_t)r * p->slots * p->D; }
+
+// The launches of T ticks from buffer k over `lanes` lanes: per tick the
+// moves before, the squarings (uniform launches of at most POOL_SQ_CHUNK),
+// the multiply d <- x * d, the moves after.  check != 0 synchronises after
+// each launch and names the first one that fails.
+cudaError_t issue_ticks(ctw_pool *p, int k, int T, int lanes, cudaStream_t cs, bool check, const char **what)
+{
+	const size_t S = (size_t)p->slots;
+	const long long stride = (long long)S * (long long)p->D;
+	cudaError_t e = cudaSuccess;
+	auto step = [&](const char *name) {
+		if (e == cudaSuccess && check) e = cudaStreamSynchronize(cs);
+		if (e != cudaSuccess && !*what) *what = name;
+	};
+	for (int t = 0; t < T && e == cudaSuccess; ++t)
+	{
+		const PrpLaneAux *aux = p->d_aux[k] + (size_t)t * 2 * S;
+		e = prp_aux_launch(aux, p->d_regs, stride, p->ln, lanes, cs);
+		step("register moves");
+		PrpKernelArgs a = p->proto;
+		a.op = OP_SQUARE;
+		a.reg_in = reg_plane(p, 0);
+		a.reg_out = reg_plane(p, 0);
+		a.bits = p->d_stage[k] + (size_t)t * S * p->nws;
+		a.nwords = p->nws;
+		for (int off = 0; off < p->B && e == cudaSuccess; off += POOL_SQ_CHUNK)
+		{
+			a.i_hi = p->B - 1 - off;
+			a.count = std::min(POOL_SQ_CHUNK, p->B - off);
+			e = prp_launch(a, p->lg, lanes, cs);
+			step("squarings");
+		}
+		if (e != cudaSuccess) break;
+		a.op = OP_MUL;
+		a.reg_in = reg_plane(p, 0);
+		a.reg_y = reg_plane(p, 1);
+		a.reg_out = reg_plane(p, 1);
+		a.count = 1;
+		a.i_hi = 0;
+		a.bits = nullptr;
+		e = prp_launch(a, p->lg, lanes, cs);
+		step("multiply");
+		if (e != cudaSuccess) break;
+		e = prp_aux_launch(aux + S, p->d_regs, stride, p->ln, lanes, cs);
+		step("register moves");
+	}
+	return e;
+}
+
+cudaError_t upload(ctw_pool *p, int k, int T, cudaStream_t cs)
+{
+	const size_t S = (size_t)p->slots;
+	cudaError_t e = cudaMemcpyAsync(p->d_aux[k], p->h_aux[k], (size_t)T * 2 * S * sizeof(PrpLaneAux),
+	                                cudaMemcpyHostToDevice, cs);
+	if (e != cudaSuccess) return e;
+	return cudaMemcpyAsync(p->d_stage[k], p->h_stage[k], (size_t)T * S * p->nws * 4, cudaMemcpyHostToDevice, cs);
 }
 
 int get_graph(ctw_pool *p, int k, int T, int lanes, cudaGraphExec_t &exec)
@@ -276,34 +327,11 @@ int get_graph(ctw_pool *p, int k, int T, int lanes, cudaGraphExec_t &exec)
 		exec = it->second;
 		return CTW_OK;
 	}
-	const size_t S = (size_t)p->slots;
 	cudaStream_t cs = p->cap_stream;
 	POOL_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
-	cudaError_t e = cudaMemcpyAsync(p->d_cmd[k], p->h_cmd[k], (size_t)T * 3 * S * sizeof(PrpLaneCmd),
-	                                cudaMemcpyHostToDevice, cs);
-	for (int t = 0; t < T && e == cudaSuccess; ++t)
-	{
-		PrpLaneCmd *c = p->d_cmd[k] + (size_t)t * 3 * S;
-		e = prp_aux_launch(c, p->d_regs, p->proto.reg_stride, p->ln, lanes, cs);
-		if (e != cudaSuccess) break;
-		PrpKernelArgs a = p->proto;
-		a.op = OP_SQUARE;
-		a.cmd = c + S;
-		// squarings in launches of at most POOL_SQ_CHUNK, so that pools of
-		// other degrees on other streams interleave with long ticks
-		for (int off = 0; off < p->B && e == cudaSuccess; off += POOL_SQ_CHUNK)
-		{
-			a.i_hi = off;
-			a.count = POOL_SQ_CHUNK;
-			e = prp_launch(a, p->lg, lanes, cs);
-		}
-		if (e != cudaSuccess) break;
-		a.op = OP_MUL;
-		a.cmd = c + 2 * S;
-		a.i_hi = 0;
-		a.count = 1;
-		e = prp_launch(a, p->lg, lanes, cs);
-	}
+	const char *what = nullptr;
+	cudaError_t e = upload(p, k, T, cs);
+	if (e == cudaSuccess) e = issue_ticks(p, k, T, lanes, cs, false, &what);
 	cudaGraph_t graph = nullptr;
 	const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
 	if (e != cudaSuccess || e2 != cudaSuccess)
@@ -350,10 +378,10 @@ int read_status(ctw_pool *p, uint32_t &st)
 int finish_slot(ctw_pool *p, int s, bool status_bad)
 {
 	PoolSlot &sl = p->slot[(size_t)s];
-	const size_t D = p->D, S = (size_t)p->slots;
-	const int regs[3] = { 0, 2, 3 };
+	const size_t D = p->D;
+	const int regs[3] = { 5, 4, 2 };     // verify result, d(t+1), result
 	for (int i = 0; i < 3; ++i)
-		POOL_CUDA(cudaMemcpyAsync(p->h_read + i * D, p->d_regs + ((size_t)regs[i] * S + s) * D, D * 4,
+		POOL_CUDA(cudaMemcpyAsync(p->h_read + i * D, reg_plane(p, regs[i]) + (size_t)s * D, D * 4,
 		                          cudaMemcpyDeviceToHost, p->rb_stream));
 	POOL_CUDA(cudaStreamSynchronize(p->rb_stream));
 	ctw_result r{};
@@ -365,20 +393,20 @@ int finish_slot(ctw_pool *p, int s, bool status_bad)
 	r.t_submit = p->t_submit[(size_t)s];
 	r.t_admit = p->t_admit[(size_t)s];
 	r.t_done = mono_seconds();
-	std::vector<uint32_t> cv(D), c2(D), c3(D);
-	int rc = canonical(p->h_read, sl.b, D, cv.data());
-	if (!rc) rc = canonical(p->h_read + D, sl.b, D, c2.data());
-	if (!rc) rc = canonical(p->h_read + 2 * D, sl.b, D, c3.data());
+	std::vector<uint32_t> cy(D), cd(D), cx(D);
+	int rc = canonical(p->h_read, sl.b, D, cy.data());
+	if (!rc) rc = canonical(p->h_read + D, sl.b, D, cd.data());
+	if (!rc) rc = canonical(p->h_read + 2 * D, sl.b, D, cx.data());
 	if (rc || status_bad)
 		r.status = (int8_t)(rc ? rc : CTW_E_COMPUTE);
 	else
 	{
 		bool prp, zero;
 		uint64_t r64;
-		res64_of(c3.data(), sl.b, D, prp, zero, r64);
+		res64_of(cx.data(), sl.b, D, prp, zero, r64);
 		r.is_prp = prp ? 1 : 0;
 		r.res64 = r64;
-		r.gl_ok = (cv == c2) ? 1 : 0;
+		r.gl_ok = (cy == cd) ? 1 : 0;
 		if (zero) r.status = (int8_t)CTW_E_COMPUTE;
 		else if (!r.gl_ok) r.status = (int8_t)CTW_E_GERBICZ;
 	}
@@ -392,30 +420,17 @@ int finish_slot(ctw_pool *p, int s, bool status_bad)
 
 namespace ctw {
 
-int pool_admit_prepared(ctw_pool *p, const PreparedTest &t, uint64_t tag, double t_submit)
+int pool_admit_prepared(ctw_pool *p, PreparedTest &&t, uint64_t tag, double t_submit)
 {
 	int s = -1;
 	for (int i = 0; i < p->slots; ++i)
 		if (p->slot[(size_t)i].state == SLOT_FREE) { s = i; break; }
 	if (s < 0) return CTW_E_FULL;
 	if (t.B != p->B) return fail(CTW_E_ARG, "prepared block %d differs from the pool's %d", t.B, p->B);
-	const size_t D = p->D;
-	uint32_t *st = p->h_stage + (size_t)s * (4 + p->nwords);
-	const uint32_t b = t.b;
-	const int sh = (31 - __builtin_clz(b)) - 1;
-	st[0] = b;
-	st[1] = (uint32_t)(((uint64_t)1 << (sh + 32)) / b);
-	st[2] = (uint32_t)sh;
-	st[3] = (8.0 * (double)D * (double)b * (double)b < 4.611686018427388e18) ? 1u : 0u;
-	uint32_t *w = st + 4;
-	memset(w, 0, (size_t)p->nwords * 4);
-	if ((int)t.E.size() > p->ewE - 1 || (int)t.res.size() > p->ewR) return fail(CTW_E_ARG, "exponent too long for the pool");
-	std::copy(t.E.begin(), t.E.end(), w);
-	std::copy(t.res.begin(), t.res.end(), w + p->ewE);
-	POOL_CUDA(cudaMemcpyAsync(p->d_laneb + 4 * (size_t)s, st, 16, cudaMemcpyHostToDevice, p->stream));
-	POOL_CUDA(cudaMemcpyAsync(p->d_exp + (size_t)s * p->nwords, w, (size_t)p->nwords * 4, cudaMemcpyHostToDevice,
-	                          p->stream));
-	slot_start(p->slot[(size_t)s], t, tag);
+	uint32_t *lb = p->h_laneb + 4 * (size_t)s;
+	lane_params(t.b, p->D, lb);
+	POOL_CUDA(cudaMemcpyAsync(p->d_laneb + 4 * (size_t)s, lb, 16, cudaMemcpyHostToDevice, p->stream));
+	slot_start(p->slot[(size_t)s], std::move(t), tag);
 	p->t_admit[(size_t)s] = mono_seconds();
 	p->t_submit[(size_t)s] = t_submit;
 	++p->active;
@@ -444,7 +459,7 @@ int ctw_pool_create(int log2_degree, int slots, int log2_ctas, int csize, uint32
 	if (!out) return fail(CTW_E_ARG, "null output pointer");
 	*out = nullptr;
 	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
-	if (slots < 1 || slots > 65535) return fail(CTW_E_ARG, "slots %d outside [1, 65535]", slots);
+	if (slots < 1 || slots > MAX_INLINE_LANES) return fail(CTW_E_ARG, "slots %d outside [1, %d]", slots, MAX_INLINE_LANES);
 	if (base != 2 && base != 3) return fail(CTW_E_ARG, "base %u not in {2,3}", base);
 	const int lg = log2_ctas < 0 ? prp_lg_for(log2_degree) : log2_ctas;
 	const int lm = log2_degree - lg;
@@ -463,13 +478,13 @@ int ctw_pool_create(int log2_degree, int slots, int log2_ctas, int csize, uint32
 	p->csize = csize;
 	p->base = base;
 	p->B = gl_block ? gl_block : default_gl_block(log2_degree);
+	p->nws = stage_words(p->B);
 	p->D = (size_t)1 << log2_degree;
 	p->G = (size_t)1 << lg;
 	p->M = p->D / p->G;
 	p->tw_smem = prp_smem_bytes(lm, lg, 1) <= 227 * 1024 ? 1 : 0;
-	slot_words(log2_degree, p->B, p->ewE, p->ewR);
-	p->nwords = p->ewE + p->ewR;
-	p->r0 = 32 * p->ewE;
+	const char *dv = getenv("CTW_POOL_DIRECT");
+	p->direct = dv && dv[0] == '1';
 	p->slot.assign((size_t)slots, PoolSlot{});
 	p->t_admit.assign((size_t)slots, 0.0);
 	p->t_submit.assign((size_t)slots, 0.0);
@@ -494,16 +509,17 @@ int ctw_pool_destroy(ctw_pool *p)
 	cudaFree(p->d_tfs);
 	cudaFree(p->d_tis);
 	cudaFree(p->d_laneb);
-	cudaFree(p->d_exp);
 	cudaFree(p->d_status);
-	cudaFree(p->d_cmd[0]);
-	cudaFree(p->d_cmd[1]);
-	cudaFreeHost(p->h_cmd[0]);
-	cudaFreeHost(p->h_cmd[1]);
-	cudaFreeHost(p->h_stage);
-	cudaFreeHost(p->h_read);
 	for (int k = 0; k < 2; ++k)
+	{
+		cudaFree(p->d_stage[k]);
+		cudaFree(p->d_aux[k]);
+		cudaFreeHost(p->h_stage[k]);
+		cudaFreeHost(p->h_aux[k]);
 		if (p->ev[k]) cudaEventDestroy(p->ev[k]);
+	}
+	cudaFreeHost(p->h_laneb);
+	cudaFreeHost(p->h_read);
 	if (p->stream) cudaStreamDestroy(p->stream);
 	if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
 	if (p->rb_stream) cudaStreamDestroy(p->rb_stream);
@@ -519,8 +535,7 @@ int ctw_pool_admit(ctw_pool *p, uint32_t b, uint64_t tag)
 	PreparedTest t;
 	t.b = b;
 	slot_prepare(t, p->ln, p->B);
-	const double now = mono_seconds();
-	return pool_admit_prepared(p, t, tag, now);
+	return pool_admit_prepared(p, std::move(t), tag, mono_seconds());
 }
 
 int ctw_pool_run(ctw_pool *p, int ticks)
@@ -545,21 +560,37 @@ int ctw_pool_run(ctw_pool *p, int ticks)
 		int lanes = 8;
 		while (lanes < hi) lanes *= 2;
 		lanes = std::min(lanes, p->slots);
-		PrpLaneCmd *hc = p->h_cmd[k];
-		memset(hc, 0, (size_t)T * 3 * S * sizeof(PrpLaneCmd));
+		memset(p->h_aux[k], 0, (size_t)T * 2 * S * sizeof(PrpLaneAux));
+		memset(p->h_stage[k], 0, (size_t)T * S * p->nws * 4);
 		for (int t = 0; t < T; ++t)
 			for (int s = 0; s < hi; ++s)
 			{
 				PoolSlot &sl = p->slot[(size_t)s];
-				if (sl.state == SLOT_FREE || sl.state == SLOT_FINISHED) continue;
-				PrpLaneCmd *c = hc + (size_t)t * 3 * S;
-				const long long before = sl.squarings;
-				if (slot_tick(sl, p->B, p->r0, c[s], c[S + s], c[2 * S + s])) sl.done_seq = p->seq_issued;
-				p->squarings += sl.squarings - before;
+				if (sl.state != SLOT_ACTIVE) continue;
+				const SlotTick tk = slot_tick(sl, p->B);
+				PrpLaneAux *ax = p->h_aux[k] + (size_t)t * 2 * S;
+				ax[s] = PrpLaneAux{ tk.before, 1u };
+				ax[S + s] = PrpLaneAux{ tk.after, 1u };
+				bit_slice(tk.source ? sl.t.res : sl.t.E, tk.lo, p->B,
+				          p->h_stage[k] + ((size_t)t * S + s) * p->nws, p->nws);
+				p->squarings += p->B + 1;
+				if (tk.last) sl.done_seq = p->seq_issued;
 			}
-		cudaGraphExec_t exec = nullptr;
-		if (int rc = get_graph(p, k, T, lanes, exec)) return rc;
-		POOL_CUDA(cudaGraphLaunch(exec, p->stream));
+		if (p->direct)
+		{
+			const char *what = nullptr;
+			cudaError_t e = upload(p, k, T, p->stream);
+			if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+			if (e != cudaSuccess) return fail(CTW_E_CUDA, "pool upload: %s", cudaGetErrorString(e));
+			e = issue_ticks(p, k, T, lanes, p->stream, true, &what);
+			if (e != cudaSuccess) return fail(CTW_E_CUDA, "pool %s launch: %s", what ? what : "?", cudaGetErrorString(e));
+		}
+		else
+		{
+			cudaGraphExec_t exec = nullptr;
+			if (int rc = get_graph(p, k, T, lanes, exec)) return rc;
+			POOL_CUDA(cudaGraphLaunch(exec, p->stream));
+		}
 		POOL_CUDA(cudaEventRecord(p->ev[k], p->stream));
 		p->ev_pending[k] = true;
 		p->ev_seq[k] = p->seq_issued;
@@ -615,43 +646,38 @@ int ctw_pool_info(ctw_pool *p, int *slots, int *active, int *in_flight, int *gl_
 
 int ctw_pool_read_slot(ctw_pool *p, int slot, int reg, int32_t *out)
 {
-	if (!p || !out || slot < 0 || slot >= p->slots || reg < 0 || reg > 3) return fail(CTW_E_ARG, "bad arguments");
+	if (!p || !out || slot < 0 || slot >= p->slots || reg < 0 || reg >= POOL_REGS)
+		return fail(CTW_E_ARG, "bad arguments");
 	POOL_CUDA(cudaStreamSynchronize(p->stream));
-	POOL_CUDA(cudaMemcpy(out, p->d_regs + ((size_t)reg * p->slots + slot) * p->D, p->D * 4, cudaMemcpyDeviceToHost));
+	POOL_CUDA(cudaMemcpy(out, reg_plane(p, reg) + (size_t)slot * p->D, p->D * 4, cudaMemcpyDeviceToHost));
 	return CTW_OK;
 }
 
 void *ctw_pool_stream(ctw_pool *p) { return p ? (void *)p->stream : nullptr; }
 
-int ctw_pool_schedule(int log2_degree, uint32_t b, int gl_block, int32_t *ticks_out, int max_ticks, int *r0)
+int ctw_pool_schedule(int log2_degree, uint32_t b, int gl_block, int32_t *ticks_out, int max_ticks, int *block)
 {
 	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
 	if (b < 64 || b >= 0x80000000u) return fail(CTW_E_ARG, "b = %u outside [64, 2^31)", b);
 	const int B = gl_block ? gl_block : default_gl_block(log2_degree);
-	int ewE, ewR;
-	slot_words(log2_degree, B, ewE, ewR);
-	if (r0) *r0 = 32 * ewE;
+	if (block) *block = B;
 	PreparedTest t;
 	t.b = b;
 	slot_prepare(t, log2_degree, B);
 	PoolSlot s;
-	slot_start(s, t, 0);
+	slot_start(s, std::move(t), 0);
 	int n = 0;
 	for (bool done = false; !done; ++n)
 	{
-		PrpLaneCmd aux, sq, mul;
-		done = slot_tick(s, B, 32 * ewE, aux, sq, mul);
+		const SlotTick k = slot_tick(s, B);
+		done = k.last;
 		if (ticks_out && n < max_ticks)
 		{
-			int32_t *o = ticks_out + 8 * (size_t)n;
-			o[0] = aux.aux;
-			o[1] = sq.count;
-			o[2] = sq.i_hi;
-			o[3] = mul.count;
-			o[4] = mul.r_in;
-			o[5] = mul.r_y;
-			o[6] = mul.r_out;
-			o[7] = 0;
+			int32_t *o = ticks_out + 4 * (size_t)n;
+			o[0] = (int32_t)k.before;
+			o[1] = (int32_t)k.after;
+			o[2] = k.source;
+			o[3] = (int32_t)k.lo;
 		}
 	}
 	return n;

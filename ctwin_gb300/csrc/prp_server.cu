@@ -220,7 +220,7 @@ void worker_loop(ctw_server *s)
 				else
 					blocked_by_budget = true;
 			}
-			if (target && pool_admit_prepared(target, w.t, w.r.tag, w.r.t_submit) >= 0)
+			if (target && pool_admit_prepared(target, std::move(w.t), w.r.tag, w.r.t_submit) >= 0)
 				++admitted;
 			else
 				still.push_back(std::move(w));

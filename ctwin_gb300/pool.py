@@ -30,15 +30,16 @@ def autotune(log2_degree: int, lanes: int):
 
 
 def schedule(log2_degree: int, b: int, gl_block: int = 0):
-    """Tick program of one test (host only): (int32 array [ticks, 8], bit offset of the block sum)."""
+    """Tick program of one test (host only): (int32 array [ticks, 4] of
+    {moves before, moves after, source 0 = E / 1 = block sum, lowest bit}, B)."""
     L = lib()
-    r0 = ctypes.c_int()
-    n = L.ctw_pool_schedule(log2_degree, b, gl_block, None, 0, ctypes.byref(r0))
+    blk = ctypes.c_int()
+    n = L.ctw_pool_schedule(log2_degree, b, gl_block, None, 0, ctypes.byref(blk))
     if n < 0:
         check(n)
-    out = np.zeros((n, 8), dtype=np.int32)
-    check(0 if L.ctw_pool_schedule(log2_degree, b, gl_block, ptr(out), n, ctypes.byref(r0)) == n else -1)
-    return out, r0.value
+    out = np.zeros((n, 4), dtype=np.int32)
+    check(0 if L.ctw_pool_schedule(log2_degree, b, gl_block, ptr(out), n, ctypes.byref(blk)) == n else -1)
+    return out, blk.value
 
 
 def slot_bytes(log2_degree: int) -> int:

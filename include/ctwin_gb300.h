@@ -167,14 +167,14 @@ typedef struct ctw_result {
 
 typedef struct ctw_pool ctw_pool;
 
-/* A pool of `slots` tests of degree 2^log2_degree kept in HBM (registers,
- * exponent bits, the multiply's scratch).  Every tick runs, for each active
- * slot, gl_block squarings of its own exponent from its own bit position and
+/* A pool of `slots` (<= 4096) tests of degree 2^log2_degree kept in HBM
+ * (six registers and the multiply's scratch per slot).  Every tick runs, for
+ * each active slot, gl_block squarings over its own next exponent bits and
  * its Gerbicz-Li multiply, so tests admitted at different times share each
  * launch (continuous batching).  Ticks are queued as CUDA graphs on the pool's
  * stream.  log2_ctas -1 and csize 0 take the default split and CSIZE 8;
- * gl_block 0 takes the reference's rule (cyclo/src/cyclo.h:272) for a
- * 20-bit b.  Results are bit-identical to ctw_prp_run's. */
+ * gl_block 0 takes the reference's rule (cyclo/src/cyclo.h:272) for a 20-bit
+ * b.  Results are bit-identical to ctw_prp_run's. */
 int ctw_pool_create(int log2_degree, int slots, int log2_ctas, int csize, uint32_t base, int gl_block,
                     ctw_pool **out);
 int ctw_pool_destroy(ctw_pool *p);
@@ -195,15 +195,16 @@ int ctw_pool_results(ctw_pool *p, ctw_result *out, int max);
  * block, split and csize in use, and squarings issued so far (any may be NULL). */
 int ctw_pool_info(ctw_pool *p, int *slots, int *active, int *in_flight, int *gl_block, int *log2_ctas, int *csize,
                   long long *squarings);
-/* Copy register reg (0..3) of one slot to the host (after ctw_pool_collect
+/* Copy register reg (0..5) of one slot to the host (after ctw_pool_collect
  * with wait); for tests. */
 int ctw_pool_read_slot(ctw_pool *p, int slot, int reg, int32_t *out);
 void *ctw_pool_stream(ctw_pool *p);
-/* The tick program of one test, without a device: per tick 8 int32 words
- * {aux, sq_count, sq_i_hi, mul_count, mul_in, mul_y, mul_out, 0}; sq_i_hi >=
- * *r0 addresses the Gerbicz-Li block sum at bit *r0.  Returns the tick count
- * (or the count needed when max_ticks is too small). */
-int ctw_pool_schedule(int log2_degree, uint32_t b, int gl_block, int32_t *ticks_out, int max_ticks, int *r0);
+/* The tick program of one test, without a device: per tick 4 int32 words
+ * {register moves before the squarings, moves after the multiply (PrpAuxOp
+ * bits), exponent source (0 = E, 1 = Gerbicz-Li block sum), lowest bit of the
+ * tick's *block bits}.  Returns the tick count (or the count needed when
+ * max_ticks is too small). */
+int ctw_pool_schedule(int log2_degree, uint32_t b, int gl_block, int32_t *ticks_out, int max_ticks, int *block);
 
 /* ------------------------------------------------------------------------ */
 /* Server: a request loop over pools of every degree.  No counterpart in the */

@@ -83,6 +83,10 @@ def pool_jobs():
         for b in (64, 65, 100, 1000):
             jobs.append((b, ln, 2, False))
     jobs.append((77, 12, 3, False))
+    for ln in (12, 13):
+        for b in (65537, 70001, 100003):
+            jobs.append((b, ln, 2, False))
+    jobs.append((65539, 12, 3, False))
     # server mixes: seeded b in [2^16, 2^20) at degrees 2^9..2^11
     rng = random.Random(5)
     for ln in (9, 10, 11):
@@ -99,8 +103,14 @@ def main():
     from oracle import oracle as O
     O.build()
     if args.only == "pool":
+        path = os.path.join(HERE, "pool_gmp.json")
+        have = {}
+        if os.path.exists(path):
+            have = {(d["b"], d["n"], d["base"], d["form"] == "-"): d for d in json.load(open(path))}
+        todo = [j for j in pool_jobs() if j not in have]
         with mp.get_context("spawn").Pool(min(8, os.cpu_count() or 1)) as pool:
-            res = pool.map(prp_case, pool_jobs())
+            new = pool.map(prp_case, todo)
+        res = [have[j] if j in have else new[todo.index(j)] for j in pool_jobs()]
         json.dump(res, open(os.path.join(HERE, "pool_gmp.json"), "w"), indent=0)
         print("done", len(res), "pool cases")
         return

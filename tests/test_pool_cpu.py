@@ -2,61 +2,77 @@
 runs (ctw_pool_schedule) replayed on the oracle's CPU restatement of the
 transform, against GMP.  The program restates cyclo::check
 (cyclo/src/cyclo.h:252-377) with the exponent padded to whole Gerbicz-Li
-blocks; its verdict, RES64 and Gerbicz-Li check must be the reference's."""
+blocks and with the pool's uniform launches (every tick: register moves, B
+squarings of register 0, d <- x * d into register 1, register moves); its
+verdict, RES64 and Gerbicz-Li check must be the reference's."""
 import numpy as np
 import pytest
 
 from oracle import oracle as O
 
+INIT, SAVE_D, SAVE_X, SAVE_D1, SET_Y, LOAD_D, TAKE, SAVE_Y = (1 << k for k in range(8))
+
 
 def _lib_or_skip():
     try:
-        from ctwin_gb300.pool import schedule  # noqa: F401
         from ctwin_gb300._native import lib
         lib()
     except ImportError as e:
         pytest.skip(f"native library not built: {e}")
 
 
+def block_sum(E, B):
+    res = 0
+    while E:
+        res += E & ((1 << B) - 1)
+        E >>= B
+    return res
+
+
+def moves(r, ops):
+    one = np.zeros_like(r[0])
+    one[0] = 1
+    if ops & INIT:
+        r[0], r[1] = one.copy(), one.copy()
+    if ops & SAVE_D:
+        r[3] = r[1].copy()
+    if ops & SAVE_X:
+        r[2] = r[0].copy()
+    if ops & SAVE_D1:
+        r[4] = r[1].copy()
+    if ops & SET_Y:
+        r[0] = one.copy()
+    if ops & LOAD_D:
+        r[1] = r[3].copy()
+    if ops & TAKE:
+        r[0] = r[1].copy()
+    if ops & SAVE_Y:
+        r[5] = r[0].copy()
+
+
 def replay(ln, b, base=2, gl_block=0, csize=16, corrupt_tick=None):
     """Run the tick program of one test on the oracle: (is_prp, res64, gl_ok)."""
     from ctwin_gb300.pool import schedule
-    prog, r0 = schedule(ln, b, gl_block)
+    prog, B = schedule(ln, b, gl_block)
     D = 1 << ln
     E = O.exponent(b, ln)
-    B = int(prog[0, 1])
-    res = 0
-    e = E
-    while e:
-        res += e & ((1 << B) - 1)
-        e >>= B
-    words = np.zeros(r0 // 32 + (res.bit_length() + 31) // 32 + 2, dtype=np.uint32)
-    ew = O.int_to_words(E)
-    words[:ew.size] = ew
-    rw = O.int_to_words(res)
-    words[r0 // 32:r0 // 32 + rw.size] = rw
-    one = np.zeros(D, dtype=np.int32)
-    one[0] = 1
-    regs = [np.zeros(D, dtype=np.int32) for _ in range(4)]
+    src = [E, block_sum(E, B)]
+    regs = [np.zeros(D, dtype=np.int32) for _ in range(6)]
     with O.Tables(ln) as T:
-        for t, (aux, sq_n, sq_hi, mul_n, m_in, m_y, m_out, _) in enumerate(prog):
-            if aux & 1:
-                regs[3] = regs[0].copy()
-            if aux & 2:
-                regs[0] = one.copy()
-            if aux & 4:
-                regs[1] = one.copy()
-            if sq_n > 0:
-                T.square_loop(regs[0], b, base, csize, words, int(sq_hi), int(sq_n))
+        for t, (before, after, source, lo) in enumerate(prog):
+            moves(regs, int(before))
+            bits = (src[source] >> int(lo)) & ((1 << B) - 1)
+            words = O.int_to_words(bits) if bits else np.zeros(1, dtype=np.uint32)
+            T.square_loop(regs[0], b, base, csize, words, B - 1, B)
             if t == corrupt_tick:
                 regs[0][5] += 1          # a planted arithmetic error on the CPU
-            if mul_n > 0:
-                x = regs[m_in].copy()
-                T.mul(x, regs[m_y], b, csize)
-                regs[m_out] = x
-    c3 = O.get_int(regs[3], b)
-    prp, r64, _ = O.is_prime(c3, b)
-    gl_ok = bool(np.array_equal(O.get_int(regs[0], b), O.get_int(regs[2], b)))
+            x = regs[0].copy()
+            T.mul(x, regs[1], b, csize)
+            regs[1] = x
+            moves(regs, int(after))
+    c = O.get_int(regs[2], b)
+    prp, r64, _ = O.is_prime(c, b)
+    gl_ok = bool(np.array_equal(O.get_int(regs[5], b), O.get_int(regs[4], b)))
     return prp, r64, gl_ok
 
 
@@ -70,7 +86,7 @@ def test_schedule_matches_gmp(ln, b, base):
 
 
 def test_schedule_finds_a_prp():
-    """A known PRP from the n = 8 golden list (GMP-pinned)."""
+    """A PRP of degree 2^8 (GMP-pinned) comes out as residue 1."""
     _lib_or_skip()
     for b in range(100000, 100400):
         if O.fermat(b, 8, 2)[2]:
@@ -96,18 +112,19 @@ def test_schedule_detects_error():
 
 
 def test_schedule_structure():
-    """Blocks are whole: the first squaring sits at a multiple of B minus one,
-    every main tick but the last multiplies into d, the last into d(t+1)."""
+    """Blocks are whole and aligned from the top of the padded exponent; the
+    register moves sit where the Gerbicz-Li program needs them."""
     _lib_or_skip()
     from ctwin_gb300.pool import schedule
     for ln, b in [(8, 100002), (12, 1 << 20), (16, 1330358)]:
-        prog, r0 = schedule(ln, b)
-        B = int(prog[0, 1])
-        L = O.exponent(b, ln).bit_length()
-        main = prog[:-2]
-        assert (int(main[0, 2]) + 1) % B == 0 and int(main[0, 2]) + 1 >= L > int(main[0, 2]) + 1 - B
-        assert main[0, 0] == 6 and all(main[1:, 0] == 0)
-        assert all(main[:-1, 6] == 1) and main[-1, 6] == 2
-        assert list(np.diff(main[:, 2])) == [-B] * (len(main) - 1) and main[-1, 2] == B - 1
-        assert prog[-2, 0] == 3 and prog[-2, 6] == 0 and prog[-1, 3] == 0
-        assert prog[-1, 2] == r0 + B - 1 and prog[-1, 1] == B
+        prog, B = schedule(ln, b)
+        E = O.exponent(b, ln)
+        nb = (E.bit_length() + B - 1) // B
+        main, ver = prog[:nb], prog[nb:]
+        assert list(main[:, 3]) == [(nb - 1 - t) * B for t in range(nb)] and all(main[:, 2] == 0)
+        assert main[0, 0] & INIT and main[-1, 0] & SAVE_D and not any(main[1:-1, 0])
+        assert all(ver[:, 2] == 1) and ver[-1, 3] == 0 and ver[-1, 1] == SAVE_Y
+        assert ver[0, 0] & (SAVE_X | SAVE_D1 | SET_Y) == SAVE_X | SAVE_D1 | SET_Y
+        assert ver[-2, 0] & LOAD_D and ver[-2, 1] == TAKE
+        kh = len(ver) - 1
+        assert block_sum(E, B) < 1 << ((kh + 1) * B)

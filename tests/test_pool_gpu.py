@@ -36,11 +36,10 @@ def server_cases(ln):
     return sorted(b for (b, n, base) in gold() if n == ln and base == 2 and b >= 1 << 16)
 
 
-@pytest.mark.parametrize("ln,lg", [(12, 0), (12, 1), (12, 2), (12, 3), (13, 0), (13, 1), (13, 2), (13, 3), (13, 4),
-                                   (14, 0), (14, 1), (14, 2), (14, 4), (15, 3)])
+@pytest.mark.parametrize("ln,lg", [(12, 0), (12, 1), (12, 2), (12, 3), (13, 0), (13, 1), (13, 2), (13, 3), (13, 4)])
 def test_pool_splits_match_gmp(native, ln, lg):
     from ctwin_gb300 import Pool
-    bs = [64, 65, 100, 1000]
+    bs = [65537, 70001, 100003]
     csize = 8 if lg % 2 == 0 else 16
     with Pool(ln, 4, log2_ctas=lg, csize=csize) as p:
         for i, b in enumerate(bs):
@@ -50,10 +49,28 @@ def test_pool_splits_match_gmp(native, ln, lg):
     check_results(res, ln)
 
 
+@pytest.mark.parametrize("ln,lg", [(14, 0), (14, 1), (14, 3), (14, 4), (15, 2), (15, 4)])
+def test_pool_splits_match_engine(native, ln, lg):
+    """Degrees 2^14 and 2^15 on every kind of split against the engine's own
+    test of the same b (default split; the engine is GMP-pinned elsewhere)."""
+    from ctwin_gb300 import Pool, PrpEngine
+    bs = [65537, 65539]
+    with PrpEngine(ln, len(bs)) as eng:
+        prp, r64, gl = eng.run(bs)
+    want = {b: (bool(p), int(r)) for b, p, r in zip(bs, prp, r64)}
+    with Pool(ln, 2, log2_ctas=lg, csize=32 if lg % 2 else 8) as p:
+        for b in bs:
+            p.admit(b)
+        res = p.run_to_completion()
+    for r in res:
+        assert r["status"] == 0 and r["gl_ok"], r
+        assert (r["is_prp"], r["res64"]) == want[r["b"]], r
+
+
 def test_pool_base3(native):
     from ctwin_gb300 import Pool
     with Pool(12, 2, base=3) as p:
-        p.admit(77, 1)
+        p.admit(65539, 1)
         res = p.run_to_completion()
     check_results(res, 12, base=3)
 
@@ -98,8 +115,8 @@ def test_autotune(native):
     assert 0 <= lg <= 3 and cs in (8, 16, 32, 64) and us > 0
     assert autotune(12, 64) == (lg, cs, us)           # cached
     with Pool(12, 2, log2_ctas=lg, csize=cs) as p:
-        p.admit(100)
-        p.admit(1000)
+        p.admit(65537)
+        p.admit(100003)
         check_results(p.run_to_completion(), 12)
 
 
