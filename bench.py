@@ -71,6 +71,21 @@ def workload(rank: int):
     return b, E, i0, B_GL, words
 
 
+TRAFFIC_PER_LAUNCH = 2.18e6     # bytes of DRAM traffic of one 651-squaring launch, from ncu
+
+
+def hbm_line(traffic: float, seconds: float) -> dict:
+    """Achieved DRAM GB/s beside the measured copy bandwidth (MEASURED_PEAKS.json)."""
+    peak = None
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+    except (OSError, ValueError):
+        pass
+    ach = traffic / seconds / 1e9
+    return {"achieved_gbs": ach, "peak_gbs": peak, "frac": ach / peak if peak else None,
+            "peak_source": "MEASURED_PEAKS.json" if peak else None}
+
+
 def imad_per_squaring(D: int) -> float:
     return 4.0 * (3 * D * math.log2(D) + 9 * D)
 
@@ -603,11 +618,15 @@ def main():
         "tests_per_s_projected": value / (i0 + 1),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": peak_imad / 1e12, "unit": "T IMAD/s",
-                     "frac": achieved / peak_imad if peak_imad else None, "traffic": None,
+                     "frac": achieved / peak_imad if peak_imad else None,
+                     "traffic": TRAFFIC_PER_LAUNCH,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 651-squaring launch "
+                                       "(profiles/prp_kernel_d65536_full.md)",
                      "peak_source": "32-bit IMAD probe kernel run on this GPU in this process",
                      "sms_used": geo["ctas_per_lane"],
                      "frac_of_used_sms": (achieved / peak_imad) * 152 / geo["ctas_per_lane"] if peak_imad else None,
-                     "kernel_ms": t_launch * 1000.0},
+                     "kernel_ms": t_launch * 1000.0,
+                     "hbm": hbm_line(TRAFFIC_PER_LAUNCH, t_launch)},
         "cpu_baseline": cpu,
         "gpu_launches": int(launches),
         "clocks": clocks,

@@ -74,6 +74,7 @@ def lib() -> ctypes.CDLL:
                                        ctypes.c_char_p], i32),
             "ctw_sieve_launches": ([], i64),
             "ctw_prp_create_split": ([i32, i32, i32, ctypes.POINTER(H)], i32),
+            "ctw_prp_create_minus": ([i32, i32, ctypes.POINTER(H)], i32),
             "ctw_prp_autotune": ([i32, i32, vp, vp, vp], i32),
             "ctw_pool_create": ([i32, i32, i32, i32, u32, i32, ctypes.POINTER(H)], i32),
             "ctw_pool_destroy": ([H], i32),

@@ -1,5 +1,6 @@
 // Host side of the PRP engine: root tables, launches, canonical digits,
 // RES64 and the Gerbicz-Li driver, behind the C ABI of include/ctwin_gb300.h.
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -86,6 +87,54 @@ int canonical(const int32_t *x, uint32_t b, size_t D, uint32_t *out)
 	return CTW_OK;
 }
 
+// Canonical digits of x mod N- = b^Dn - b^{Dn/2} - 1 (the twin partner,
+// sieve/CPU/ctsieve.cpp:434-439): carry base b, fold the top carry T as +T at
+// 0 and +T at Dn/2 (b^Dn = b^{Dn/2} + 1 mod N-) until it vanishes, then
+// subtract N- once if the value is >= N-.
+int canonical_minus(const int32_t *x, uint32_t b, size_t Dn, uint32_t *out)
+{
+	const int64_t B = b;
+	auto divmod = [B](int64_t &v) -> uint32_t {
+		int64_t q = v / B, r = v % B;
+		if (r < 0) { r += B; --q; }
+		v = q;
+		return (uint32_t)r;
+	};
+	int64_t c = 0;
+	for (size_t j = 0; j < Dn; ++j)
+	{
+		int64_t v = c + x[j];
+		out[j] = divmod(v);
+		c = v;
+	}
+	for (int guard = 0; c != 0; ++guard)
+	{
+		if (guard > 64) return fail(CTW_E_COMPUTE, "getInt: carry does not settle");
+		int64_t v = c;
+		for (size_t j = 0; j < Dn / 2; ++j) { v += out[j]; out[j] = divmod(v); }
+		v += c;
+		for (size_t j = Dn / 2; j < Dn; ++j) { v += out[j]; out[j] = divmod(v); }
+		c = v;
+	}
+	// N- digits: b-1 below Dn/2, b-2 at Dn/2, b-1 above
+	auto ndig = [&](size_t j) -> uint32_t { return j == Dn / 2 ? b - 2 : b - 1; };
+	bool ge = true;
+	for (size_t j = Dn; j-- > 0;)
+		if (out[j] != ndig(j)) { ge = out[j] > ndig(j); break; }
+	if (ge)
+	{
+		int64_t borrow = 0;
+		for (size_t j = 0; j < Dn; ++j)
+		{
+			int64_t v = (int64_t)out[j] - ndig(j) - borrow;
+			borrow = v < 0;
+			if (v < 0) v += B;
+			out[j] = (uint32_t)v;
+		}
+	}
+	return CTW_OK;
+}
+
 void res64_of(const uint32_t *c, uint32_t b, size_t D, bool &prp, bool &zero, uint64_t &r64)
 {
 	prp = (c[0] == 1);
@@ -113,6 +162,8 @@ struct ctw_prp {
 	size_t smem = 0;
 	int tw_smem = 0;
 	int narrow = 0;                   // 64-bit carry arithmetic is exact for the current b
+	int minus = 0;                    // N- = b^Dn - b^{Dn/2} - 1 on the transform of degree D = 2 Dn
+	size_t Dn = 0;                    // degree of the tested numbers (D, or D/2 for N-)
 	cudaStream_t stream = nullptr;
 	int32_t *d_regs = nullptr;        // [3][lanes][D]
 	uint32_t *d_scratch = nullptr;    // [lanes][G][3][M]
@@ -174,6 +225,7 @@ PrpKernelArgs make_args(ctw_prp *h)
 	a.mult = (int)h->base;
 	a.tw_smem = h->tw_smem;
 	a.narrow = h->narrow;
+	a.minus = h->minus;
 	a.scratch = h->d_scratch;
 	return a;
 }
@@ -224,9 +276,14 @@ int canonical_reg(ctw_prp *h, int reg, std::vector<uint32_t> &c)
 	int rc = check_status(h);
 	if (rc) return rc;
 	if ((rc = read_reg_host(h, reg, v))) return rc;
-	c.resize(v.size());
+	c.resize((size_t)h->lanes * h->Dn);
 	for (int l = 0; l < h->lanes; ++l)
-		if ((rc = canonical(v.data() + (size_t)l * h->D, h->b[(size_t)l], h->D, c.data() + (size_t)l * h->D))) return rc;
+	{
+		const int32_t *x = v.data() + (size_t)l * h->D;
+		uint32_t *o = c.data() + (size_t)l * h->Dn;
+		rc = h->minus ? canonical_minus(x, h->b[(size_t)l], h->Dn, o) : canonical(x, h->b[(size_t)l], h->D, o);
+		if (rc) return rc;
+	}
 	return CTW_OK;
 }
 
@@ -289,6 +346,24 @@ int ctw_prp_create(int log2_degree, int lanes, ctw_prp **out)
 	return ctw_prp_create_split(log2_degree, lanes, -1, out);
 }
 
+int ctw_prp_create_minus(int log2_degree, int lanes, ctw_prp **out)
+{
+	if (!out) return fail(CTW_E_ARG, "null output pointer");
+	*out = nullptr;
+	if (log2_degree < 8 || log2_degree > 16) return fail(CTW_E_ARG, "N- log2_degree %d outside [8, 16]", log2_degree);
+	// the product of two degree < Dn polynomials is exact on the transform of
+	// degree 2 Dn; one CTA up to 2^12 coefficients, else a column-layout
+	// cluster of >= 4 CTAs (the fold stays inside each CTA's columns)
+	const int ln2 = log2_degree + 1;
+	const int lg = ln2 <= 12 ? 0 : std::max(2, prp_lg_for(ln2));
+	ctw_prp *h = nullptr;
+	if (int rc = ctw_prp_create_split(ln2, lanes, lg, &h)) return rc;
+	h->minus = 1;
+	h->Dn = h->D / 2;
+	*out = h;
+	return CTW_OK;
+}
+
 int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **out)
 {
 	if (!out) return fail(CTW_E_ARG, "null output pointer");
@@ -305,6 +380,7 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	h->lg = lg;
 	h->lm = log2_degree - h->lg;
 	h->D = (size_t)1 << log2_degree;
+	h->Dn = h->D;
 	h->G = (size_t)1 << h->lg;
 	h->M = h->D / h->G;
 	h->tw_smem = prp_smem_bytes(h->lm, h->lg, 1) <= 227 * 1024 ? 1 : 0;
@@ -357,6 +433,7 @@ int ctw_prp_set_csize(ctw_prp *h, int csize)
 	if ((size_t)csize * 2 > h->M) return fail(CTW_E_ARG, "csize too large for this degree");
 	if (h->lg > 0 && h->lm <= 13 && (size_t)csize > (h->M >> h->lg))
 		return fail(CTW_E_ARG, "csize %d longer than a column run of this split", csize);
+	if (h->minus && h->lg == 0 && (size_t)csize * 4 > h->M) return fail(CTW_E_ARG, "csize too large for this degree");
 	h->csize = csize;
 	return CTW_OK;
 }
@@ -496,7 +573,7 @@ int ctw_prp_is_prime(ctw_prp *h, int reg, uint8_t *is_prp, uint64_t *res64)
 	{
 		bool prp, zero;
 		uint64_t r;
-		res64_of(c.data() + (size_t)l * h->D, h->b[(size_t)l], h->D, prp, zero, r);
+		res64_of(c.data() + (size_t)l * h->Dn, h->b[(size_t)l], h->Dn, prp, zero, r);
 		if (is_prp) is_prp[l] = prp ? 1 : 0;
 		if (res64) res64[l] = r;
 		any_zero |= zero;
@@ -538,7 +615,13 @@ int ctw_prp_run(ctw_prp *h, const uint32_t *bv, int count, uint8_t *is_prp, uint
 	for (int l = 0; l < V; ++l)
 	{
 		if (l > 0 && b[(size_t)l] == b[(size_t)l - 1]) E[(size_t)l] = E[(size_t)l - 1];
-		else E[(size_t)l] = prp_exponent(b[(size_t)l], h->ln);
+		else
+		{
+			// N+ - 1 = b^D - b^{D/2}; N- - 1 = b^Dn - b^{Dn/2} - 2
+			const int lnn = h->minus ? h->ln - 1 : h->ln;
+			E[(size_t)l] = prp_exponent(b[(size_t)l], lnn);
+			if (h->minus) big_sub_inplace(E[(size_t)l], big_from_u64(2));
+		}
 		i0 = std::max(i0, (long long)big_bitlen(E[(size_t)l]) - 1);
 	}
 	const int L = 2 << ((31 - __builtin_clz((uint32_t)i0)) / 2);
@@ -605,11 +688,11 @@ int ctw_prp_run(ctw_prp *h, const uint32_t *bv, int count, uint8_t *is_prp, uint
 	{
 		bool prp, zero;
 		uint64_t r;
-		const size_t off = (size_t)l * h->D;
-		res64_of(c0.data() + off, b[(size_t)l], h->D, prp, zero, r);
+		const size_t off = (size_t)l * h->Dn;
+		res64_of(c0.data() + off, b[(size_t)l], h->Dn, prp, zero, r);
 		if (is_prp) is_prp[l] = prp ? 1 : 0;
 		if (res64) res64[l] = r;
-		if (gl_ok) gl_ok[l] = (memcmp(c1.data() + off, c2.data() + off, h->D * sizeof(uint32_t)) == 0) ? 1 : 0;
+		if (gl_ok) gl_ok[l] = (memcmp(c1.data() + off, c2.data() + off, h->Dn * sizeof(uint32_t)) == 0) ? 1 : 0;
 		any_zero |= zero;
 	}
 	// reset like the reference between vectors (cyclo/src/cyclo.h:475-477)

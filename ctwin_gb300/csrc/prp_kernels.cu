@@ -509,6 +509,12 @@ __device__ __forceinline__ int64_t load64(const uint32_t *X, int M, int p)
 {
 	return (int64_t)((uint64_t)X[p] | ((uint64_t)X[M + p] << 32));
 }
+__device__ __forceinline__ void store96(uint32_t *X, int M, int p, i128 v)
+{
+	X[p] = (uint32_t)v;
+	X[M + p] = (uint32_t)(v >> 32);
+	X[2 * M + p] = (uint32_t)(v >> 64);
+}
 
 // ---------------------------------------------------------------------------
 // Cross-CTA levels 0..LG-1 through a shared-memory stage.
@@ -759,23 +765,44 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 			}
 			__syncthreads();
 		}
+		// N- = b^Dn - b^{Dn/2} - 1 (one CTA, M = 2 Dn): the transform gave the
+		// exact product c_0..c_{2Dn-2}; fold it with X^Dn = X^{Dn/2} + 1:
+		// j < Dn/2: c_j + c_{j+Dn} + c_{j+3Dn/2}; j >= Dn/2: c_j + c_{j+Dn/2} + 2 c_{j+Dn}
+		int ncu = ncl;                                   // chunks carried
+		if constexpr (LG == 0)
+		{
+			if (a.minus)
+			{
+				const int Dh = M / 2, Dq = M / 4;
+				for (int j = tid; j < Dh; j += nt)
+				{
+					i128 v = load96(X, M, swz(j, sb)) + load96(X, M, swz(j + Dh, sb));
+					if (j < Dq) v += load96(X, M, swz(j + Dh + Dq, sb));
+					else v += load96(X, M, swz(j + Dq, sb)) + load96(X, M, swz(j + Dh, sb));
+					store96(X, M, swz(j, sb), v);
+				}
+				ncu = ncl / 2;
+				__syncthreads();
+			}
+		}
 		// normalize1: one thread per chunk
-		for (int c = tid; c < ncl; c += nt)
+		for (int c = tid; c < ncu; c += nt)
 		{
 			const int64_t f = narrow ? carry_chunk<int64_t>(X, M, c, a.csize, sb, mult, b, b_inv, b_s, err)
 			                         : carry_chunk<i128>(X, M, c, a.csize, sb, mult, b, b_inv, b_s, err);
 			fch[c] = f;
-			if (c == ncl - 1) xch[0] = f;
+			if (c == ncu - 1) xch[0] = f;
 		}
 		csync<LG>();
 		// normalize2: carry into chunk c from chunk c-1, wrap -f -> 0, +f -> D/2
-		for (int c = tid; c < ncl; c += nt)
+		// (N-: +f -> 0 and +f -> Dn/2)
+		for (int c = tid; c < ncu; c += nt)
 		{
 			i128 acc;
 			if (c > 0)
 			{
 				acc = fch[c - 1];
-				if (LG == 0 && c == ncl / 2) acc += fch[ncl - 1];
+				if (LG == 0 && c == ncu / 2) acc += fch[ncu - 1];
 			}
 			else if constexpr (LG > 0)
 			{
@@ -787,7 +814,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 			}
 			else
 			{
-				acc = -(i128)fch[ncl - 1];
+				acc = a.minus ? (i128)fch[ncu - 1] : -(i128)fch[ncu - 1];
 			}
 			int i = 0;
 			bool done = false;
@@ -806,6 +833,8 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 				X[p] = (uint32_t)(int32_t)s;
 			}
 		}
+		if (ncu < ncl)
+			for (int t = ncu * a.csize + tid; t < M; t += nt) X[swz(t, sb)] = 0;   // N-: upper half stays 0
 		__syncthreads();
 	};
 
@@ -1017,8 +1046,27 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 			XC[2 * M + p] = w2;
 		}
 		__syncthreads();
+		// N- (G >= 4, rows of M coefficients, Dn = G/2 rows): fold rows G/2..G-1
+		// into rows 0..G/2-1 of each column (all in this CTA):
+		// h < G/4: v_h + v_{h+G/2} + v_{h+3G/4}; h >= G/4: v_h + v_{h+G/4} + 2 v_{h+G/2}
+		int ncu = ncl;
+		if (a.minus)
+		{
+			const int H2 = G / 2, H4 = G / 4;
+			for (int it = tid; it < H2 * MG; it += nt)
+			{
+				const int h = it / MG, tt = it - h * MG;
+				const int p = swz(cb + tt, sb) - cb;
+				i128 v = load96(XC + h * MG, M, p) + load96(XC + (h + H2) * MG, M, p);
+				if (h < H4) v += load96(XC + (h + H2 + H4) * MG, M, p);
+				else v += load96(XC + (h + H4) * MG, M, p) + load96(XC + (h + H2) * MG, M, p);
+				store96(XC + h * MG, M, p, v);
+			}
+			ncu = H2 * runc;
+			__syncthreads();
+		}
 		// normalize1 over the runs; the last chunk of run h publishes its carry
-		for (int c = tid; c < ncl; c += nt)
+		for (int c = tid; c < ncu; c += nt)
 		{
 			const int h = c / runc, j = c - h * runc;
 			int64_t acc_f;
@@ -1055,7 +1103,9 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 		cl.sync();
 		// normalize2: chunk j of run (h, g) takes the carry of the chunk before it
 		// in natural order; -f of the last chunk goes to coefficient 0, +f to D/2
-		for (int c = tid; c < ncl; c += nt)
+		// (N-: the last of the Dn = G/2 rows; +f to 0 and +f to Dn/2)
+		const int hl = a.minus ? G / 2 - 1 : G - 1, hw = a.minus ? G / 4 : G / 2;
+		for (int c = tid; c < ncu; c += nt)
 		{
 			const int h = c / runc, j = c - h * runc;
 			i128 acc;
@@ -1063,12 +1113,12 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 			else if (g > 0) acc = *cl.map_shared_rank(xch + h, g - 1);
 			else
 			{
-				const int64_t last = *cl.map_shared_rank(xch + (G - 1), G - 1);
-				if (h == 0) acc = -(i128)last;
+				const int64_t last = *cl.map_shared_rank(xch + hl, G - 1);
+				if (h == 0) acc = a.minus ? (i128)last : -(i128)last;
 				else
 				{
 					acc = *cl.map_shared_rank(xch + (h - 1), G - 1);
-					if (h == G / 2) acc += last;
+					if (h == hw) acc += last;
 				}
 			}
 			uint32_t *Xh = XC + h * MG;
@@ -1090,6 +1140,8 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 				Xh[p] = (uint32_t)(int32_t)s;
 			}
 		}
+		if (ncu < ncl)
+			for (int e = (G / 2) * MG + tid; e < M; e += nt) XC[e] = 0;   // N-: rows G/2..G-1 stay 0
 		__syncthreads();
 	};
 

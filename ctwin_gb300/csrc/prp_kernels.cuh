@@ -51,6 +51,7 @@ struct PrpKernelArgs {
 	int swz_b;                  // swizzle selector of the shared planes (prp_swizzle_bit)
 	int scols;                  // columns per staging round of the cross-CTA levels
 	int narrow;                 // 1: |coefficients| * 3 + carries < 2^62, carry in 64-bit arithmetic
+	int minus;                  // 1: arithmetic mod N- = b^Dn - b^{Dn/2} - 1 on the transform of degree 2 Dn
 	uint32_t omega[3];          // 6th root w1 (Montgomery form)
 	uint32_t k1[3];             // S / (2 w1 - 1)
 	uint32_t sc[3];             // S = 2^32 * 2 / D   (Montgomery form)

@@ -18,12 +18,19 @@ from ._native import check, lib, ptr
 class PrpEngine:
     """Fermat-test engine for `lanes` candidates of degree D = 2^log2_degree."""
 
-    def __init__(self, log2_degree: int, lanes: int = 1, csize: int = 8, base: int = 2):
+    def __init__(self, log2_degree: int, lanes: int = 1, csize: int = 8, base: int = 2, minus: bool = False):
+        """minus=True tests the twin partner N- = b^D - b^{D/2} - 1 (no reference
+        counterpart; its registers hold 2D words, its digits D)."""
         h = ctypes.c_void_p()
-        check(lib().ctw_prp_create(log2_degree, lanes, ctypes.byref(h)))
+        if minus:
+            check(lib().ctw_prp_create_minus(log2_degree, lanes, ctypes.byref(h)))
+        else:
+            check(lib().ctw_prp_create(log2_degree, lanes, ctypes.byref(h)))
         self._h = h
         self.ln = log2_degree
         self.D = 1 << log2_degree
+        self.minus = minus
+        self.regD = self.D * (2 if minus else 1)
         self.lanes = lanes
         self.set_csize(csize)
         self.set_base(base)
@@ -109,13 +116,13 @@ class PrpEngine:
         return prp.astype(bool), r64
 
     def read_regs(self, first: int = 0, nregs: int = 1) -> np.ndarray:
-        out = np.zeros((nregs, self.lanes, self.D), dtype=np.int32)
+        out = np.zeros((nregs, self.lanes, self.regD), dtype=np.int32)
         check(lib().ctw_prp_read_regs(self._h, first, nregs, ptr(out)))
         return out
 
     def write_regs(self, regs: np.ndarray, first: int = 0):
         arr = np.ascontiguousarray(regs, dtype=np.int32)
-        nregs = arr.size // (self.lanes * self.D)
+        nregs = arr.size // (self.lanes * self.regD)
         check(lib().ctw_prp_write_regs(self._h, first, nregs, ptr(arr)))
 
     def run(self, b):
@@ -146,12 +153,12 @@ class PrpEngine:
         return int(lib().ctw_prp_launches(self._h))
 
 
-def prp_test(b_values, n: int, base: int = 2, lanes: int | None = None, csize: int = 8):
-    """Fermat-test b^(2^n) - b^(2^(n-1)) + 1 for every b: list of (b, is_prp, res64, gl_ok)."""
+def prp_test(b_values, n: int, base: int = 2, lanes: int | None = None, csize: int = 8, minus: bool = False):
+    """Fermat-test b^(2^n) - b^(2^(n-1)) + 1 (minus: ... - 1) for every b: list of (b, is_prp, res64, gl_ok)."""
     b_values = [int(x) for x in b_values]
     lanes = lanes or min(64, max(1, len(b_values)))
     out = []
-    with PrpEngine(n, lanes, csize=csize, base=base) as eng:
+    with PrpEngine(n, lanes, csize=csize, base=base, minus=minus) as eng:
         for i in range(0, len(b_values), lanes):
             chunk = b_values[i:i + lanes]
             prp, r64, gl = eng.run(chunk)

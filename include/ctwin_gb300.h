@@ -44,6 +44,15 @@ typedef struct ctw_prp ctw_prp;
  * Replaces: engine ctor + allocMemory + createKernels (cyclo/src/engine.h:40-65,132)
  *           and transform ctor / initEngine roots (cyclo/src/transform.h:300-433). */
 int ctw_prp_create(int log2_degree, int lanes, ctw_prp **out);
+/* An engine for the twin partner N- = b^D - b^{D/2} - 1 (D = 2^log2_degree,
+ * 8..16), which the sieve's "-" form pairs with N+ (sieve/CPU/ctsieve.cpp:
+ * 434-439); the reference has no PRP test for it.  The product of two residues
+ * of degree < D is taken exactly on the transform of degree 2D and folded
+ * with b^D = b^{D/2} + 1.  Every call of the PRP engine applies:
+ * ctw_prp_run tests N- (exponent N- - 1 = b^D - b^{D/2} - 2), get_digits and
+ * is_prime give the canonical residue mod N- (D digits per lane), while
+ * read_regs / write_regs move the 2D-word registers of the transform. */
+int ctw_prp_create_minus(int log2_degree, int lanes, ctw_prp **out);
 /* The same with an explicit cluster split: 2^log2_ctas CTAs per candidate
  * (-1: the default split).  Registers and results do not depend on the split;
  * it is an autotuning choice (ctw_prp_autotune).  CTW_E_ARG when the degree
