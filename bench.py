@@ -21,6 +21,8 @@ Two more workloads print their own line (not the default):
          CSIZE); one step = one tick of every pool (B squarings + the Gerbicz-Li multiply
          of every candidate), the pools' graphs running side by side on their streams;
          compared per degree with the plain one-candidate-per-launch-sequence path
+  --workload sieve  sieved b/s of the GPU sieve on n = 20, b < 2^30, p < 2^40 (and the
+         n = 11 both-form sieve of b in [10^5, 3 10^5) to 2^32 beside it)
   --workload serve  a seeded Poisson stream of full PRP tests, degree 2^k with k
          log-uniform in [12, 15) (k = 12, 13, 14), b uniform in [2^16, 2^24), through the
          server (continuous batching by degree, admission by pool bytes); tests/s and
@@ -274,8 +276,7 @@ def run_batch(args):
     t_tune = time.perf_counter() - t0
     t0 = time.perf_counter()
     for k, bl in groups.items():
-        for j, b in enumerate(bl):
-            assert pools[k].admit(b, tag=j) == j
+        assert pools[k].admit_many(bl) == len(bl)
     t_admit = time.perf_counter() - t0
     info = {k: p.info() for k, p in pools.items()}
     sq_per_step = {k: info[k]["slots"] * (info[k]["gl_block"] + 1) for k in pools}
@@ -456,6 +457,103 @@ def run_serve(args):
     return 0
 
 
+def _is_prime64(p: int) -> bool:
+    if p < 2:
+        return False
+    for q in (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37):
+        if p % q == 0:
+            return p == q
+    d, r = p - 1, 0
+    while d % 2 == 0:
+        d //= 2
+        r += 1
+    for a in (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37):
+        x = pow(a, d, p)
+        if x in (1, p - 1):
+            continue
+        for _ in range(r - 1):
+            x = x * x % p
+            if x == p - 1:
+                break
+        else:
+            return False
+    return True
+
+
+def run_sieve(args):
+    """Sieved b/s: config 4 (n = 20, b < 2^30, p = 3k 2^20 + 1 < 2^40) on the GPU,
+    config 1 (n = 11, b in [10^5, 3 10^5), both forms to 2^32) beside it, the
+    oracle's C restatement of the CPU sieve timed on a bounded sample."""
+    import torch  # noqa: F401  (CUDA context)
+    from ctwin_gb300 import sieve_pass
+    from ctwin_gb300._native import lib
+    from ctwin_gb300.sieve import unpack
+    L = lib()
+    n, b_min, b_max = 20, 2, (1 << 30) - 1
+    p_min, p_max = 3 * (1 << n) + 1, 1 << 40
+    for _ in range(args.warmup):
+        sieve_pass(n, b_min, b_max, p_min, p_max, 1)
+    times, launches0 = [], L.ctw_sieve_launches()
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            struck, p_last = sieve_pass(n, b_min, b_max, p_min, p_max, 1)
+            times.append(time.perf_counter() - t0)
+    launches = L.ctw_sieve_launches() - launches0
+    t = statistics.median(times)
+    size = b_max - b_min + 1
+    survivors = int((unpack(struck, size) == 0).sum())
+    # algorithmic work: 2^(n-1) root products per prime (0.5 mulmod per root) + an
+    # Euler/PRP test of log2 p squarings per candidate k
+    step = 3 << n
+    ks = list(range(1, (p_max - 1) // step + 1))
+    primes = sum(1 for k in ks if _is_prime64(k * step + 1))
+    work = primes * (1 << (n - 1)) + len(ks) * 40
+    peak = L.ctw_mulmod64_peak()
+    # config 1, both forms
+    c1 = {}
+    for name, mode, pmn in (("pos", 1, 3 * 2048 + 1), ("neg", -1, 11)):
+        sieve_pass(11, 100000, 299999, pmn, 1 << 32, mode)
+        t0 = time.perf_counter()
+        sieve_pass(11, 100000, 299999, pmn, 1 << 32, mode)
+        c1[name] = time.perf_counter() - t0
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        cores = os.cpu_count() or 1
+        p_s = 1 << 38                       # bounded sample: primes below 2^38 of config 4
+        t0 = time.perf_counter()
+        O.sieve(n, b_min, b_max, p_min, p_s, 1, threads=cores)
+        dt = time.perf_counter() - t0
+        frac = (p_s - p_min) / (p_max - p_min)
+        t0 = time.perf_counter()
+        O.sieve(11, 100000, 299999, 3 * 2048 + 1, 1 << 32, 1, threads=cores)
+        dt1 = time.perf_counter() - t0
+        cpu = {"value": size * frac / dt, "unit": "sieved b/s", "cores": cores, "kind": "port",
+               "sample": f"config 4 primes below 2^38 ({frac:.4f} of the p range) in {dt:.1f} s; "
+                         f"config 1 '+' form in {dt1:.2f} s",
+               "config1_pos_s": dt1}
+    line = {
+        "metric": "sieved b/s", "value": size / t, "unit": "sieved b/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic (the full b and p ranges)",
+        "config": {"workload": "n = 20 (N = b^(2^20) - b^(2^19) + 1), b in [2, 2^30), p = 3k 2^20 + 1 < 2^40, + form",
+                   "survivors": survivors, "p_last": p_last, "primes": primes, "candidates_k": len(ks),
+                   "config1_s": c1, "config1_sieved_b_per_s": {k: 200000 / v for k, v in c1.items()}},
+        "e2e": {"value": size / t, "unit": "sieved b/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(struck.nbytes)},
+        "roofline": {"bound": "mulmod64", "achieved": work / t / 1e12, "peak": peak / 1e12,
+                     "unit": "T mulmod64/s", "frac": work / t / peak if peak else None,
+                     "work_per_step": work, "traffic": None,
+                     "peak_source": "64-bit Montgomery probe kernel run on this GPU in this process",
+                     "hbm": hbm_line(struck.nbytes, t)},
+        "cpu_baseline": cpu, "gpu_launches": launches // max(1, args.steps), "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
@@ -467,7 +565,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve"])
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve", "sieve"])
     ap.add_argument("--candidates", type=int, default=4096, help="batch: candidates")
     ap.add_argument("--requests", type=int, default=0, help="serve: requests (0: rate x --serve-seconds)")
     ap.add_argument("--serve-seconds", type=float, default=60.0)
@@ -497,6 +595,8 @@ def main():
         return run_batch(args) if rank == 0 else 0
     if args.workload == "serve":
         return run_serve(args) if rank == 0 else 0
+    if args.workload == "sieve":
+        return run_sieve(args) if rank == 0 else 0
     import ctwin_gb300
     from ctwin_gb300 import PrpEngine
     from ctwin_gb300._native import lib

@@ -73,6 +73,7 @@ def lib() -> ctypes.CDLL:
             "ctw_sieve_write_files": ([i32, ctypes.c_uint64, ctypes.c_uint64, vp, ctypes.c_uint64, ctypes.c_uint64,
                                        ctypes.c_char_p], i32),
             "ctw_sieve_launches": ([], i64),
+            "ctw_mulmod64_peak": ([], ctypes.c_double),
             "ctw_prp_create_split": ([i32, i32, i32, ctypes.POINTER(H)], i32),
             "ctw_prp_create_minus": ([i32, i32, ctypes.POINTER(H)], i32),
             "ctw_prp_autotune": ([i32, i32, vp, vp, vp], i32),
@@ -80,6 +81,7 @@ def lib() -> ctypes.CDLL:
             "ctw_pool_destroy": ([H], i32),
             "ctw_pool_slot_bytes": ([i32], ctypes.c_size_t),
             "ctw_pool_admit": ([H, u32, ctypes.c_uint64], i32),
+            "ctw_pool_admit_many": ([H, vp, vp, i32, i32], i32),
             "ctw_pool_run": ([H, i32], i32),
             "ctw_pool_collect": ([H, i32], i32),
             "ctw_pool_results": ([H, vp, i32], i32),

@@ -25,6 +25,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -536,6 +537,33 @@ int ctw_pool_admit(ctw_pool *p, uint32_t b, uint64_t tag)
 	t.b = b;
 	slot_prepare(t, p->ln, p->B);
 	return pool_admit_prepared(p, std::move(t), tag, mono_seconds());
+}
+
+int ctw_pool_admit_many(ctw_pool *p, const uint32_t *b, const uint64_t *tags, int count, int threads)
+{
+	if (!p || (!b && count > 0) || count < 0) return fail(CTW_E_ARG, "bad arguments");
+	for (int i = 0; i < count; ++i)
+		if (b[i] < 64 || b[i] >= 0x80000000u) return fail(CTW_E_ARG, "b = %u outside [64, 2^31)", b[i]);
+	const int n = std::min(count, pool_free_slots(p));
+	std::vector<PreparedTest> prep((size_t)n);
+	const int nt = std::max(1, std::min(threads > 0 ? threads : (int)std::thread::hardware_concurrency(), n));
+	std::vector<std::thread> th;
+	for (int t = 0; t < nt; ++t)
+		th.emplace_back([&, t] {
+			for (int i = t; i < n; i += nt)
+			{
+				prep[(size_t)i].b = b[i];
+				slot_prepare(prep[(size_t)i], p->ln, p->B);
+			}
+		});
+	for (auto &x : th) x.join();
+	const double now = mono_seconds();
+	for (int i = 0; i < n; ++i)
+	{
+		const int s = pool_admit_prepared(p, std::move(prep[(size_t)i]), tags ? tags[i] : (uint64_t)i, now);
+		if (s < 0) return s;
+	}
+	return n;
 }
 
 int ctw_pool_run(ctw_pool *p, int ticks)

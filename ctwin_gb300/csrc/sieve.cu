@@ -563,6 +563,57 @@ extern "C" int ctw_sieve_run(int n, uint64_t b_min, uint64_t b_max, uint64_t p_m
 
 extern "C" long long ctw_sieve_launches(void) { return g_sieve_launches; }
 
+// Roofline probe of the sieve: independent chains of 64-bit Montgomery
+// products (mp_mul, the sieve's inner operation) over all SMs.
+__global__ void mulmod64_probe_kernel(uint64_t *out, int iters)
+{
+	Mp m;
+	m.p = 0xFFFFFFFFFFC00001ull - 2 * (uint64_t)blockIdx.x;   // odd moduli near 2^64
+	uint64_t q = m.p;                                          // p^-1 mod 2^64 (Newton)
+	for (int k = 0; k < 6; ++k) q *= 2 - m.p * q;
+	m.q = q;
+	m.one = 0;
+	uint64_t v[4];
+#pragma unroll
+	for (int j = 0; j < 4; ++j) v[j] = (threadIdx.x * 0x9E3779B97F4A7C15ull + j) % m.p;
+	for (int i = 0; i < iters; ++i)
+	{
+#pragma unroll
+		for (int j = 0; j < 4; ++j) v[j] = mp_mul(m, v[j], v[j]);
+	}
+	uint64_t x = v[0] ^ v[1] ^ v[2] ^ v[3];
+	if (x == 0x123456789ull) out[0] = x;
+}
+
+extern "C" double ctw_mulmod64_peak(void)
+{
+	int dev = 0, sms = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) return 0.0;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	uint64_t *out = nullptr;
+	if (cudaMalloc(&out, 64) != cudaSuccess) return 0.0;
+	const int grid = sms * 8, block = 256, iters = 4096;
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	mulmod64_probe_kernel<<<grid, block>>>(out, 64);
+	float best = 1e30f;
+	for (int rep = 0; rep < 3; ++rep)
+	{
+		cudaEventRecord(e0);
+		mulmod64_probe_kernel<<<grid, block>>>(out, iters);
+		cudaEventRecord(e1);
+		cudaEventSynchronize(e1);
+		float ms = 0;
+		cudaEventElapsedTime(&ms, e0, e1);
+		if (ms < best) best = ms;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(out);
+	return double(grid) * block * 4 * iters / (best * 1e-3);
+}
+
 // sv_<n>_<bmin>_<bmax>.dat and cand_<n>_<bmin>_<bmax>.txt in the reference's
 // format (sieve/CPU/ctsieve.cpp:591-626): u64 p_min_pos, u64 p_min_neg,
 // u64 count, u32 index[count], u32 crc32 (Rosetta CRC-32, ~crc ^ 0xa23777ac);

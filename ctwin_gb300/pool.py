@@ -84,6 +84,16 @@ class Pool:
             check(rc)
         return rc
 
+    def admit_many(self, bs, tags=None, threads: int = 0) -> int:
+        """Admit as many of bs as there are free slots (exponents prepared on
+        `threads` host threads); returns the number admitted."""
+        b = np.ascontiguousarray(bs, dtype=np.uint32)
+        t = None if tags is None else np.ascontiguousarray(tags, dtype=np.uint64)
+        n = lib().ctw_pool_admit_many(self._h, ptr(b), ptr(t) if t is not None else None, b.size, threads)
+        if n < 0:
+            check(n)
+        return n
+
     def run(self, ticks: int = 1):
         check(lib().ctw_pool_run(self._h, ticks))
 

@@ -192,6 +192,10 @@ size_t ctw_pool_slot_bytes(int log2_degree);
 /* Admit a test of b (64 <= b < 2^31) into the lowest free slot; returns the
  * slot (>= 0) or CTW_E_FULL.  The test starts with the next queued tick. */
 int ctw_pool_admit(ctw_pool *p, uint32_t b, uint64_t tag);
+/* Admit up to `count` tests at once (as many as there are free slots),
+ * preparing their exponents on `threads` host threads (0: all cores); tags
+ * may be NULL (tag = index).  Returns the number admitted. */
+int ctw_pool_admit_many(ctw_pool *p, const uint32_t *b, const uint64_t *tags, int count, int threads);
 /* Queue `ticks` ticks (asynchronous; blocks only while two graph launches of
  * this pool are already in flight). */
 int ctw_pool_run(ctw_pool *p, int ticks);
@@ -271,6 +275,9 @@ int ctw_sieve_write_files(int n, uint64_t b_min, uint64_t b_max, const uint32_t 
                           uint64_t p_min_pos, uint64_t p_min_neg, const char *dir);
 /* Sieve kernel launches issued by this process. */
 long long ctw_sieve_launches(void);
+/* Measured 64-bit Montgomery multiply throughput of the device (mulmods/s),
+ * from an in-library probe kernel; the sieve's roofline denominator. */
+double ctw_mulmod64_peak(void);
 
 #ifdef __cplusplus
 }

@@ -171,3 +171,16 @@ def test_server_budget_admission(native):
         s.submit(12, 100003, tag=7)                 # no pool of degree 2^12 fits in 64 KiB
         r = s.drain(1, timeout_s=60)[0]
         assert r["status"] == -3 and r["tag"] == 7
+
+
+def test_pool_admit_many(native):
+    """Parallel admission (exponents prepared on several host threads)."""
+    from ctwin_gb300 import Pool
+    bs = server_cases(11)[:10]
+    with Pool(11, 8) as p:
+        assert p.admit_many(bs, tags=list(range(len(bs))), threads=4) == 8   # as many as there are slots
+        res = p.run_to_completion()
+        assert p.admit_many(bs[8:]) == 2
+        res += p.run_to_completion()
+    assert sorted(r["b"] for r in res) == sorted(bs)
+    check_results(res, 11)
