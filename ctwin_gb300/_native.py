@@ -76,6 +76,14 @@ def lib() -> ctypes.CDLL:
             "ctw_mulmod64_peak": ([], ctypes.c_double),
             "ctw_prp_create_split": ([i32, i32, i32, ctypes.POINTER(H)], i32),
             "ctw_prp_create_minus": ([i32, i32, ctypes.POINTER(H)], i32),
+            "ctw_prp_shape": ([H, vp, vp, vp], i32),
+            "ctw_prp_run_ex": ([H, vp, i32, i64, vp, vp, vp, vp, vp], i32),
+            "ctw_prp_save_context": ([H, ctypes.c_char_p, i32, i32, ctypes.c_double], i32),
+            "ctw_prp_read_context": ([H, ctypes.c_char_p, vp, vp, vp], i32),
+            "ctw_context_bytes": ([i32, i32, i32], ctypes.c_size_t),
+            "ctw_context_encode": ([i32, i32, i32, vp, i32, i32, ctypes.c_double, vp], i32),
+            "ctw_context_decode": ([i32, i32, i32, vp, ctypes.c_size_t, vp, vp, vp, vp], i32),
+            "ctw_cyclo_check_file": ([i32, ctypes.c_char_p, ctypes.c_char_p, i32, ctypes.c_double, vp, i32], i32),
             "ctw_prp_autotune": ([i32, i32, vp, vp, vp], i32),
             "ctw_pool_create": ([i32, i32, i32, i32, u32, i32, ctypes.POINTER(H)], i32),
             "ctw_pool_destroy": ([H], i32),

@@ -601,6 +601,12 @@ int ctw_prp_write_regs(ctw_prp *h, int first, int nregs, const int32_t *in)
 
 int ctw_prp_run(ctw_prp *h, const uint32_t *bv, int count, uint8_t *is_prp, uint64_t *res64, uint8_t *gl_ok)
 {
+	return ctw_prp_run_ex(h, bv, count, -1, nullptr, nullptr, is_prp, res64, gl_ok);
+}
+
+int ctw_prp_run_ex(ctw_prp *h, const uint32_t *bv, int count, long long i_start, ctw_checkpoint_fn checkpoint,
+                   void *user, uint8_t *is_prp, uint64_t *res64, uint8_t *gl_ok)
+{
 	if (int rc = check_handle(h)) return rc;
 	if (!bv || count < 1 || count > h->lanes) return fail(CTW_E_ARG, "count must be in [1, lanes]");
 	const int V = h->lanes;
@@ -642,12 +648,23 @@ int ctw_prp_run(ctw_prp *h, const uint32_t *bv, int count, uint8_t *is_prp, uint
 
 	int nw = 0;
 	if ((rc = upload(E, nw))) return rc;
-	if ((rc = op_set(h, 0, 1)) || (rc = op_set(h, 1, 1))) return rc;
+	if (i_start > i0) return fail(CTW_E_ARG, "resume bit %lld above the exponent's top bit %lld", i_start, i0);
+	if (i_start < 0)
+	{
+		if ((rc = op_set(h, 0, 1)) || (rc = op_set(h, 1, 1))) return rc;
+	}
 
-	// bits i0..0; after bit i with i % B_GL == 0 and i / B_GL != 0: d <- d * x
-	long long i = i0;
+	// bits i0..0; after bit i with i % B_GL == 0 and i / B_GL != 0: d <- d * x.
+	// The checkpoint callback runs where the reference may save its context:
+	// before the squaring of a bit i with i % B_GL == 0 (cyclo/src/cyclo.h:281-294).
+	long long i = i_start < 0 ? i0 : i_start;
 	while (i >= 0)
 	{
+		if (checkpoint && i % B_GL == 0)
+		{
+			CTW_CUDA(cudaStreamSynchronize(h->stream));
+			if (checkpoint(user, i)) return CTW_STOPPED;
+		}
 		const long long stop = (i / B_GL) * B_GL;    // next checkpoint at or below i
 		const int cnt = (int)(i - stop + 1);
 		if ((rc = op_square_bits(h, h->d_bits, nw, i, cnt))) return rc;
@@ -722,6 +739,15 @@ int ctw_prp_geometry(ctw_prp *h, int *ctas, int *threads, int *smem)
 }
 
 long long ctw_prp_launches(ctw_prp *h) { return h ? h->launches : 0; }
+
+int ctw_prp_shape(ctw_prp *h, int *log2_degree, int *lanes, int *minus)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (log2_degree) *log2_degree = h->minus ? h->ln - 1 : h->ln;
+	if (lanes) *lanes = h->lanes;
+	if (minus) *minus = h->minus;
+	return CTW_OK;
+}
 
 double ctw_imad_peak(void)
 {

@@ -25,6 +25,7 @@ extern "C" {
 #define CTW_E_NOMEM (-3)      /* device or host allocation failed */
 #define CTW_E_COMPUTE (-4)    /* arithmetic self-check failed (range, getInt, zero residue) */
 #define CTW_E_GERBICZ (-5)    /* Gerbicz-Li check failed */
+#define CTW_STOPPED 1         /* a run stopped at a checkpoint on request (not an error) */
 
 const char *ctw_last_error(void);
 /* Library version string. */
@@ -114,6 +115,48 @@ int ctw_prp_write_regs(ctw_prp *h, int first, int nregs, const int32_t *in);
  * Lanes past count repeat the last b (cyclo/src/cyclo.h:233-236).
  * Outputs per candidate: is_prp, res64, gl_ok (1 = Gerbicz-Li passed). */
 int ctw_prp_run(ctw_prp *h, const uint32_t *b, int count, uint8_t *is_prp, uint64_t *res64, uint8_t *gl_ok);
+/* ctw_prp_run with resume and checkpoints, as cyclo::check(b, ctx, k, ri)
+ * (cyclo/src/cyclo.h:252-377).  i_start < 0 starts afresh (registers 0 and 1
+ * set to 1); i_start >= 0 resumes before the squaring of bit i_start with
+ * registers 0 (x) and 1 (d) as they are (restored with
+ * ctw_prp_read_context).  checkpoint(user, i), if not NULL, is called on the
+ * host before the squaring of every bit i with i % B_GL == 0 (where the
+ * reference may save its context), the device idle; a nonzero return stops
+ * the run with CTW_STOPPED and the registers at that point. */
+typedef int (*ctw_checkpoint_fn)(void *user, long long i);
+int ctw_prp_run_ex(ctw_prp *h, const uint32_t *b, int count, long long i_start, ctw_checkpoint_fn checkpoint,
+                   void *user, uint8_t *is_prp, uint64_t *res64, uint8_t *gl_ok);
+/* Save registers 0 and 1 with (k, i, elapsed) as the reference's context file
+ * (cyclo/src/cyclo.h:146-177, cyclo/src/transform.h:458-468, file.h CRC32):
+ * version 1, k, i (int32), elapsed (double), for registers 0..1 the residues of
+ * every digit mod the reference's primes 4293918721, 4253024257 (pairs) and
+ * 4231004161, indexed (register * D + j) * lanes + lane, then the CRC32
+ * trailer; written to path.new, the previous file kept as path.old.  Files are
+ * interchangeable with the reference's when lanes = 64. */
+int ctw_prp_save_context(ctw_prp *h, const char *path, int k, int i, double elapsed);
+/* Read such a file (path, else path.old) into registers 0 and 1: 0 = read,
+ * 1 = no file, CTW_E_ARG = invalid (bad size, CRC or residues). */
+int ctw_prp_read_context(ctw_prp *h, const char *path, int *k, int *i, double *elapsed);
+/* Encode / decode the context bytes of digits [nregs][D][lanes]-ordered as
+ * the reference lays them out, without a device (bytes: 20 + 12 * nregs * D *
+ * lanes + 4).  decode returns CTW_E_ARG on a bad CRC or inconsistent residues. */
+size_t ctw_context_bytes(int log2_degree, int lanes, int nregs);
+int ctw_context_encode(int log2_degree, int lanes, int nregs, const int32_t *digits, int k, int i, double elapsed,
+                       uint8_t *out);
+int ctw_context_decode(int log2_degree, int lanes, int nregs, const uint8_t *in, size_t size, int32_t *digits,
+                       int *k, int *i, double *elapsed);
+/* The cyclog file loop (cyclo/src/cyclo.h:416-480): b values of `filename`
+ * (one per line) in vectors of 64 (the last padded with its last b), the CSIZE
+ * of filename.ini (tuned and written when absent), cyclo.ctx in workdir
+ * (resumed when present, saved every save_every_s seconds at checkpoints and
+ * when stopping), result lines appended to workdir/result_c.txt in the
+ * reference's words ("... is a probable prime." / "... is composite. RES64:
+ * %016X"), PRP b appended to workdir/prp_<n>.txt.  minus != 0 tests the twin
+ * partners N- instead (lines "... - 1 is ...", PRPs to prpm_<n>.txt, context
+ * cyclom.ctx).  The run stops (context saved, CTW_STOPPED) when *quit becomes
+ * nonzero or after stop_after checkpoints (0 = never).  0 = all done. */
+int ctw_cyclo_check_file(int n, const char *filename, const char *workdir, int minus, double save_every_s,
+                         volatile int *quit, int stop_after);
 
 /* Block until all work queued on the handle's stream is done. */
 int ctw_prp_sync(ctw_prp *h);
@@ -124,6 +167,8 @@ void *ctw_prp_stream(ctw_prp *h);
 int ctw_prp_geometry(ctw_prp *h, int *ctas_per_lane, int *threads, int *smem_bytes);
 /* Kernel launches issued by this handle since creation. */
 long long ctw_prp_launches(ctw_prp *h);
+/* Degree of the tested numbers (log2), lanes, and 1 for an N- engine. */
+int ctw_prp_shape(ctw_prp *h, int *log2_degree, int *lanes, int *minus);
 
 /* z = x * y for `lanes` candidates of degree D = 2^log2_degree (8..14), with
  * x, y, z caller-owned DEVICE buffers of lanes * D int32 digits (the register
