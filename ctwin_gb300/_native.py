@@ -74,6 +74,9 @@ def lib() -> ctypes.CDLL:
                                        ctypes.c_char_p], i32),
             "ctw_sieve_launches": ([], i64),
             "ctw_mulmod64_peak": ([], ctypes.c_double),
+            "ctw_sieve_factors": ([i32, ctypes.c_uint64, ctypes.c_uint64, i32, ctypes.c_uint64, vp, ctypes.c_uint64,
+                                   vp], i32),
+            "ctw_gfsieve_check": ([i32, ctypes.c_uint64, ctypes.c_uint64, i32, ctypes.c_char_p, vp, i32, vp], i32),
             "ctw_prp_create_split": ([i32, i32, i32, ctypes.POINTER(H)], i32),
             "ctw_prp_create_minus": ([i32, i32, ctypes.POINTER(H)], i32),
             "ctw_prp_shape": ([H, vp, vp, vp], i32),

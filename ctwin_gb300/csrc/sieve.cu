@@ -217,10 +217,31 @@ struct StrikeTarget {
 	uint32_t *gbits;        // HBM bitmap (1 = struck), bit i <-> b_min + i
 	uint64_t b_min, b_max;
 	int smem_words;         // > 0: strike into a shared copy of this many words
+	// factor mode (gbits == null): append (p, b) pairs, as the reference's GPU
+	// sieve does (push_factor, sieve/GPU/ocl/kernel.cl:233-240)
+	unsigned long long *pairs;
+	uint32_t *pair_count;
+	uint32_t pair_cap;
+	uint32_t *status;       // bit 4 set when the pair buffer overflows
 };
 
 __device__ __forceinline__ void strike_root(const StrikeTarget &T, uint32_t *sbits, uint64_t r, uint64_t p)
 {
+	if (T.pairs)
+	{
+		// factor mode: the root itself, as push_factor(b) / push_factor(p - b)
+		if (r >= T.b_min && r <= T.b_max)
+		{
+			const uint32_t idx = atomicAdd(T.pair_count, 1u);
+			if (idx < T.pair_cap)
+			{
+				T.pairs[2 * (size_t)idx] = p;
+				T.pairs[2 * (size_t)idx + 1] = r;
+			}
+			else atomicOr(T.status, 16u);
+		}
+		return;
+	}
 	// smallest s >= b_min with s = r (mod p)
 	uint64_t s = r;
 	if (s < T.b_min)
@@ -520,7 +541,7 @@ extern "C" int ctw_sieve_run(int n, uint64_t b_min, uint64_t b_max, uint64_t p_m
 	int sms = 0;
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
 	const bool use_smem = words <= (uint64_t)SMEM_BITMAP_MAX_WORDS;
-	StrikeTarget T{ d.bits, b_min, b_max, use_smem ? (int)words : 0 };
+	StrikeTarget T{ d.bits, b_min, b_max, use_smem ? (int)words : 0, nullptr, nullptr, 0, nullptr };
 	const size_t smem = use_smem ? words * 4 : 0;
 	if (use_smem)
 	{
@@ -558,6 +579,78 @@ extern "C" int ctw_sieve_run(int n, uint64_t b_min, uint64_t b_max, uint64_t p_m
 	unsigned long long pl = 0;
 	SV_CUDA(cudaMemcpy(&pl, d.p_last, 8, cudaMemcpyDeviceToHost));
 	*p_last = pl;
+	return CTW_OK;
+}
+
+extern "C" int ctw_sieve_factors(int n, uint64_t k_begin, uint64_t k_end, int mode, uint64_t b_max,
+                                 uint64_t *pairs, uint64_t cap, uint64_t *count)
+{
+	if (n < 8 || n > 24) return fail(CTW_E_ARG, "n = %d outside [8, 24]", n);
+	if (mode != 1 && mode != -1) return fail(CTW_E_ARG, "mode must be +1 or -1");
+	if (!count || (!pairs && cap > 0) || k_end < k_begin || k_begin < 1) return fail(CTW_E_ARG, "bad arguments");
+	if (b_max < 2) return fail(CTW_E_ARG, "b_max must be >= 2");
+	const uint64_t pk = (mode > 0) ? 3 * (k_end << n) + 1 : 10 * k_end + 1;
+	if (pk >= (1ull << 62) || (mode > 0 && (k_end >> (62 - n)) != 0)) return fail(CTW_E_ARG, "p must stay below 2^62");
+	if (ctw_device_count() == 0) return fail(CTW_E_CUDA, "no CUDA device");
+	*count = 0;
+	constexpr uint32_t PAIR_CAP = 1u << 24;              // the reference's factor buffer
+	SieveDev d;
+	unsigned long long *dpairs = nullptr;
+	SV_CUDA(cudaMalloc(&d.primes, (size_t)PRIME_CAP * 16));
+	SV_CUDA(cudaMalloc(&d.gen, (size_t)PRIME_CAP * 8));
+	SV_CUDA(cudaMalloc(&d.count, 8));
+	SV_CUDA(cudaMalloc(&d.p_last, 8));
+	SV_CUDA(cudaMalloc(&d.status, 4));
+	SV_CUDA(cudaMalloc(&dpairs, (size_t)PAIR_CAP * 16));
+	struct PairsFree { unsigned long long *p; ~PairsFree() { cudaFree(p); } } pf{ dpairs };
+	SV_CUDA(cudaMemset(d.p_last, 0, 8));
+	SV_CUDA(cudaMemset(d.status, 0, 4));
+	uint32_t *pair_count = d.count + 1;
+	StrikeTarget T{ nullptr, 2, b_max, 0, dpairs, pair_count, PAIR_CAP, d.status };
+	int sms = 0;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+	std::vector<unsigned long long> host;
+	for (uint64_t k0 = k_begin; k0 < k_end; k0 += K_BLOCK)
+	{
+		const uint64_t nk = std::min<uint64_t>(K_BLOCK, k_end - k0);
+		SV_CUDA(cudaMemset(d.count, 0, 8));
+		if (mode > 0)
+		{
+			pos_candidates<<<sms * 8, 256>>>(n, k0, nk, (PosPrime *)d.primes, d.count, d.p_last, PRIME_CAP);
+			pos_generators<<<sms * 4, 128>>>(n, (PosPrime *)d.primes, d.count, PRIME_CAP, d.gen, d.status);
+			pos_roots<<<sms * 8, 256, 0>>>(n, 6, (PosPrime *)d.primes, d.count, PRIME_CAP, d.gen, T);
+			g_sieve_launches += 3;
+		}
+		else
+		{
+			neg_candidates<<<sms * 8, 256>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
+			neg_roots<<<sms * 8, 128, 0>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
+			g_sieve_launches += 2;
+		}
+		SV_CUDA(cudaGetLastError());
+		uint32_t np = 0, st = 0;
+		SV_CUDA(cudaMemcpy(&np, pair_count, 4, cudaMemcpyDeviceToHost));
+		SV_CUDA(cudaMemcpy(&st, d.status, 4, cudaMemcpyDeviceToHost));
+		if (st & 16) return fail(CTW_E_NOMEM, "more than %u factors in one block of 2^22 k", PAIR_CAP);
+		if (st) return fail(CTW_E_COMPUTE, "sieve root computation failed for a prime (status 0x%x)", st);
+		const size_t old = host.size();
+		host.resize(old + 2 * (size_t)np);
+		if (np) SV_CUDA(cudaMemcpy(host.data() + old, dpairs, (size_t)np * 16, cudaMemcpyDeviceToHost));
+	}
+	// deterministic order: by p, then b (the reference's order is that of its atomics)
+	const size_t m = host.size() / 2;
+	std::vector<size_t> ord(m);
+	for (size_t i = 0; i < m; ++i) ord[i] = i;
+	std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+		return host[2 * a] != host[2 * b] ? host[2 * a] < host[2 * b] : host[2 * a + 1] < host[2 * b + 1];
+	});
+	*count = m;
+	if (m > cap) return fail(CTW_E_NOMEM, "%zu factors, room for %llu", m, (unsigned long long)cap);
+	for (size_t i = 0; i < m; ++i)
+	{
+		pairs[2 * i] = host[2 * ord[i]];
+		pairs[2 * i + 1] = host[2 * ord[i] + 1];
+	}
 	return CTW_OK;
 }
 

@@ -318,6 +318,23 @@ int ctw_sieve_run(int n, uint64_t b_min, uint64_t b_max, uint64_t p_min, uint64_
  * byte-identical to Sieve::write(true) (sieve/CPU/ctsieve.cpp:591-626). */
 int ctw_sieve_write_files(int n, uint64_t b_min, uint64_t b_max, const uint32_t *struck_words,
                           uint64_t p_min_pos, uint64_t p_min_neg, const char *dir);
+/* Factor pairs of the reference's GPU sieve (sieve/GPU/ocl/kernel.cl:233-479):
+ * for every prime p = 3k*2^n + 1 (mode +1) or 10k +- 1 (mode -1) with k in
+ * [k_begin, k_end), every root b of b^(2^n) - b^(2^(n-1)) +- 1 mod p with
+ * 2 <= b <= b_max, as (p, b) in pairs[2i], pairs[2i+1], sorted by p then b.
+ * *count = the number found; CTW_E_NOMEM when it exceeds cap. */
+int ctw_sieve_factors(int n, uint64_t k_begin, uint64_t k_end, int mode, uint64_t b_max, uint64_t *pairs,
+                      uint64_t cap, uint64_t *count);
+/* The ctsieveg run (sieve/GPU/src/ctsieve.h:326-421, main.cpp): blocks of
+ * 2^21 k from floor(p_min f) to ceil(p_max f), factors with p in [p_min,
+ * p_max] and b <= bMax (5e9, or 1e10 for p >= 1e16 (+) / 1e13 (-)) checked on
+ * the host and appended as "p b" lines to workdir/fp<n>_<p_min/1e12>_<p_max/1e12>.txt
+ * (fn... for mode -1, lines of one block sorted); after each block
+ * workdir/ctx<...> (ctx_n<...>) holds the blocks done and the elapsed time,
+ * and a new run resumes from it.  Stops with CTW_STOPPED when *quit becomes
+ * nonzero or after stop_after_blocks blocks (0 = never). */
+int ctw_gfsieve_check(int n, uint64_t p_min, uint64_t p_max, int mode, const char *workdir, volatile int *quit,
+                      int stop_after_blocks, uint64_t *factors_written);
 /* Sieve kernel launches issued by this process. */
 long long ctw_sieve_launches(void);
 /* Measured 64-bit Montgomery multiply throughput of the device (mulmods/s),
