@@ -655,16 +655,19 @@ int ctw_prp_run_ex(ctw_prp *h, const uint32_t *bv, int count, long long i_start,
 	}
 
 	// bits i0..0; after bit i with i % B_GL == 0 and i / B_GL != 0: d <- d * x.
-	// The checkpoint callback runs where the reference may save its context:
-	// before the squaring of a bit i with i % B_GL == 0 (cyclo/src/cyclo.h:281-294).
+	// The checkpoint callback runs right after each Gerbicz-Li multiply, with
+	// i the next bit to square; the reference saves its context one squaring
+	// earlier (cyclo/src/cyclo.h:281-294) and resumes from any i just as well.
 	long long i = i_start < 0 ? i0 : i_start;
+	bool first = true;
 	while (i >= 0)
 	{
-		if (checkpoint && i % B_GL == 0)
+		if (checkpoint && !first)
 		{
 			CTW_CUDA(cudaStreamSynchronize(h->stream));
 			if (checkpoint(user, i)) return CTW_STOPPED;
 		}
+		first = false;
 		const long long stop = (i / B_GL) * B_GL;    // next checkpoint at or below i
 		const int cnt = (int)(i - stop + 1);
 		if ((rc = op_square_bits(h, h->d_bits, nw, i, cnt))) return rc;

@@ -120,9 +120,10 @@ int ctw_prp_run(ctw_prp *h, const uint32_t *b, int count, uint8_t *is_prp, uint6
  * set to 1); i_start >= 0 resumes before the squaring of bit i_start with
  * registers 0 (x) and 1 (d) as they are (restored with
  * ctw_prp_read_context).  checkpoint(user, i), if not NULL, is called on the
- * host before the squaring of every bit i with i % B_GL == 0 (where the
- * reference may save its context), the device idle; a nonzero return stops
- * the run with CTW_STOPPED and the registers at that point. */
+ * host after every Gerbicz-Li multiply, i being the next bit to square and
+ * the device idle (the reference saves one squaring earlier; either point
+ * resumes correctly); a nonzero return stops the run with CTW_STOPPED and the
+ * registers at that point. */
 typedef int (*ctw_checkpoint_fn)(void *user, long long i);
 int ctw_prp_run_ex(ctw_prp *h, const uint32_t *b, int count, long long i_start, ctw_checkpoint_fn checkpoint,
                    void *user, uint8_t *is_prp, uint64_t *res64, uint8_t *gl_ok);
