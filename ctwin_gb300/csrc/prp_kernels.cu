@@ -679,12 +679,12 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 {
 	constexpr int G = 1 << LG;
 	extern __shared__ __align__(16) uint32_t sm[];
-	const int lm = a.lm, M = 1 << lm, D = M * G;
+	const int lm = M12 ? 12 : a.lm, M = 1 << lm, D = M * G;   // compile-time sizes on the 4096 path
 	const int tid = threadIdx.x, nt = blockDim.x;
 	int g = 0;
 	if constexpr (LG > 0) g = (int)cg::this_cluster().block_rank();
 	const int lane = blockIdx.x / G;
-	const int ncl = M / a.csize, sb = a.swz_b;
+	const int ncl = M / a.csize, sb = M12 ? 3 : a.swz_b;
 
 	uint32_t *X = sm;                                           // [3][M] swizzled planes
 	uint32_t *ST = sm + 3 * M;                                  // stage / chunk carries
@@ -888,12 +888,12 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 {
 	constexpr int G = 1 << LG;
 	extern __shared__ __align__(16) uint32_t sm[];
-	const int lm = a.lm, M = 1 << lm, D = M * G, MG = M >> LG;
+	const int lm = M12 ? 12 : a.lm, M = 1 << lm, D = M * G, MG = M >> LG;   // compile-time on the 4096 path
 	const int tid = threadIdx.x, nt = blockDim.x;
 	cg::cluster_group cl = cg::this_cluster();
 	const int g = (int)cl.block_rank();
 	const int lane = blockIdx.x / G;
-	const int csz = a.csize, sb = a.swz_b;
+	const int csz = a.csize, sb = M12 ? 3 : a.swz_b;
 	const int runc = MG / csz;                                  // chunks per run
 	const int ncl = G * runc;                                   // chunks held by this CTA
 	const int cb = g * MG;                                      // first column of this CTA
