@@ -37,7 +37,8 @@ CTW_HD uint32_t subq(uint32_t a, uint32_t b, uint32_t q) { const uint32_t r = a 
 // (P. L. Montgomery, Modular multiplication without trial division, 1985.)
 CTW_HD uint32_t mmulq(uint32_t a, uint32_t b, uint32_t q, uint32_t qi)
 {
-	const uint32_t lo = a * b, hi = mulhi32(a, b);
+	const uint64_t p = (uint64_t)a * b;            // one wide product for lo and hi
+	const uint32_t lo = (uint32_t)p, hi = (uint32_t)(p >> 32);
 	const uint32_t mq = mulhi32(lo * qi, q);
 	const uint32_t r = hi - mq + q;
 	return umin32(r, r - q);

@@ -53,7 +53,8 @@ __device__ __forceinline__ uint32_t qiv(int pi) { return pi == 0 ? QI0 : (pi == 
 // u*w/2^32 mod q in [0, 2q) for any u < 2^32 and w < q (or u, w < 2q).
 __device__ __forceinline__ uint32_t mlazy(uint32_t u, uint32_t w, uint32_t q, uint32_t qi)
 {
-	const uint32_t lo = u * w, hi = __umulhi(u, w);
+	const uint64_t p = (uint64_t)u * w;            // one wide product for lo and hi
+	const uint32_t lo = (uint32_t)p, hi = (uint32_t)(p >> 32);
 	const uint32_t mq = __umulhi(lo * qi, q);
 	return hi - mq + q;
 }
