@@ -799,7 +799,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 		// (N-: +f -> 0 and +f -> Dn/2)
 		for (int c = tid; c < ncu; c += nt)
 		{
-			i128 acc;
+			int64_t acc;                  // a chunk carry plus digits: 64-bit arithmetic is exact
 			if (c > 0)
 			{
 				acc = fch[c - 1];
@@ -815,7 +815,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 			}
 			else
 			{
-				acc = a.minus ? (i128)fch[ncu - 1] : -(i128)fch[ncu - 1];
+				acc = a.minus ? fch[ncu - 1] : -fch[ncu - 1];
 			}
 			int i = 0;
 			bool done = false;
@@ -823,7 +823,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 			{
 				const int p = swz(c * a.csize + i, sb);
 				acc += (int32_t)X[p];
-				X[p] = (uint32_t)reduce_b<i128>(acc, b, b_inv, b_s, err);
+				X[p] = (uint32_t)reduce_b<int64_t>(acc, b, b_inv, b_s, err);
 				if (acc == 0) { done = true; break; }
 			}
 			if (!done)
@@ -940,15 +940,33 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 
 	auto transform_and_normalize = [&](int mode, int mult) {
 		__syncthreads();
-		for (int e = tid; e < M; e += nt)
+		// one (prime, column) item per thread: read the digits straight into the
+		// item's registers (no separate digit -> residue pass)
+		const bool fused = M12 && 3 * MG <= nt;
+		if (!fused)
 		{
-			const int p = (e / MG) * MG + (swz(cb + e % MG, sb) - cb);
-			const int32_t d = (int32_t)XC[p];
-			XC[p] = modq_i32(d, Q0);
-			XC[M + p] = modq_i32(d, Q1);
-			XC[2 * M + p] = modq_i32(d, Q2);
+			for (int e = tid; e < M; e += nt)
+			{
+				const int p = (e / MG) * MG + (swz(cb + e % MG, sb) - cb);
+				const int32_t d = (int32_t)XC[p];
+				XC[p] = modq_i32(d, Q0);
+				XC[M + p] = modq_i32(d, Q1);
+				XC[2 * M + p] = modq_i32(d, Q2);
+			}
+			__syncthreads();
 		}
-		__syncthreads();
+		uint32_t vf[G];
+		if (fused)
+		{
+			if (tid < 3 * MG)
+			{
+				const int pi = tid / MG, tt = tid - pi * MG;
+				const uint32_t *S0 = XC + (swz(cb + tt, sb) - cb);
+#pragma unroll
+				for (int h = 0; h < G; ++h) vf[h] = modq_i32((int32_t)S0[h * MG], qv(pi));
+			}
+			__syncthreads();              // every digit read before any residue plane is written
+		}
 		// forward cross levels, one radix-G transform per (prime, column)
 		for (int it = tid; it < 3 * MG; it += nt)
 		{
@@ -958,7 +976,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 			uint32_t *S = XC + pi * M + p0;
 			uint32_t v[G];
 #pragma unroll
-			for (int h = 0; h < G; ++h) v[h] = S[h * MG];
+			for (int h = 0; h < G; ++h) v[h] = fused ? vf[h] : S[h * MG];
 #pragma unroll
 			for (int L = 0; L < LG; ++L)
 			{
@@ -1077,12 +1095,18 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 				if (narrow)
 				{
 					int64_t acc = 0;
-					for (int i = 0; i < csz; ++i)
-					{
+					auto step = [&](int i) {
 						const int p = swz(base + i, sb) - cb;
 						acc += load64(Xh, M, p) * (int64_t)mult;
 						Xh[p] = (uint32_t)reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+					};
+					if (csz == 8)
+					{
+#pragma unroll
+						for (int i = 0; i < 8; ++i) step(i);
 					}
+					else
+						for (int i = 0; i < csz; ++i) step(i);
 					acc_f = acc;
 				}
 				else
@@ -1109,13 +1133,14 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 		for (int c = tid; c < ncu; c += nt)
 		{
 			const int h = c / runc, j = c - h * runc;
-			i128 acc;
+			// a chunk carry plus digits: |acc| < 2^62, 64-bit arithmetic is exact
+			int64_t acc;
 			if (j > 0) acc = fch[c - 1];
 			else if (g > 0) acc = *cl.map_shared_rank(xch + h, g - 1);
 			else
 			{
 				const int64_t last = *cl.map_shared_rank(xch + hl, G - 1);
-				if (h == 0) acc = a.minus ? (i128)last : -(i128)last;
+				if (h == 0) acc = a.minus ? last : -last;
 				else
 				{
 					acc = *cl.map_shared_rank(xch + (h - 1), G - 1);
@@ -1130,7 +1155,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 			{
 				const int p = swz(base + i, sb) - cb;
 				acc += (int32_t)Xh[p];
-				Xh[p] = (uint32_t)reduce_b<i128>(acc, b, b_inv, b_s, err);
+				Xh[p] = (uint32_t)reduce_b<int64_t>(acc, b, b_inv, b_s, err);
 				if (acc == 0) { done = true; break; }
 			}
 			if (!done)
