@@ -379,8 +379,27 @@ def run_serve(args):
     degrees = (12, 13, 14)
     lo, hi = math.log(12), math.log(15)
     # service demand per degree from the tuned per-lane squaring time
-    us = {k: autotune(k, 64)[2] for k in degrees}
-    mean_bits = {k: (1 << k) * 20.0 for k in degrees}
+    # capacity from the pools themselves: device time per lane-squaring of a
+    # 64-slot pool tick (squarings, multiply, register moves, graph launch)
+    from ctwin_gb300 import Pool
+    import torch
+    us = {}
+    for k in degrees:
+        lg, cs, _ = autotune(k, 64)
+        with Pool(k, 64, log2_ctas=lg, csize=cs) as p:
+            p.admit_many([rng.randrange(1 << 16, 1 << 24) for _ in range(64)])
+            p.run(1)
+            p.collect(wait=True)
+            B = p.info()["gl_block"]
+            st = torch.cuda.ExternalStream(p.stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            p.run(2)
+            e1.record(st)
+            e1.synchronize()
+            us[k] = e0.elapsed_time(e1) * 1e3 / (2 * (B + 1) * 64)
+    mean_bits = {k: (1 << k) * statistics.mean(math.log2(rng.randrange(1 << 16, 1 << 24)) for _ in range(2000))
+                 for k in degrees}
     w = {k: (math.log(k + 1) - math.log(k)) / (hi - lo) for k in degrees}
     demand = sum(w[k] * mean_bits[k] * us[k] * 1e-6 for k in degrees)
     lam = args.load / demand
@@ -438,8 +457,10 @@ def run_serve(args):
         "metric": "PRP tests/s (served, mixed degrees)", "value": len(res) / span, "unit": "tests/s",
         "n_gpus": 1, "steps": n, "warmup": 0, "ms_per_step": 1000.0 * span / max(1, len(res)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"{n} Poisson arrivals (seed 11, rate {lam:.2f}/s = {args.load:.0%} of the tuned "
-                               "capacity), degree 2^k, k log-uniform in [12, 15), b uniform in [2^16, 2^24)",
+        "config": {"workload": f"{n} Poisson arrivals (seed 11, rate {lam:.2f}/s = {args.load:.0%} of the capacity "
+                               "measured on 64-slot pool ticks), degree 2^k, k log-uniform in [12, 15), "
+                               "b uniform in [2^16, 2^24)",
+                   "us_per_lane_squaring": us,
                    "hbm_budget_gib": args.hbm_budget, "ticks_per_launch": 1},
         "latency_s": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
                       "max": lat[-1]},
