@@ -543,7 +543,7 @@ def run_sieve(args):
         from oracle import oracle as O
         O.build()
         cores = os.cpu_count() or 1
-        p_s = 1 << 36                       # bounded sample: primes below 2^36 of config 4
+        p_s = 1 << 34                       # bounded sample: primes below 2^34 of config 4
         t0 = time.perf_counter()
         O.sieve(n, b_min, b_max, p_min, p_s, 1, threads=cores)
         dt = time.perf_counter() - t0
@@ -552,7 +552,7 @@ def run_sieve(args):
         O.sieve(11, 100000, 299999, 3 * 2048 + 1, 1 << 32, 1, threads=cores)
         dt1 = time.perf_counter() - t0
         cpu = {"value": size * frac / dt, "unit": "sieved b/s", "cores": cores, "kind": "port",
-               "sample": f"config 4 primes below 2^36 ({frac:.4f} of the p range) in {dt:.1f} s; "
+               "sample": f"config 4 primes below 2^34 ({frac:.4f} of the p range) in {dt:.1f} s; "
                          f"config 1 '+' form in {dt1:.2f} s",
                "config1_pos_s": dt1}
     line = {

@@ -584,10 +584,8 @@ int ctw_pool_run(ctw_pool *p, int ticks)
 		int hi = 0;
 		for (int s = 0; s < p->slots; ++s)
 			if (p->slot[(size_t)s].state != SLOT_FREE) hi = s + 1;
-		// launch over the lowest slots only, rounded up to a power of two (few graphs)
-		int lanes = 8;
-		while (lanes < hi) lanes *= 2;
-		lanes = std::min(lanes, p->slots);
+		// launch over the lowest slots only, in steps of 8 lanes (one graph per step)
+		const int lanes = std::min(p->slots, std::max(8, (hi + 7) / 8 * 8));
 		memset(p->h_aux[k], 0, (size_t)T * 2 * S * sizeof(PrpLaneAux));
 		memset(p->h_stage[k], 0, (size_t)T * S * p->nws * 4);
 		for (int t = 0; t < T; ++t)
