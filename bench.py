@@ -23,6 +23,8 @@ Two more workloads print their own line (not the default):
          compared per degree with the plain one-candidate-per-launch-sequence path
   --workload sieve  sieved b/s of the GPU sieve on n = 20, b < 2^30, p < 2^40 (and the
          n = 11 both-form sieve of b in [10^5, 3 10^5) to 2^32 beside it)
+  --workload config1  the reference's workflow at n = 11: sieve b in [10^5, 3 10^5) to
+         2^32 (both forms), then base-3 PRP of every survivor and of its twin partner N-
   --workload serve  a seeded Poisson stream of full PRP tests, degree 2^k with k
          log-uniform in [12, 15) (k = 12, 13, 14), b uniform in [2^16, 2^24), through the
          server (continuous batching by degree, admission by pool bytes); tests/s and
@@ -575,6 +577,86 @@ def run_sieve(args):
     return 0
 
 
+def run_pool_all(pool, bs, ticks: int = 8):
+    """Every b through one pool, admitting as slots free up; results by b."""
+    queue, res = list(bs), []
+    while queue or pool.info()["active"]:
+        free = pool.slots - pool.info()["active"]
+        if queue and free:
+            k = pool.admit_many(queue[:free])
+            queue = queue[k:]
+        pool.run(ticks)
+        pool.collect(wait=True)
+        res += pool.results()
+    return {r["b"]: r for r in res}
+
+
+def run_config1(args):
+    """The reference's own workflow at n = 11: the GPU sieve of b in
+    [100000, 300000) to p < 2^32 for both forms, then the base-3 Fermat test of
+    every survivor N+ and of its twin partner N- (cyclo's PRP and the N- test)."""
+    import torch  # noqa: F401
+    from ctwin_gb300 import Pool, sieve_pass
+    from ctwin_gb300.sieve import unpack
+    n, b0, b1 = 11, 100000, 299999
+    t0 = time.perf_counter()
+    struck, _ = sieve_pass(n, b0, b1, 3 * (1 << n) + 1, 1 << 32, 1)
+    struck, _ = sieve_pass(n, b0, b1, 11, 1 << 32, -1, struck)
+    t_sieve = time.perf_counter() - t0
+    surv = [b0 + int(i) for i in np.flatnonzero(unpack(struck, b1 - b0 + 1) == 0)]
+    t0 = time.perf_counter()
+    with Pool(n, 2048, base=3) as pp:
+        plus = run_pool_all(pp, surv)
+    t_plus = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    with Pool(n, 2048, base=3, minus=True) as pm:
+        minus = run_pool_all(pm, surv)
+    t_minus = time.perf_counter() - t0
+    bad = sum(1 for r in list(plus.values()) + list(minus.values()) if r["status"] != 0 or not r["gl_ok"])
+    twins = [b for b in surv if plus[b]["is_prp"] and minus[b]["is_prp"]]
+    # parity sample: the GMP residues of the first 64 survivors (N+, base 3)
+    gold = {}
+    try:
+        for x in json.load(open(os.path.join(ROOT, "tests", "golden", "prp_gmp.json"))):
+            if x["n"] == n and x["form"] == "+" and x["base"] == 3:
+                gold[x["b"]] = int(x["res64"], 16)
+    except OSError:
+        pass
+    checked = [b for b in surv if b in gold]
+    agree = sum(1 for b in checked if plus[b]["res64"] == gold[b])
+    tests = 2 * len(surv)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        cores = os.cpu_count() or 1
+        sample = surv[:cores]
+        t1 = time.perf_counter()
+        threads = [threading.Thread(target=O.prp_check, args=(b, n, 3)) for b in sample]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        dt = time.perf_counter() - t1
+        cpu = {"value": len(sample) / dt, "unit": "PRP tests/s", "cores": cores, "kind": "port",
+               "sample": f"{len(sample)} N+ base-3 tests of degree 2^11 (oracle C restatement, one per core) "
+                         f"in {dt:.1f} s"}
+    line = {
+        "metric": "PRP tests/s (config 1: N+ and N- of every sieve survivor)", "value": tests / (t_plus + t_minus),
+        "unit": "tests/s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * (t_plus + t_minus),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "n = 11, b in [100000, 300000), sieve to p < 2^32 (both forms), base-3 Fermat "
+                               "test of N+ and N- for every survivor, pools of 2048 slots",
+                   "survivors": len(surv), "sieve_s": t_sieve, "plus_s": t_plus, "minus_s": t_minus,
+                   "twin_prps": twins, "failed": bad, "gmp_checked": len(checked), "gmp_agree": agree},
+        "e2e": {"value": tests / (t_sieve + t_plus + t_minus), "unit": "tests/s", "h2d_bytes_per_step": None,
+                "d2h_bytes_per_step": None},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
@@ -586,7 +668,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve", "sieve"])
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve", "sieve", "config1"])
     ap.add_argument("--candidates", type=int, default=4096, help="batch: candidates")
     ap.add_argument("--requests", type=int, default=0, help="serve: requests (0: rate x --serve-seconds)")
     ap.add_argument("--serve-seconds", type=float, default=60.0)
@@ -618,6 +700,8 @@ def main():
         return run_serve(args) if rank == 0 else 0
     if args.workload == "sieve":
         return run_sieve(args) if rank == 0 else 0
+    if args.workload == "config1":
+        return run_config1(args) if rank == 0 else 0
     import ctwin_gb300
     from ctwin_gb300 import PrpEngine
     from ctwin_gb300._native import lib

@@ -90,6 +90,7 @@ def lib() -> ctypes.CDLL:
             "ctw_prp_autotune": ([i32, i32, vp, vp, vp], i32),
             "ctw_pool_create": ([i32, i32, i32, i32, u32, i32, ctypes.POINTER(H)], i32),
             "ctw_pool_destroy": ([H], i32),
+            "ctw_pool_create_minus": ([i32, i32, i32, u32, i32, ctypes.POINTER(H)], i32),
             "ctw_pool_slot_bytes": ([i32], ctypes.c_size_t),
             "ctw_pool_admit": ([H, u32, ctypes.c_uint64], i32),
             "ctw_pool_admit_many": ([H, vp, vp, i32, i32], i32),

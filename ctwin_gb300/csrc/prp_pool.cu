@@ -74,9 +74,10 @@ size_t pool_bytes_estimate(int ln, int lg, int slots, int B)
 	return (size_t)slots * pool_slot_bytes(ln, B) + 2 * 3 * D * 4 + shoup + 4;
 }
 
-void slot_prepare(PreparedTest &t, int ln, int B)
+void slot_prepare(PreparedTest &t, int ln, int B, bool minus)
 {
 	t.E = prp_exponent(t.b, ln);
+	if (minus) big_sub_inplace(t.E, big_from_u64(2));
 	t.res = big_block_sum(t.E, B);
 	t.B = B;
 }
@@ -173,6 +174,9 @@ struct ctw_pool {
 	long long squarings = 0;
 	size_t bytes = 0;
 	bool direct = false;     // CTW_POOL_DIRECT=1: direct launches, each checked (diagnostics)
+	int minus = 0;           // N- = b^Dn - b^{Dn/2} - 1 on the transform of degree D = 2 Dn
+	int ln_test = 0;         // log2 of the tested degree (ln, or ln - 1 for N-)
+	size_t Dn = 0;           // digits of the tested numbers
 };
 
 namespace {
@@ -254,6 +258,7 @@ int pool_init(ctw_pool *p)
 	a.mult = (int)p->base;
 	a.tw_smem = p->tw_smem;
 	a.narrow = 0;                 // per lane (lane_b[3])
+	a.minus = p->minus;
 	a.scratch = p->d_scratch;
 	a.use_dupmask = 0;
 	POOL_CUDA(cudaDeviceSynchronize());
@@ -388,23 +393,27 @@ int finish_slot(ctw_pool *p, int s, bool status_bad)
 	ctw_result r{};
 	r.tag = sl.tag;
 	r.b = sl.b;
-	r.log2_degree = p->ln;
+	r.log2_degree = p->ln_test;
 	r.slot = s;
 	r.squarings = sl.squarings;
 	r.t_submit = p->t_submit[(size_t)s];
 	r.t_admit = p->t_admit[(size_t)s];
 	r.t_done = mono_seconds();
-	std::vector<uint32_t> cy(D), cd(D), cx(D);
-	int rc = canonical(p->h_read, sl.b, D, cy.data());
-	if (!rc) rc = canonical(p->h_read + D, sl.b, D, cd.data());
-	if (!rc) rc = canonical(p->h_read + 2 * D, sl.b, D, cx.data());
+	const size_t Dn = p->Dn;
+	std::vector<uint32_t> cy(Dn), cd(Dn), cx(Dn);
+	auto canon = [&](const int32_t *x, uint32_t *o) {
+		return p->minus ? canonical_minus(x, sl.b, Dn, o) : canonical(x, sl.b, D, o);
+	};
+	int rc = canon(p->h_read, cy.data());
+	if (!rc) rc = canon(p->h_read + D, cd.data());
+	if (!rc) rc = canon(p->h_read + 2 * D, cx.data());
 	if (rc || status_bad)
 		r.status = (int8_t)(rc ? rc : CTW_E_COMPUTE);
 	else
 	{
 		bool prp, zero;
 		uint64_t r64;
-		res64_of(cx.data(), sl.b, D, prp, zero, r64);
+		res64_of(cx.data(), sl.b, Dn, prp, zero, r64);
 		r.is_prp = prp ? 1 : 0;
 		r.res64 = r64;
 		r.gl_ok = (cy == cd) ? 1 : 0;
@@ -439,7 +448,7 @@ int pool_admit_prepared(ctw_pool *p, PreparedTest &&t, uint64_t tag, double t_su
 }
 
 int pool_block(const ctw_pool *p) { return p->B; }
-int pool_degree(const ctw_pool *p) { return p->ln; }
+int pool_degree(const ctw_pool *p) { return p->ln_test; }
 int pool_free_slots(const ctw_pool *p) { return p->slots - p->active; }
 int pool_active(const ctw_pool *p) { return p->active; }
 int pool_in_flight(const ctw_pool *p) { return (p->ev_pending[0] ? 1 : 0) + (p->ev_pending[1] ? 1 : 0); }
@@ -455,7 +464,25 @@ size_t ctw_pool_slot_bytes(int log2_degree)
 	return pool_slot_bytes(log2_degree, default_gl_block(log2_degree));
 }
 
+static int pool_create(int log2_degree, int slots, int log2_ctas, int csize, uint32_t base, int gl_block, int minus,
+                       ctw_pool **out);
+
 int ctw_pool_create(int log2_degree, int slots, int log2_ctas, int csize, uint32_t base, int gl_block, ctw_pool **out)
+{
+	return pool_create(log2_degree, slots, log2_ctas, csize, base, gl_block, 0, out);
+}
+
+int ctw_pool_create_minus(int log2_degree, int slots, int csize, uint32_t base, int gl_block, ctw_pool **out)
+{
+	if (log2_degree < 8 || log2_degree > 16) return fail(CTW_E_ARG, "N- log2_degree %d outside [8, 16]", log2_degree);
+	// the split of ctw_prp_create_minus: one CTA up to 2^12 coefficients, else >= 4 CTAs
+	const int ln2 = log2_degree + 1;
+	const int lg = ln2 <= 12 ? 0 : std::max(2, prp_lg_for(ln2));
+	return pool_create(ln2, slots, lg, csize, base, gl_block, 1, out);
+}
+
+static int pool_create(int log2_degree, int slots, int log2_ctas, int csize, uint32_t base, int gl_block, int minus,
+                       ctw_pool **out)
 {
 	if (!out) return fail(CTW_E_ARG, "null output pointer");
 	*out = nullptr;
@@ -478,9 +505,12 @@ int ctw_pool_create(int log2_degree, int slots, int log2_ctas, int csize, uint32
 	p->slots = slots;
 	p->csize = csize;
 	p->base = base;
-	p->B = gl_block ? gl_block : default_gl_block(log2_degree);
+	p->minus = minus;
+	p->ln_test = minus ? log2_degree - 1 : log2_degree;
+	p->B = gl_block ? gl_block : default_gl_block(p->ln_test);
 	p->nws = stage_words(p->B);
 	p->D = (size_t)1 << log2_degree;
+	p->Dn = minus ? p->D / 2 : p->D;
 	p->G = (size_t)1 << lg;
 	p->M = p->D / p->G;
 	p->tw_smem = prp_smem_bytes(lm, lg, 1) <= 227 * 1024 ? 1 : 0;
@@ -535,7 +565,7 @@ int ctw_pool_admit(ctw_pool *p, uint32_t b, uint64_t tag)
 	if (p->active >= p->slots) return CTW_E_FULL;
 	PreparedTest t;
 	t.b = b;
-	slot_prepare(t, p->ln, p->B);
+	slot_prepare(t, p->ln_test, p->B, p->minus != 0);
 	return pool_admit_prepared(p, std::move(t), tag, mono_seconds());
 }
 
@@ -553,7 +583,7 @@ int ctw_pool_admit_many(ctw_pool *p, const uint32_t *b, const uint64_t *tags, in
 			for (int i = t; i < n; i += nt)
 			{
 				prep[(size_t)i].b = b[i];
-				slot_prepare(prep[(size_t)i], p->ln, p->B);
+				slot_prepare(prep[(size_t)i], p->ln_test, p->B, p->minus != 0);
 			}
 		});
 	for (auto &x : th) x.join();

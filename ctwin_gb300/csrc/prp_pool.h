@@ -51,7 +51,8 @@ int default_gl_block(int ln);
 size_t pool_slot_bytes(int ln, int B);
 // Device bytes of a whole pool (slots, root tables, status), as pool creation allocates them.
 size_t pool_bytes_estimate(int ln, int lg, int slots, int B);
-void slot_prepare(PreparedTest &t, int ln, int B);
+// E = b^D - b^{D/2} (N+) or b^D - b^{D/2} - 2 (N-, minus) for D = 2^ln, and its block sum.
+void slot_prepare(PreparedTest &t, int ln, int B, bool minus = false);
 void slot_start(PoolSlot &s, PreparedTest &&t, uint64_t tag);
 SlotTick slot_tick(PoolSlot &s, int B);
 

@@ -50,12 +50,18 @@ class Pool:
     """`slots` resident tests of degree 2^log2_degree (continuous batching)."""
 
     def __init__(self, log2_degree: int, slots: int, log2_ctas: int = -1, csize: int = 0, base: int = 2,
-                 gl_block: int = 0):
+                 gl_block: int = 0, minus: bool = False):
+        """minus=True: tests of the twin partners N- = b^D - b^{D/2} - 1 (the
+        split is then chosen as for PrpEngine(minus=True))."""
         h = ctypes.c_void_p()
-        check(lib().ctw_pool_create(log2_degree, slots, log2_ctas, csize, base, gl_block, ctypes.byref(h)))
+        if minus:
+            check(lib().ctw_pool_create_minus(log2_degree, slots, csize, base, gl_block, ctypes.byref(h)))
+        else:
+            check(lib().ctw_pool_create(log2_degree, slots, log2_ctas, csize, base, gl_block, ctypes.byref(h)))
         self._h = h
         self.ln = log2_degree
         self.D = 1 << log2_degree
+        self.regD = self.D * (2 if minus else 1)
         self.slots = slots
 
     def close(self):
@@ -124,7 +130,7 @@ class Pool:
         return d
 
     def read_slot(self, slot: int, reg: int) -> np.ndarray:
-        out = np.zeros(self.D, dtype=np.int32)
+        out = np.zeros(self.regD, dtype=np.int32)
         check(lib().ctw_pool_read_slot(self._h, slot, reg, ptr(out)))
         return out
 

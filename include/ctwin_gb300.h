@@ -232,6 +232,9 @@ typedef struct ctw_pool ctw_pool;
  * b.  Results are bit-identical to ctw_prp_run's. */
 int ctw_pool_create(int log2_degree, int slots, int log2_ctas, int csize, uint32_t base, int gl_block,
                     ctw_pool **out);
+/* A pool of twin partners N- = b^D - b^{D/2} - 1 (D = 2^log2_degree, 8..16;
+ * see ctw_prp_create_minus); every pool call applies unchanged. */
+int ctw_pool_create_minus(int log2_degree, int slots, int csize, uint32_t base, int gl_block, ctw_pool **out);
 int ctw_pool_destroy(ctw_pool *p);
 /* Device bytes a pool holds per slot at this degree (admission by footprint). */
 size_t ctw_pool_slot_bytes(int log2_degree);

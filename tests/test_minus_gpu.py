@@ -84,3 +84,26 @@ def test_minus_mul(native):
         x = O.digits_to_int([int(v) for v in regs[0, l, : 1 << n]], b)
         y = O.digits_to_int([int(v) for v in regs[1, l, : 1 << n]], b)
         assert O.digits_to_int(got[l], b) == x * y % N
+
+
+@pytest.mark.parametrize("n", [8, 11])
+def test_minus_pool_matches_gmp(native, n):
+    """N- tests in a pool (continuous batching on the degree-2D transform)."""
+    from ctwin_gb300 import Pool
+    cases = minus_cases(n)[:40]
+    with Pool(n, 16, minus=True) as p:
+        queue = [c[0] for c in cases]
+        res = []
+        while queue or p.info()["active"]:
+            take = min(len(queue), 16 - p.info()["active"])
+            if take:
+                assert p.admit_many(queue[:take]) == take
+                queue = queue[take:]
+            p.run(4)
+            p.collect(wait=True)
+            res += p.results()
+    want = {b: (prp, r64) for b, r64, prp in cases}
+    assert sorted(r["b"] for r in res) == sorted(want)
+    for r in res:
+        assert r["status"] == 0 and r["gl_ok"] and r["log2_degree"] == n
+        assert (r["is_prp"], r["res64"]) == want[r["b"]], r
