@@ -10,8 +10,9 @@ work cyclo::check does between two checkpoints (cyclo/src/cyclo.h:277-308).
   e2e    same metric through the C ABI with host buffers: per step the exponent
          slice is copied host->device and the residue read back device->host
   roofline  32-bit integer multiply-add work per launch (4 IMAD per Montgomery
-         multiply, 3 D log2 D + 9 D multiplies per squaring) / launch time,
-         against the IMAD throughput probed on the same GPU in this run
+         multiply, P (D log2 D + 3 D) multiplies per squaring for P NTT primes:
+         P = 2 when b keeps the product exact in two primes, as here, else 3)
+         / launch time, against the IMAD throughput probed on the same GPU in this run
   cpu_baseline  the oracle's C restatement of the reference transform (the
          reference has no CPU PRP path), one candidate per host core
 
@@ -90,8 +91,9 @@ def hbm_line(traffic: float, seconds: float) -> dict:
             "peak_source": "MEASURED_PEAKS.json" if peak else None}
 
 
-def imad_per_squaring(D: int) -> float:
-    return 4.0 * (3 * D * math.log2(D) + 9 * D)
+def imad_per_squaring(D: int, primes: int = 3) -> float:
+    """4 IMAD per modular multiply; per NTT prime D log2 D + 3 D multiplies per squaring."""
+    return 4.0 * primes * (D * math.log2(D) + 3 * D)
 
 
 class ClockSampler:
@@ -772,7 +774,8 @@ def main():
         sq_times.append(e0.elapsed_time(e1) / 1000.0)
         i -= B_GL
     t_launch = statistics.median(sq_times)
-    achieved = imad_per_squaring(D) * B_GL / t_launch
+    primes = eng.prime_count
+    achieved = imad_per_squaring(D, primes) * B_GL / t_launch
     geo = eng.geometry()
 
     # e2e through the C ABI with host buffers: exponent slice in, residue out
@@ -819,7 +822,7 @@ def main():
                    "step": "one Gerbicz-Li block: B_GL resident squarings + one multiply",
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}",
                    "cluster_ctas": geo["ctas_per_lane"], "threads_per_cta": geo["threads"],
-                   "smem_per_cta": geo["smem_bytes"]},
+                   "smem_per_cta": geo["smem_bytes"], "ntt_primes": primes},
         "tests_per_s_projected": value / (i0 + 1),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": peak_imad / 1e12, "unit": "T IMAD/s",

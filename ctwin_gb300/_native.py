@@ -48,6 +48,9 @@ def lib() -> ctypes.CDLL:
             "ctw_prp_create": ([i32, i32, ctypes.POINTER(H)], i32),
             "ctw_prp_destroy": ([H], i32),
             "ctw_prp_set_csize": ([H, i32], i32),
+            "ctw_prp_set_prime_count": ([H, i32], i32),
+            "ctw_prp_prime_count": ([H], i32),
+            "ctw_prp_two_primes": ([i32, i32, u32], i32),
             "ctw_prp_set_base": ([H, u32], i32),
             "ctw_prp_set_b": ([H, vp, i32], i32),
             "ctw_prp_set": ([H, u32], i32),
@@ -99,6 +102,8 @@ def lib() -> ctypes.CDLL:
             "ctw_pool_results": ([H, vp, i32], i32),
             "ctw_pool_info": ([H, vp, vp, vp, vp, vp, vp, vp], i32),
             "ctw_pool_read_slot": ([H, i32, i32, vp], i32),
+            "ctw_pool_set_prime_count": ([H, i32], i32),
+            "ctw_pool_prime_count": ([H], i32),
             "ctw_pool_stream": ([H], vp),
             "ctw_pool_schedule": ([i32, u32, i32, vp, i32, vp], i32),
             "ctw_server_create": ([ctypes.c_size_t, i32, u32, i32, i32, ctypes.POINTER(H)], i32),

@@ -162,6 +162,9 @@ struct ctw_prp {
 	size_t smem = 0;
 	int tw_smem = 0;
 	int narrow = 0;                   // 64-bit carry arithmetic is exact for the current b
+	int nprime = 3;                   // NTT primes of the launches (2 when exact for the current b)
+	int prime_mode = 0;               // 0: two primes whenever exact; 3: always three
+	uint32_t bmax = 0;                // largest b of the lanes
 	int minus = 0;                    // N- = b^Dn - b^{Dn/2} - 1 on the transform of degree D = 2 Dn
 	size_t Dn = 0;                    // degree of the tested numbers (D, or D/2 for N-)
 	cudaStream_t stream = nullptr;
@@ -226,8 +229,18 @@ PrpKernelArgs make_args(ctw_prp *h)
 	a.tw_smem = h->tw_smem;
 	a.narrow = h->narrow;
 	a.minus = h->minus;
+	a.nprime = h->nprime;
 	a.scratch = h->d_scratch;
 	return a;
+}
+
+// Two NTT primes when the split has a two-prime kernel and the product of two
+// residues stays exact with them for every lane's b (prp_two_primes_exact).
+void choose_primes(ctw_prp *h)
+{
+	const double terms = h->minus ? (double)h->Dn : 1.5 * (double)h->D;
+	h->nprime = (h->prime_mode != 3 && h->bmax > 0 && prp_two_prime_split(h->lm, h->lg) &&
+	             prp_two_primes_exact(terms, h->bmax)) ? 2 : 3;
 }
 
 int launch(ctw_prp *h, const PrpKernelArgs &a)
@@ -466,10 +479,32 @@ int ctw_prp_set_b(ctw_prp *h, const uint32_t *b, int count)
 	}
 	// |coefficient| <= 1.5 D b^2, accumulated x3 plus carries: 64-bit when 8 D b^2 < 2^62
 	h->narrow = (8.0 * (double)h->D * (double)bmax * (double)bmax < 4.611686018427388e18) ? 1 : 0;
+	h->bmax = bmax;
+	choose_primes(h);
 	CTW_CUDA(cudaMemcpyAsync(h->d_laneb, lb.data(), lb.size() * 4, cudaMemcpyHostToDevice, h->stream));
 	CTW_CUDA(cudaStreamSynchronize(h->stream));
 	return CTW_OK;
 }
+
+int ctw_prp_two_primes(int log2_degree, int minus, uint32_t b)
+{
+	if (minus ? (log2_degree < 8 || log2_degree > 16) : (log2_degree < 8 || log2_degree > 18)) return 0;
+	const int ln = minus ? log2_degree + 1 : log2_degree;
+	const int lg = minus ? (ln <= 12 ? 0 : std::max(2, prp_lg_for(ln))) : prp_lg_for(ln);
+	const double Dn = (double)((size_t)1 << log2_degree);
+	return (prp_two_prime_split(ln - lg, lg) && prp_two_primes_exact(minus ? Dn : 1.5 * Dn, b)) ? 1 : 0;
+}
+
+int ctw_prp_set_prime_count(ctw_prp *h, int count)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (count != 0 && count != 3) return fail(CTW_E_ARG, "prime count %d not in {0 (automatic), 3}", count);
+	h->prime_mode = count;
+	choose_primes(h);
+	return CTW_OK;
+}
+
+int ctw_prp_prime_count(ctw_prp *h) { return h ? h->nprime : 0; }
 
 int ctw_prp_set(ctw_prp *h, uint32_t a)
 {
@@ -735,9 +770,12 @@ void *ctw_prp_stream(ctw_prp *h) { return h ? (void *)h->stream : nullptr; }
 int ctw_prp_geometry(ctw_prp *h, int *ctas, int *threads, int *smem)
 {
 	if (int rc = check_handle(h)) return rc;
+	// the launch shape of the current prime count
+	const int np = h->nprime;
+	const int tw = np == 2 ? (prp_smem_bytes(h->lm, h->lg, 1, 2) <= 227 * 1024 ? 1 : 0) : h->tw_smem;
 	if (ctas) *ctas = (int)h->G;
-	if (threads) *threads = h->threads;
-	if (smem) *smem = (int)h->smem;
+	if (threads) *threads = prp_threads(h->lm, np);
+	if (smem) *smem = (int)prp_smem_bytes(h->lm, h->lg, tw, np);
 	return CTW_OK;
 }
 

@@ -215,7 +215,7 @@ __device__ __forceinline__ Pass pass_at(int lm, int i)
 
 // Generic radix-R pass over the CTA's M coefficients, one prime per item.
 // dir: 0 forward, 1 inverse; LAST: fused forward + pointwise + inverse.
-template <int R, bool LAST>
+template <int R, bool LAST, int NP>
 __device__ void run_pass(uint32_t *X, const uint32_t *TF, const uint32_t *TI, int M, int lm, int l0, int dir,
                          int mode, bool special_local0, const PrpKernelArgs &a, const uint32_t *ybase,
                          uint32_t *ystore, int tid, int nt)
@@ -223,7 +223,7 @@ __device__ void run_pass(uint32_t *X, const uint32_t *TF, const uint32_t *TI, in
 	constexpr int r = Log2<R>::v;
 	const int ng = M >> r, stride = M >> (l0 + r);
 	const int lsh = lm - l0 - r, sb = a.swz_b;
-	for (int it = tid; it < 3 * ng; it += nt)
+	for (int it = tid; it < NP * ng; it += nt)
 	{
 		const int pi = it >> (lm - r);
 		const int gam = it & (ng - 1);
@@ -253,21 +253,22 @@ __device__ void run_pass(uint32_t *X, const uint32_t *TF, const uint32_t *TI, in
 	}
 }
 
-template <bool LAST>
+template <bool LAST, int NP>
 __device__ __forceinline__ void dispatch_pass(uint32_t *X, const uint32_t *TF, const uint32_t *TI, int M, int lm,
                                               Pass ps, int dir, int mode, bool sp, const PrpKernelArgs &a,
                                               const uint32_t *ybase, uint32_t *ystore, int tid, int nt)
 {
 	switch (ps.r)
 	{
-	case 1: run_pass<2, LAST>(X, TF, TI, M, lm, ps.l0, dir, mode, sp, a, ybase, ystore, tid, nt); break;
-	case 2: run_pass<4, LAST>(X, TF, TI, M, lm, ps.l0, dir, mode, sp, a, ybase, ystore, tid, nt); break;
-	case 3: run_pass<8, LAST>(X, TF, TI, M, lm, ps.l0, dir, mode, sp, a, ybase, ystore, tid, nt); break;
-	default: run_pass<16, LAST>(X, TF, TI, M, lm, ps.l0, dir, mode, sp, a, ybase, ystore, tid, nt); break;
+	case 1: run_pass<2, LAST, NP>(X, TF, TI, M, lm, ps.l0, dir, mode, sp, a, ybase, ystore, tid, nt); break;
+	case 2: run_pass<4, LAST, NP>(X, TF, TI, M, lm, ps.l0, dir, mode, sp, a, ybase, ystore, tid, nt); break;
+	case 3: run_pass<8, LAST, NP>(X, TF, TI, M, lm, ps.l0, dir, mode, sp, a, ybase, ystore, tid, nt); break;
+	default: run_pass<16, LAST, NP>(X, TF, TI, M, lm, ps.l0, dir, mode, sp, a, ybase, ystore, tid, nt); break;
 	}
 }
 
 // Generic local transform: forward passes, pointwise op, inverse passes.
+template <int NP>
 __device__ void local_transform(uint32_t *X, const uint32_t *TF, const uint32_t *TI, int M, int lm, int mode,
                                 bool sp, const PrpKernelArgs &a, const uint32_t *ybase, uint32_t *ystore, int tid,
                                 int nt)
@@ -275,15 +276,15 @@ __device__ void local_transform(uint32_t *X, const uint32_t *TF, const uint32_t 
 	const int np = pass_count(lm);
 	for (int i = 0; i < np - 1; ++i)
 	{
-		dispatch_pass<false>(X, TF, TI, M, lm, pass_at(lm, i), 0, mode, sp, a, ybase, ystore, tid, nt);
+		dispatch_pass<false, NP>(X, TF, TI, M, lm, pass_at(lm, i), 0, mode, sp, a, ybase, ystore, tid, nt);
 		__syncthreads();
 	}
-	dispatch_pass<true>(X, TF, TI, M, lm, pass_at(lm, np - 1), 0, mode, sp, a, ybase, ystore, tid, nt);
+	dispatch_pass<true, NP>(X, TF, TI, M, lm, pass_at(lm, np - 1), 0, mode, sp, a, ybase, ystore, tid, nt);
 	__syncthreads();
 	if (mode == LM_FWD_ONLY) return;
 	for (int i = np - 2; i >= 0; --i)
 	{
-		dispatch_pass<false>(X, TF, TI, M, lm, pass_at(lm, i), 1, mode, sp, a, ybase, ystore, tid, nt);
+		dispatch_pass<false, NP>(X, TF, TI, M, lm, pass_at(lm, i), 1, mode, sp, a, ybase, ystore, tid, nt);
 		__syncthreads();
 	}
 }
@@ -400,21 +401,22 @@ __device__ __forceinline__ void pass12(uint32_t *X, const uint32_t *TF, const ui
 	for (int k = 0; k < 16; ++k) P[ph[k]] = u[k];
 }
 
-// 768 items per pass: (prime, radix-16 group).
+// NP * 256 items per pass: (prime, radix-16 group).
+template <int NP>
 __device__ void local_transform12(uint32_t *X, const uint32_t *TF, const uint32_t *TI, const uint32_t *SF,
                                   const uint32_t *SI, int mode, bool sp, const PrpKernelArgs &a,
                                   const uint32_t *ybase, uint32_t *ystore, int tid, int nt)
 {
-	for (int it = tid; it < 768; it += nt) pass12<0>(X, TF, TI, SF, SI, 0, mode, sp, a, ybase, ystore, it);
+	for (int it = tid; it < NP * 256; it += nt) pass12<0>(X, TF, TI, SF, SI, 0, mode, sp, a, ybase, ystore, it);
 	__syncthreads();
-	for (int it = tid; it < 768; it += nt) pass12<1>(X, TF, TI, SF, SI, 0, mode, sp, a, ybase, ystore, it);
+	for (int it = tid; it < NP * 256; it += nt) pass12<1>(X, TF, TI, SF, SI, 0, mode, sp, a, ybase, ystore, it);
 	__syncthreads();
-	for (int it = tid; it < 768; it += nt) pass12<2>(X, TF, TI, SF, SI, 0, mode, sp, a, ybase, ystore, it);
+	for (int it = tid; it < NP * 256; it += nt) pass12<2>(X, TF, TI, SF, SI, 0, mode, sp, a, ybase, ystore, it);
 	__syncthreads();
 	if (mode == LM_FWD_ONLY) return;
-	for (int it = tid; it < 768; it += nt) pass12<1>(X, TF, TI, SF, SI, 1, mode, sp, a, ybase, ystore, it);
+	for (int it = tid; it < NP * 256; it += nt) pass12<1>(X, TF, TI, SF, SI, 1, mode, sp, a, ybase, ystore, it);
 	__syncthreads();
-	for (int it = tid; it < 768; it += nt) pass12<0>(X, TF, TI, SF, SI, 1, mode, sp, a, ybase, ystore, it);
+	for (int it = tid; it < NP * 256; it += nt) pass12<0>(X, TF, TI, SF, SI, 1, mode, sp, a, ybase, ystore, it);
 	__syncthreads();
 }
 
@@ -500,6 +502,19 @@ __device__ __forceinline__ void garner3(uint32_t r0, uint32_t r1, uint32_t r2, c
 	w2 = (uint32_t)(uv >> 64);
 }
 
+// Balanced CRT value of residues r0 mod q0 and r1 mod q1 as a 64-bit two's
+// complement word (two-prime launches: every product coefficient lies in
+// (-q0 q1 / 2, q0 q1 / 2)).  x = r1 + q1 a1, a1 = (r0 - r1) / q1 mod q0, in [0, q0 q1).
+__device__ __forceinline__ void garner2(uint32_t r0, uint32_t r1, const PrpKernelArgs &a, uint32_t &w0, uint32_t &w1)
+{
+	constexpr uint64_t P2 = (uint64_t)Q0 * Q1;
+	const uint32_t a1 = mmulq(subq(r0, r1, Q0), a.ginv[2], Q0, QI0);   // r1 < q1 < q0
+	const uint64_t x = (uint64_t)r1 + (uint64_t)Q1 * a1;
+	const uint64_t v = (2 * x > P2) ? x - P2 : x;
+	w0 = (uint32_t)v;
+	w1 = (uint32_t)(v >> 32);
+}
+
 __device__ __forceinline__ i128 load96(const uint32_t *X, int M, int p)
 {
 	const uint64_t lo = (uint64_t)X[p] | ((uint64_t)X[M + p] << 32);
@@ -515,6 +530,34 @@ __device__ __forceinline__ void store96(uint32_t *X, int M, int p, i128 v)
 	X[p] = (uint32_t)v;
 	X[M + p] = (uint32_t)(v >> 32);
 	X[2 * M + p] = (uint32_t)(v >> 64);
+}
+__device__ __forceinline__ void store64(uint32_t *X, int M, int p, int64_t v)
+{
+	X[p] = (uint32_t)v;
+	X[M + p] = (uint32_t)((uint64_t)v >> 32);
+}
+// Garner on the NP planes at word p, the result as 96-bit (NP = 3) or 64-bit words.
+template <int NP>
+__device__ __forceinline__ void garner_at(uint32_t *X, int M, int p, const PrpKernelArgs &a, bool narrow)
+{
+	uint32_t w0, w1;
+	if constexpr (NP == 3)
+	{
+		uint32_t w2;
+		garner3(X[p], X[M + p], X[2 * M + p], a, narrow, w0, w1, w2);
+		X[2 * M + p] = w2;
+	}
+	else garner2(X[p], X[M + p], a, w0, w1);
+	X[p] = w0;
+	X[M + p] = w1;
+}
+// Residues of a digit in the NP planes at word p.
+template <int NP>
+__device__ __forceinline__ void to_residues(uint32_t *X, int M, int p, int32_t d)
+{
+	X[p] = modq_i32(d, Q0);
+	X[M + p] = modq_i32(d, Q1);
+	if constexpr (NP == 3) X[2 * M + p] = modq_i32(d, Q2);
 }
 
 // ---------------------------------------------------------------------------
@@ -675,10 +718,11 @@ __host__ __device__ __forceinline__ size_t smem_stage_words(int lm, int lg, int 
 	return stage > fch ? stage : fch;
 }
 
-template <int LG, bool M12>
-__global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKernelArgs a)
+template <int LG, bool M12, int NP>
+__global__ void __launch_bounds__(M12 ? NP * 256 : NT_MAX, 1) prp_kernel(const PrpKernelArgs a)
 {
 	constexpr int G = 1 << LG;
+	static_assert(NP == 3 || LG == 0, "two-prime launches use one CTA or the column layout");
 	extern __shared__ __align__(16) uint32_t sm[];
 	const int lm = M12 ? 12 : a.lm, M = 1 << lm, D = M * G;   // compile-time sizes on the 4096 path
 	const int tid = threadIdx.x, nt = blockDim.x;
@@ -687,32 +731,34 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 	const int lane = blockIdx.x / G;
 	const int ncl = M / a.csize, sb = M12 ? 3 : a.swz_b;
 
-	uint32_t *X = sm;                                           // [3][M] swizzled planes
-	uint32_t *ST = sm + 3 * M;                                  // stage / chunk carries
+	uint32_t *X = sm;                                           // [NP][M] swizzled planes
+	uint32_t *ST = sm + NP * M;                                 // stage / chunk carries
 	int64_t *fch = reinterpret_cast<int64_t *>(ST);             // [M/8]
 	const size_t sw = smem_stage_words(lm, LG, a.scols);
 	int64_t *xch = reinterpret_cast<int64_t *>(ST + sw);        // [2] carry out of this CTA's last chunk
-	uint32_t *TF = ST + sw + 8;                                 // [3][M] forward roots of this CTA
-	uint32_t *TI = TF + 3 * M;                                  // [3][M] inverse roots
+	uint32_t *TF = ST + sw + 8;                                 // [NP][M] forward roots of this CTA
+	uint32_t *TI = TF + NP * M;                                 // [NP][M] inverse roots
 
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
 	const int b_s = (int)a.lane_b[4 * lane + 2];
-	const bool narrow = (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;   // launch-wide or per-lane 64-bit carries
+	// 64-bit carries: always with two primes, else launch-wide or per lane
+	const bool narrow = NP == 2 || (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;
 	uint32_t err = 0;
 
-	// Root tables are laid out [G][3][M]: the slice of CTA g is contiguous.
+	// Root tables are laid out [G][3][M]: the slice of CTA g is contiguous,
+	// and a two-prime launch uses the first two primes of it.
 	const uint32_t *tfg = a.tf + (size_t)g * 3 * M, *tig = a.ti + (size_t)g * 3 * M;
 	if (a.tw_smem)
 	{
-		for (int i = tid; i < 3 * M; i += nt) { TF[i] = tfg[i]; TI[i] = tig[i]; }
+		for (int i = tid; i < NP * M; i += nt) { TF[i] = tfg[i]; TI[i] = tig[i]; }
 	}
 	const uint32_t *TFl = a.tw_smem ? TF : tfg;
 	const uint32_t *TIl = a.tw_smem ? TI : tig;
-	uint32_t *SF = a.tw_smem ? TI + 3 * M : TF, *SI = SF + 3 * 256 * 2;   // Shoup roots of levels 0..7 (M12)
+	uint32_t *SF = a.tw_smem ? TI + NP * M : TF, *SI = SF + NP * 256 * 2;   // Shoup roots of levels 0..7 (M12)
 	if constexpr (M12)
 	{
 		const uint32_t *sfg = a.tfs + (size_t)g * 3 * 256 * 2, *sig = a.tis + (size_t)g * 3 * 256 * 2;
-		for (int i = tid; i < 3 * 256 * 2; i += nt) { SF[i] = sfg[i]; SI[i] = sig[i]; }
+		for (int i = tid; i < NP * 256 * 2; i += nt) { SF[i] = sfg[i]; SI[i] = sig[i]; }
 	}
 
 	const size_t lane_off = (size_t)lane * D + (size_t)g * M;
@@ -737,15 +783,12 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 			for (int t = tid; t < M; t += nt)
 			{
 				const int p = swz(t, sb);
-				const int32_t d = (int32_t)X[p];
-				X[p] = modq_i32(d, Q0);
-				X[M + p] = modq_i32(d, Q1);
-				X[2 * M + p] = modq_i32(d, Q2);
+				to_residues<NP>(X, M, p, (int32_t)X[p]);
 			}
 			__syncthreads();
 		}
-		if constexpr (M12) local_transform12(X, TFl, TIl, SF, SI, mode, sp_local, a, scr, scr, tid, nt);
-		else local_transform(X, TFl, TIl, M, lm, mode, sp_local, a, scr, scr, tid, nt);
+		if constexpr (M12) local_transform12<NP>(X, TFl, TIl, SF, SI, mode, sp_local, a, scr, scr, tid, nt);
+		else local_transform<NP>(X, TFl, TIl, M, lm, mode, sp_local, a, scr, scr, tid, nt);
 		if (mode == LM_FWD_ONLY) return;
 		if constexpr (LG > 0)
 		{
@@ -755,15 +798,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 		}
 		else
 		{
-			for (int t = tid; t < M; t += nt)
-			{
-				const int p = swz(t, sb);
-				uint32_t w0, w1, w2;
-				garner3(X[p], X[M + p], X[2 * M + p], a, narrow, w0, w1, w2);
-				X[p] = w0;
-				X[M + p] = w1;
-				X[2 * M + p] = w2;
-			}
+			for (int t = tid; t < M; t += nt) garner_at<NP>(X, M, swz(t, sb), a, narrow);
 			__syncthreads();
 		}
 		// N- = b^Dn - b^{Dn/2} - 1 (one CTA, M = 2 Dn): the transform gave the
@@ -777,10 +812,21 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 				const int Dh = M / 2, Dq = M / 4;
 				for (int j = tid; j < Dh; j += nt)
 				{
-					i128 v = load96(X, M, swz(j, sb)) + load96(X, M, swz(j + Dh, sb));
-					if (j < Dq) v += load96(X, M, swz(j + Dh + Dq, sb));
-					else v += load96(X, M, swz(j + Dq, sb)) + load96(X, M, swz(j + Dh, sb));
-					store96(X, M, swz(j, sb), v);
+					if constexpr (NP == 3)
+					{
+						i128 v = load96(X, M, swz(j, sb)) + load96(X, M, swz(j + Dh, sb));
+						if (j < Dq) v += load96(X, M, swz(j + Dh + Dq, sb));
+						else v += load96(X, M, swz(j + Dq, sb)) + load96(X, M, swz(j + Dh, sb));
+						store96(X, M, swz(j, sb), v);
+					}
+					else
+					{
+						// |c| < q0 q1 / 2 < 2^59: the sum of four stays in 64 bits
+						int64_t v = load64(X, M, swz(j, sb)) + load64(X, M, swz(j + Dh, sb));
+						if (j < Dq) v += load64(X, M, swz(j + Dh + Dq, sb));
+						else v += load64(X, M, swz(j + Dq, sb)) + load64(X, M, swz(j + Dh, sb));
+						store64(X, M, swz(j, sb), v);
+					}
 				}
 				ncu = ncl / 2;
 				__syncthreads();
@@ -789,8 +835,10 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 		// normalize1: one thread per chunk
 		for (int c = tid; c < ncu; c += nt)
 		{
-			const int64_t f = narrow ? carry_chunk<int64_t>(X, M, c, a.csize, sb, mult, b, b_inv, b_s, err)
-			                         : carry_chunk<i128>(X, M, c, a.csize, sb, mult, b, b_inv, b_s, err);
+			int64_t f;
+			if constexpr (NP == 2) f = carry_chunk<int64_t>(X, M, c, a.csize, sb, mult, b, b_inv, b_s, err);
+			else f = narrow ? carry_chunk<int64_t>(X, M, c, a.csize, sb, mult, b, b_inv, b_s, err)
+			                : carry_chunk<i128>(X, M, c, a.csize, sb, mult, b, b_inv, b_s, err);
 			fch[c] = f;
 			if (c == ncu - 1) xch[0] = f;
 		}
@@ -878,14 +926,14 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel(const PrpKer
 //   local again; carry over the runs (run-end carries through DSMEM); cluster
 //   barrier; chunk carries.  Three cluster barriers and two transposes.
 // ---------------------------------------------------------------------------
-__host__ __device__ __forceinline__ size_t cols_words(int lm, int lg, int tw_smem)
+__host__ __device__ __forceinline__ size_t cols_words(int lm, int lg, int tw_smem, int np)
 {
 	const size_t M = (size_t)1 << lm, G = (size_t)1 << lg;
-	return 6 * M + M / 4 + 2 * G + 8 + (tw_smem ? 6 * M : 0);
+	return 2 * np * M + M / 4 + 2 * G + 8 + (tw_smem ? 2 * np * M : 0);
 }
 
-template <int LG, bool M12>
-__global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const PrpKernelArgs a)
+template <int LG, bool M12, int NP>
+__global__ void __launch_bounds__(M12 ? NP * 256 : NT_MAX, 1) prp_kernel_cols(const PrpKernelArgs a)
 {
 	constexpr int G = 1 << LG;
 	extern __shared__ __align__(16) uint32_t sm[];
@@ -899,30 +947,31 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 	const int ncl = G * runc;                                   // chunks held by this CTA
 	const int cb = g * MG;                                      // first column of this CTA
 
-	uint32_t *XC = sm;                                          // [3][G][MG] column runs
-	uint32_t *XR = sm + 3 * M;                                  // [3][M] row block g
-	int64_t *fch = reinterpret_cast<int64_t *>(sm + 6 * M);     // [M/8] chunk carries
+	uint32_t *XC = sm;                                          // [NP][G][MG] column runs
+	uint32_t *XR = sm + NP * M;                                 // [NP][M] row block g
+	int64_t *fch = reinterpret_cast<int64_t *>(sm + 2 * NP * M);   // [M/8] chunk carries
 	int64_t *xch = fch + M / 8;                                 // [G] run-end carries
-	uint32_t *TF = reinterpret_cast<uint32_t *>(xch + G) + 8;   // [3][M] roots of row block g
-	uint32_t *TI = TF + 3 * M;
+	uint32_t *TF = reinterpret_cast<uint32_t *>(xch + G) + 8;   // [NP][M] roots of row block g
+	uint32_t *TI = TF + NP * M;
 
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
 	const int b_s = (int)a.lane_b[4 * lane + 2];
-	const bool narrow = (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;   // launch-wide or per-lane 64-bit carries
+	// 64-bit carries: always with two primes, else launch-wide or per lane
+	const bool narrow = NP == 2 || (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;
 	uint32_t err = 0;
 
 	const uint32_t *tfg = a.tf + (size_t)g * 3 * M, *tig = a.ti + (size_t)g * 3 * M;
 	if (a.tw_smem)
 	{
-		for (int i = tid; i < 3 * M; i += nt) { TF[i] = tfg[i]; TI[i] = tig[i]; }
+		for (int i = tid; i < NP * M; i += nt) { TF[i] = tfg[i]; TI[i] = tig[i]; }
 	}
 	const uint32_t *TFl = a.tw_smem ? TF : tfg;
 	const uint32_t *TIl = a.tw_smem ? TI : tig;
-	uint32_t *SF = a.tw_smem ? TI + 3 * M : TF, *SI = SF + 3 * 256 * 2;   // Shoup roots of levels 0..7 (M12)
+	uint32_t *SF = a.tw_smem ? TI + NP * M : TF, *SI = SF + NP * 256 * 2;   // Shoup roots of levels 0..7 (M12)
 	if constexpr (M12)
 	{
 		const uint32_t *sfg = a.tfs + (size_t)g * 3 * 256 * 2, *sig = a.tis + (size_t)g * 3 * 256 * 2;
-		for (int i = tid; i < 3 * 256 * 2; i += nt) { SF[i] = sfg[i]; SI[i] = sig[i]; }
+		for (int i = tid; i < NP * 256 * 2; i += nt) { SF[i] = sfg[i]; SI[i] = sig[i]; }
 	}
 	uint32_t *scr = a.scratch ? a.scratch + ((size_t)lane * G + g) * 3 * M : nullptr;
 	const size_t lane_base = (size_t)lane * D;
@@ -942,23 +991,20 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 		__syncthreads();
 		// one (prime, column) item per thread: read the digits straight into the
 		// item's registers (no separate digit -> residue pass)
-		const bool fused = M12 && 3 * MG <= nt;
+		const bool fused = M12 && NP * MG <= nt;
 		if (!fused)
 		{
 			for (int e = tid; e < M; e += nt)
 			{
 				const int p = (e / MG) * MG + (swz(cb + e % MG, sb) - cb);
-				const int32_t d = (int32_t)XC[p];
-				XC[p] = modq_i32(d, Q0);
-				XC[M + p] = modq_i32(d, Q1);
-				XC[2 * M + p] = modq_i32(d, Q2);
+				to_residues<NP>(XC, M, p, (int32_t)XC[p]);
 			}
 			__syncthreads();
 		}
 		uint32_t vf[G];
 		if (fused)
 		{
-			if (tid < 3 * MG)
+			if (tid < NP * MG)
 			{
 				const int pi = tid / MG, tt = tid - pi * MG;
 				const uint32_t *S0 = XC + (swz(cb + tt, sb) - cb);
@@ -968,7 +1014,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 			__syncthreads();              // every digit read before any residue plane is written
 		}
 		// forward cross levels, one radix-G transform per (prime, column)
-		for (int it = tid; it < 3 * MG; it += nt)
+		for (int it = tid; it < NP * MG; it += nt)
 		{
 			const int pi = it / MG, tt = it - pi * MG;
 			const int p0 = swz(cb + tt, sb) - cb;
@@ -1000,7 +1046,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 		// row block g: XR[pi][c*MG + p] <- XC_c[pi][g*MG + p]
 		{
 			const int MG4 = MG >> 2;
-			for (int v = tid; v < 3 * G * MG4; v += nt)
+			for (int v = tid; v < NP * G * MG4; v += nt)
 			{
 				const int pc_ = v / MG4, o = (v - pc_ * MG4) * 4;
 				const int pi = pc_ / G, c = pc_ - pi * G;
@@ -1009,14 +1055,14 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 			}
 		}
 		__syncthreads();
-		if constexpr (M12) local_transform12(XR, TFl, TIl, SF, SI, mode, false, a, scr, scr, tid, nt);
-		else local_transform(XR, TFl, TIl, M, lm, mode, false, a, scr, scr, tid, nt);
+		if constexpr (M12) local_transform12<NP>(XR, TFl, TIl, SF, SI, mode, false, a, scr, scr, tid, nt);
+		else local_transform<NP>(XR, TFl, TIl, M, lm, mode, false, a, scr, scr, tid, nt);
 		if (mode == LM_FWD_ONLY) return;
 		cl.sync();
 		// columns back: XC[pi][h*MG + p] <- XR_h[pi][g*MG + p]
 		{
 			const int MG4 = MG >> 2;
-			for (int v = tid; v < 3 * G * MG4; v += nt)
+			for (int v = tid; v < NP * G * MG4; v += nt)
 			{
 				const int ph = v / MG4, o = (v - ph * MG4) * 4;
 				const int pi = ph / G, h = ph - pi * G;
@@ -1026,7 +1072,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 		}
 		__syncthreads();
 		// inverse cross levels
-		for (int it = tid; it < 3 * MG; it += nt)
+		for (int it = tid; it < NP * MG; it += nt)
 		{
 			const int pi = it / MG, tt = it - pi * MG;
 			const int p0 = swz(cb + tt, sb) - cb;
@@ -1056,14 +1102,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 		}
 		__syncthreads();
 		for (int e = tid; e < M; e += nt)
-		{
-			const int p = (e / MG) * MG + (swz(cb + e % MG, sb) - cb);
-			uint32_t w0, w1, w2;
-			garner3(XC[p], XC[M + p], XC[2 * M + p], a, narrow, w0, w1, w2);
-			XC[p] = w0;
-			XC[M + p] = w1;
-			XC[2 * M + p] = w2;
-		}
+			garner_at<NP>(XC, M, (e / MG) * MG + (swz(cb + e % MG, sb) - cb), a, narrow);
 		__syncthreads();
 		// N- (G >= 4, rows of M coefficients, Dn = G/2 rows): fold rows G/2..G-1
 		// into rows 0..G/2-1 of each column (all in this CTA):
@@ -1076,10 +1115,20 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 			{
 				const int h = it / MG, tt = it - h * MG;
 				const int p = swz(cb + tt, sb) - cb;
-				i128 v = load96(XC + h * MG, M, p) + load96(XC + (h + H2) * MG, M, p);
-				if (h < H4) v += load96(XC + (h + H2 + H4) * MG, M, p);
-				else v += load96(XC + (h + H4) * MG, M, p) + load96(XC + (h + H2) * MG, M, p);
-				store96(XC + h * MG, M, p, v);
+				if constexpr (NP == 3)
+				{
+					i128 v = load96(XC + h * MG, M, p) + load96(XC + (h + H2) * MG, M, p);
+					if (h < H4) v += load96(XC + (h + H2 + H4) * MG, M, p);
+					else v += load96(XC + (h + H4) * MG, M, p) + load96(XC + (h + H2) * MG, M, p);
+					store96(XC + h * MG, M, p, v);
+				}
+				else
+				{
+					int64_t v = load64(XC + h * MG, M, p) + load64(XC + (h + H2) * MG, M, p);
+					if (h < H4) v += load64(XC + (h + H2 + H4) * MG, M, p);
+					else v += load64(XC + (h + H4) * MG, M, p) + load64(XC + (h + H2) * MG, M, p);
+					store64(XC + h * MG, M, p, v);
+				}
 			}
 			ncu = H2 * runc;
 			__syncthreads();
@@ -1088,11 +1137,11 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 		for (int c = tid; c < ncu; c += nt)
 		{
 			const int h = c / runc, j = c - h * runc;
-			int64_t acc_f;
+			int64_t acc_f = 0;
 			{
 				uint32_t *Xh = XC + h * MG;
 				const int base = cb + j * csz;
-				if (narrow)
+				if (NP == 2 || narrow)
 				{
 					int64_t acc = 0;
 					auto step = [&](int i) {
@@ -1109,7 +1158,7 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 						for (int i = 0; i < csz; ++i) step(i);
 					acc_f = acc;
 				}
-				else
+				else if constexpr (NP == 3)
 				{
 					i128 acc = 0;
 					for (int i = 0; i < csz; ++i)
@@ -1200,36 +1249,36 @@ __global__ void __launch_bounds__(M12 ? 768 : NT_MAX, 1) prp_kernel_cols(const P
 	cl.sync();                    // peers may still read this CTA's carries
 }
 
-size_t prp_smem_bytes(int lm, int lg, int tw_smem)
+size_t prp_smem_bytes(int lm, int lg, int tw_smem, int np)
 {
-	if (lg > 0 && lm <= 13) return (cols_words(lm, lg, tw_smem) + prp_shoup_words(lm)) * 4;
+	if (lg > 0 && lm <= 13) return (cols_words(lm, lg, tw_smem, np) + prp_shoup_words(lm, np)) * 4;
 	const size_t M = size_t(1) << lm;
 	const int MG = (int)(M >> lg);
 	const int cap = lm <= 13 ? 256 : 128;
 	const int scols = MG < cap ? MG : cap;
-	size_t words = 3 * M + smem_stage_words(lm, lg, scols) + 8;
-	if (tw_smem) words += 6 * M;
-	return (words + prp_shoup_words(lm)) * 4;
+	size_t words = np * M + smem_stage_words(lm, lg, scols) + 8;
+	if (tw_smem) words += 2 * np * M;
+	return (words + prp_shoup_words(lm, np)) * 4;
 }
 
-int prp_threads(int lm)
+int prp_threads(int lm, int np)
 {
-	if (lm == 12) return 768;       // one thread per (prime, radix-16 group)
+	if (lm == 12) return np * 256;  // one thread per (prime, radix-16 group)
 	const int M = 1 << lm;
-	int nt = 3 * M / 16;
+	int nt = np * M / 16;
 	if (nt > NT_MAX) nt = NT_MAX;
 	if (nt < 64) nt = 64;
 	return (nt + 31) / 32 * 32;
 }
 
-template <int LG, bool M12, bool COLS>
+template <int LG, bool M12, bool COLS, int NP>
 static cudaError_t launch_lg(const PrpKernelArgs &a, int lanes, cudaStream_t stream)
 {
 	constexpr int G = 1 << LG;
 	void (*kern)(const PrpKernelArgs);
-	if constexpr (COLS) kern = prp_kernel_cols<LG, M12>;
-	else kern = prp_kernel<LG, M12>;
-	const size_t smem = prp_smem_bytes(a.lm, LG, a.tw_smem);
+	if constexpr (COLS) kern = prp_kernel_cols<LG, M12, NP>;
+	else kern = prp_kernel<LG, M12, NP>;
+	const size_t smem = prp_smem_bytes(a.lm, LG, a.tw_smem, NP);
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
 	if (G > 8)
@@ -1239,7 +1288,7 @@ static cudaError_t launch_lg(const PrpKernelArgs &a, int lanes, cudaStream_t str
 	}
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(lanes * G);
-	cfg.blockDim = dim3(prp_threads(a.lm));
+	cfg.blockDim = dim3(prp_threads(a.lm, NP));
 	cfg.dynamicSmemBytes = smem;
 	cfg.stream = stream;
 	cudaLaunchAttribute at[1];
@@ -1265,28 +1314,48 @@ bool prp_split_supported(int lm, int lg)
 	return lg == 4;
 }
 
+bool prp_two_prime_split(int lm, int lg)
+{
+	return prp_split_supported(lm, lg) && (lm == 12 || lg == 0);
+}
+
 cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t stream)
 {
 	if (!prp_split_supported(a.lm, lg)) return cudaErrorInvalidValue;
+	if (a.nprime == 2)
+	{
+		if (!prp_two_prime_split(a.lm, lg)) return cudaErrorInvalidValue;
+		PrpKernelArgs a2 = a;     // two planes of roots may fit where three do not
+		a2.tw_smem = prp_smem_bytes(a.lm, lg, 1, 2) <= 227 * 1024 ? 1 : 0;
+		if (a.lm != 12) return launch_lg<0, false, false, 2>(a2, lanes, stream);
+		switch (lg)
+		{
+		case 0: return launch_lg<0, true, false, 2>(a2, lanes, stream);
+		case 1: return launch_lg<1, true, true, 2>(a2, lanes, stream);
+		case 2: return launch_lg<2, true, true, 2>(a2, lanes, stream);
+		case 3: return launch_lg<3, true, true, 2>(a2, lanes, stream);
+		default: return launch_lg<4, true, true, 2>(a2, lanes, stream);
+		}
+	}
 	if (a.lm == 12)
 	{
 		switch (lg)
 		{
-		case 0: return launch_lg<0, true, false>(a, lanes, stream);
-		case 1: return launch_lg<1, true, true>(a, lanes, stream);
-		case 2: return launch_lg<2, true, true>(a, lanes, stream);
-		case 3: return launch_lg<3, true, true>(a, lanes, stream);
-		default: return launch_lg<4, true, true>(a, lanes, stream);
+		case 0: return launch_lg<0, true, false, 3>(a, lanes, stream);
+		case 1: return launch_lg<1, true, true, 3>(a, lanes, stream);
+		case 2: return launch_lg<2, true, true, 3>(a, lanes, stream);
+		case 3: return launch_lg<3, true, true, 3>(a, lanes, stream);
+		default: return launch_lg<4, true, true, 3>(a, lanes, stream);
 		}
 	}
-	if (lg == 0) return launch_lg<0, false, false>(a, lanes, stream);
-	if (a.lm == 14) return launch_lg<4, false, false>(a, lanes, stream);
+	if (lg == 0) return launch_lg<0, false, false, 3>(a, lanes, stream);
+	if (a.lm == 14) return launch_lg<4, false, false, 3>(a, lanes, stream);
 	switch (lg)
 	{
-	case 1: return launch_lg<1, false, true>(a, lanes, stream);
-	case 2: return launch_lg<2, false, true>(a, lanes, stream);
-	case 3: return launch_lg<3, false, true>(a, lanes, stream);
-	default: return launch_lg<4, false, true>(a, lanes, stream);
+	case 1: return launch_lg<1, false, true, 3>(a, lanes, stream);
+	case 2: return launch_lg<2, false, true, 3>(a, lanes, stream);
+	case 3: return launch_lg<3, false, true, 3>(a, lanes, stream);
+	default: return launch_lg<4, false, true, 3>(a, lanes, stream);
 	}
 }
 

@@ -3,6 +3,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "prp_arith.cuh"
+
 namespace ctw {
 
 constexpr int MAX_LG = 4;          // up to 16 CTAs (one thread-block cluster) per candidate
@@ -52,6 +54,7 @@ struct PrpKernelArgs {
 	int scols;                  // columns per staging round of the cross-CTA levels
 	int narrow;                 // 1: |coefficients| * 3 + carries < 2^62, carry in 64-bit arithmetic
 	int minus;                  // 1: arithmetic mod N- = b^Dn - b^{Dn/2} - 1 on the transform of degree 2 Dn
+	int nprime;                 // NTT primes: 3, or 2 when every product coefficient fits (prp_two_primes_exact)
 	uint32_t omega[3];          // 6th root w1 (Montgomery form)
 	uint32_t k1[3];             // S / (2 w1 - 1)
 	uint32_t sc[3];             // S = 2^32 * 2 / D   (Montgomery form)
@@ -70,12 +73,26 @@ enum PrpStatus : uint32_t {
 	ST_DIGIT_RANGE = 2,         // a digit left the int32 range
 };
 
-size_t prp_smem_bytes(int lm, int lg, int tw_smem);
+size_t prp_smem_bytes(int lm, int lg, int tw_smem, int np = 3);
 // Words of the Shoup root tables of one CTA (both directions), 0 unless M = 4096.
-inline size_t prp_shoup_words(int lm) { return lm == 12 ? 2 * 3 * 256 * 2 : 0; }
-int prp_threads(int lm);
+inline size_t prp_shoup_words(int lm, int np = 3) { return lm == 12 ? 2 * (size_t)np * 256 * 2 : 0; }
+int prp_threads(int lm, int np = 3);
 // Whether a cluster split D = 2^lg CTAs x 2^lm coefficients has a kernel.
 bool prp_split_supported(int lm, int lg);
+// Whether that split also has a two-prime kernel (one CTA, or 4096 coefficients per CTA).
+bool prp_two_prime_split(int lm, int lg);
+
+// Two primes carry the exact product when every coefficient stays inside
+// (-q0 q1 / 2, q0 q1 / 2), q0 q1 = 2^59.89.  Digits satisfy |d| <= b (the carry
+// leaves |d| < b, plus at most 1 in a chunk's last digit), and a coefficient
+// sums at most `terms` products of two digits: 1.5 D for N+ (X^D = X^{D/2} - 1
+// folds at most 1.5 D products into one coefficient) and Dn for the exact N-
+// product of degree < 2 Dn.  So two primes serve b when 2 terms (b + 1)^2 < q0 q1.
+inline bool prp_two_primes_exact(double terms, uint32_t bmax)
+{
+	const double bb = (double)bmax + 1.0;
+	return 2.0 * terms * bb * bb * (1.0 + 1e-12) < (double)Q0 * (double)Q1;
+}
 cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t stream);
 // Register moves of a pool tick (PrpLaneAux) for lanes of degree 2^ln; six
 // register planes `reg_stride` words apart.

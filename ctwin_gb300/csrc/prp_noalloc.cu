@@ -152,6 +152,7 @@ extern "C" int ctw_prp_mul_noalloc(int log2_degree, int lanes, const uint32_t *b
 	a.mult = 2;
 	a.tw_smem = prp_smem_bytes(proto.lm, lg, 1) <= 227 * 1024 ? 1 : 0;
 	a.narrow = (8.0 * (double)D * (double)bmax * (double)bmax < 4.611686018427388e18) ? 1 : 0;
+	a.nprime = (prp_two_prime_split(proto.lm, lg) && prp_two_primes_exact(1.5 * (double)D, bmax)) ? 2 : 3;
 	a.op = OP_MUL;
 	a.reg_in = x_dev;
 	a.reg_y = y_dev;

@@ -165,7 +165,7 @@ struct ctw_pool {
 	bool ev_pending[2] = { false, false };
 	long long ev_seq[2] = { -1, -1 };
 	long long seq_issued = 0, seq_complete = 0;
-	std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
+	std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;   // (buffer, ticks, lanes, primes)
 	std::vector<PoolSlot> slot;
 	std::vector<double> t_admit, t_submit;
 	std::vector<ctw_result> results;
@@ -177,6 +177,7 @@ struct ctw_pool {
 	int minus = 0;           // N- = b^Dn - b^{Dn/2} - 1 on the transform of degree D = 2 Dn
 	int ln_test = 0;         // log2 of the tested degree (ln, or ln - 1 for N-)
 	size_t Dn = 0;           // digits of the tested numbers
+	int prime_mode = 0;      // 0: two NTT primes whenever the launch's lanes allow it; 3: always three
 };
 
 namespace {
@@ -259,6 +260,7 @@ int pool_init(ctw_pool *p)
 	a.tw_smem = p->tw_smem;
 	a.narrow = 0;                 // per lane (lane_b[3])
 	a.minus = p->minus;
+	a.nprime = 3;                 // per launch (pool_primes)
 	a.scratch = p->d_scratch;
 	a.use_dupmask = 0;
 	POOL_CUDA(cudaDeviceSynchronize());
@@ -267,11 +269,22 @@ int pool_init(ctw_pool *p)
 
 int32_t *reg_plane(ctw_pool *p, int r) { return p->d_regs + (size_t)r * p->slots * p->D; }
 
+// NTT primes of a launch over lanes [0, lanes): two when the split has a
+// two-prime kernel and every lane's b keeps the product exact with two.
+int pool_primes(const ctw_pool *p, int lanes)
+{
+	if (p->prime_mode == 3 || !prp_two_prime_split(p->lm, p->lg)) return 3;
+	uint32_t bmax = 0;
+	for (int s = 0; s < lanes; ++s) bmax = std::max(bmax, p->h_laneb[4 * (size_t)s]);
+	const double terms = p->minus ? (double)p->Dn : 1.5 * (double)p->D;
+	return prp_two_primes_exact(terms, bmax) ? 2 : 3;
+}
+
 // The launches of T ticks from buffer k over `lanes` lanes: per tick the
 // moves before, the squarings (uniform launches of at most POOL_SQ_CHUNK),
 // the multiply d <- x * d, the moves after.  check != 0 synchronises after
 // each launch and names the first one that fails.
-cudaError_t issue_ticks(ctw_pool *p, int k, int T, int lanes, cudaStream_t cs, bool check, const char **what)
+cudaError_t issue_ticks(ctw_pool *p, int k, int T, int lanes, int np, cudaStream_t cs, bool check, const char **what)
 {
 	const size_t S = (size_t)p->slots;
 	const long long stride = (long long)S * (long long)p->D;
@@ -286,6 +299,7 @@ cudaError_t issue_ticks(ctw_pool *p, int k, int T, int lanes, cudaStream_t cs, b
 		e = prp_aux_launch(aux, p->d_regs, stride, p->ln, lanes, cs);
 		step("register moves");
 		PrpKernelArgs a = p->proto;
+		a.nprime = np;
 		a.op = OP_SQUARE;
 		a.reg_in = reg_plane(p, 0);
 		a.reg_out = reg_plane(p, 0);
@@ -324,9 +338,9 @@ cudaError_t upload(ctw_pool *p, int k, int T, cudaStream_t cs)
 	return cudaMemcpyAsync(p->d_stage[k], p->h_stage[k], (size_t)T * S * p->nws * 4, cudaMemcpyHostToDevice, cs);
 }
 
-int get_graph(ctw_pool *p, int k, int T, int lanes, cudaGraphExec_t &exec)
+int get_graph(ctw_pool *p, int k, int T, int lanes, int np, cudaGraphExec_t &exec)
 {
-	const auto key = std::make_tuple(k, T, lanes);
+	const auto key = std::make_tuple(k, T, lanes, np);
 	auto it = p->graphs.find(key);
 	if (it != p->graphs.end())
 	{
@@ -337,7 +351,7 @@ int get_graph(ctw_pool *p, int k, int T, int lanes, cudaGraphExec_t &exec)
 	POOL_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
 	const char *what = nullptr;
 	cudaError_t e = upload(p, k, T, cs);
-	if (e == cudaSuccess) e = issue_ticks(p, k, T, lanes, cs, false, &what);
+	if (e == cudaSuccess) e = issue_ticks(p, k, T, lanes, np, cs, false, &what);
 	cudaGraph_t graph = nullptr;
 	const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
 	if (e != cudaSuccess || e2 != cudaSuccess)
@@ -423,6 +437,13 @@ int finish_slot(ctw_pool *p, int s, bool status_bad)
 	p->results.push_back(r);
 	sl = PoolSlot{};
 	--p->active;
+	// the free slot computes on zeros with b = 2^16 + 1 (valid for every launch,
+	// two primes included) until its next admission
+	uint32_t *lb = p->h_laneb + 4 * (size_t)s;
+	lane_params(65537u, D, lb);
+	POOL_CUDA(cudaMemcpyAsync(p->d_laneb + 4 * (size_t)s, lb, 16, cudaMemcpyHostToDevice, p->stream));
+	POOL_CUDA(cudaMemsetAsync(reg_plane(p, 0) + (size_t)s * D, 0, D * 4, p->stream));
+	POOL_CUDA(cudaMemsetAsync(reg_plane(p, 1) + (size_t)s * D, 0, D * 4, p->stream));
 	return CTW_OK;
 }
 
@@ -616,6 +637,7 @@ int ctw_pool_run(ctw_pool *p, int ticks)
 			if (p->slot[(size_t)s].state != SLOT_FREE) hi = s + 1;
 		// launch over the lowest slots only, in steps of 8 lanes (one graph per step)
 		const int lanes = std::min(p->slots, std::max(8, (hi + 7) / 8 * 8));
+		const int np = pool_primes(p, lanes);
 		memset(p->h_aux[k], 0, (size_t)T * 2 * S * sizeof(PrpLaneAux));
 		memset(p->h_stage[k], 0, (size_t)T * S * p->nws * 4);
 		for (int t = 0; t < T; ++t)
@@ -638,13 +660,13 @@ int ctw_pool_run(ctw_pool *p, int ticks)
 			cudaError_t e = upload(p, k, T, p->stream);
 			if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
 			if (e != cudaSuccess) return fail(CTW_E_CUDA, "pool upload: %s", cudaGetErrorString(e));
-			e = issue_ticks(p, k, T, lanes, p->stream, true, &what);
+			e = issue_ticks(p, k, T, lanes, np, p->stream, true, &what);
 			if (e != cudaSuccess) return fail(CTW_E_CUDA, "pool %s launch: %s", what ? what : "?", cudaGetErrorString(e));
 		}
 		else
 		{
 			cudaGraphExec_t exec = nullptr;
-			if (int rc = get_graph(p, k, T, lanes, exec)) return rc;
+			if (int rc = get_graph(p, k, T, lanes, np, exec)) return rc;
 			POOL_CUDA(cudaGraphLaunch(exec, p->stream));
 		}
 		POOL_CUDA(cudaEventRecord(p->ev[k], p->stream));
@@ -698,6 +720,23 @@ int ctw_pool_info(ctw_pool *p, int *slots, int *active, int *in_flight, int *gl_
 	if (csize) *csize = p->csize;
 	if (squarings) *squarings = p->squarings;
 	return CTW_OK;
+}
+
+int ctw_pool_set_prime_count(ctw_pool *p, int count)
+{
+	if (!p) return fail(CTW_E_ARG, "null pool");
+	if (count != 0 && count != 3) return fail(CTW_E_ARG, "prime count %d not in {0 (automatic), 3}", count);
+	p->prime_mode = count;
+	return CTW_OK;
+}
+
+int ctw_pool_prime_count(ctw_pool *p)
+{
+	if (!p) return 0;
+	int hi = 0;
+	for (int s = 0; s < p->slots; ++s)
+		if (p->slot[(size_t)s].state != SLOT_FREE) hi = s + 1;
+	return pool_primes(p, std::min(p->slots, std::max(8, (hi + 7) / 8 * 8)));
 }
 
 int ctw_pool_read_slot(ctw_pool *p, int slot, int reg, int32_t *out)

@@ -129,6 +129,15 @@ class Pool:
         d["squarings"] = sq.value
         return d
 
+    def set_prime_count(self, count: int):
+        """0: two NTT primes for launches whose lanes allow it (default); 3: always three."""
+        check(lib().ctw_pool_set_prime_count(self._h, count))
+
+    @property
+    def prime_count(self) -> int:
+        """NTT primes of the next launch over the current slots (2 or 3)."""
+        return int(lib().ctw_pool_prime_count(self._h))
+
     def read_slot(self, slot: int, reg: int) -> np.ndarray:
         out = np.zeros(self.regD, dtype=np.int32)
         check(lib().ctw_pool_read_slot(self._h, slot, reg, ptr(out)))

@@ -18,12 +18,16 @@ from ._native import check, lib, ptr
 class PrpEngine:
     """Fermat-test engine for `lanes` candidates of degree D = 2^log2_degree."""
 
-    def __init__(self, log2_degree: int, lanes: int = 1, csize: int = 8, base: int = 2, minus: bool = False):
+    def __init__(self, log2_degree: int, lanes: int = 1, csize: int = 8, base: int = 2, minus: bool = False,
+                 log2_ctas: int = -1):
         """minus=True tests the twin partner N- = b^D - b^{D/2} - 1 (no reference
-        counterpart; its registers hold 2D words, its digits D)."""
+        counterpart; its registers hold 2D words, its digits D).  log2_ctas >= 0
+        picks the cluster split (2^log2_ctas CTAs per candidate) of an N+ engine."""
         h = ctypes.c_void_p()
         if minus:
             check(lib().ctw_prp_create_minus(log2_degree, lanes, ctypes.byref(h)))
+        elif log2_ctas >= 0:
+            check(lib().ctw_prp_create_split(log2_degree, lanes, log2_ctas, ctypes.byref(h)))
         else:
             check(lib().ctw_prp_create(log2_degree, lanes, ctypes.byref(h)))
         self._h = h
@@ -66,6 +70,15 @@ class PrpEngine:
         arr = np.ascontiguousarray(b, dtype=np.uint32)
         check(lib().ctw_prp_set_b(self._h, ptr(arr), arr.size))
         self.b = arr.copy()
+
+    def set_prime_count(self, count: int):
+        """0: two NTT primes whenever they keep the product exact (default); 3: always three."""
+        check(lib().ctw_prp_set_prime_count(self._h, count))
+
+    @property
+    def prime_count(self) -> int:
+        """NTT primes of the next launch (2 or 3)."""
+        return int(lib().ctw_prp_prime_count(self._h))
 
     # -- register operations (reference engine.h) --
     def set(self, a: int):

@@ -72,6 +72,18 @@ int ctw_prp_set_base(ctw_prp *h, uint32_t base);
 /* b of each lane, 64 <= b < 2^31; count == lanes.
  * Replaces transform::set_b / engine::writeMemory_b (cyclo/src/transform.h:472-486). */
 int ctw_prp_set_b(ctw_prp *h, const uint32_t *b, int count);
+/* NTT primes: 0 (default) uses two primes whenever every product coefficient
+ * of the current b fits in them (2 * terms * (b + 1)^2 < q0 q1 with terms =
+ * 1.5 D, or D for N-) and the split has a two-prime kernel (one CTA, or 4096
+ * coefficients per CTA); 3 always uses three.  Registers are the same either
+ * way: the products are exact integers.  No reference counterpart (the
+ * reference always uses three primes, cyclo/src/transform.h:26-28). */
+int ctw_prp_set_prime_count(ctw_prp *h, int count);
+/* Primes the next launch uses (2 or 3). */
+int ctw_prp_prime_count(ctw_prp *h);
+/* 1 when a test of degree 2^log2_degree (N- when minus != 0) and this b runs
+ * on two primes with the default split; host only, no device needed. */
+int ctw_prp_two_primes(int log2_degree, int minus, uint32_t b);
 
 /* Register 0 of every lane <- a.   Replaces engine::set (cyclo/src/engine.h:231-237). */
 int ctw_prp_set(ctw_prp *h, uint32_t a);
@@ -260,6 +272,11 @@ int ctw_pool_info(ctw_pool *p, int *slots, int *active, int *in_flight, int *gl_
 /* Copy register reg (0..5) of one slot to the host (after ctw_pool_collect
  * with wait); for tests. */
 int ctw_pool_read_slot(ctw_pool *p, int slot, int reg, int32_t *out);
+/* NTT primes of the pool's launches: 0 (default) picks two for a launch whose
+ * lanes all allow it (as ctw_prp_set_prime_count), 3 always three. */
+int ctw_pool_set_prime_count(ctw_pool *p, int count);
+/* Primes the next launch over the current slots would use (2 or 3). */
+int ctw_pool_prime_count(ctw_pool *p);
 void *ctw_pool_stream(ctw_pool *p);
 /* The tick program of one test, without a device: per tick 4 int32 words
  * {register moves before the squarings, moves after the multiply (PrpAuxOp

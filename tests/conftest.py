@@ -20,6 +20,15 @@ def golden_dir():
 
 
 @pytest.fixture(scope="session")
+def native_lib():
+    """The native library for host-only calls (no device needed); built if stale."""
+    from ctwin_gb300 import build as _build
+    _build.build()
+    from ctwin_gb300._native import lib
+    return lib()
+
+
+@pytest.fixture(scope="session")
 def native():
     """The native library; GPU tests require it to be built and a device present."""
     from ctwin_gb300 import build as _build  # noqa: F401

@@ -87,6 +87,10 @@ def pool_jobs():
         for b in (65537, 70001, 100003):
             jobs.append((b, ln, 2, False))
     jobs.append((65539, 12, 3, False))
+    # b on both sides of the two-prime bound 3 D (b + 1)^2 < q0 q1 at degrees 2^12 and 2^13
+    for ln, bs in ((12, (9000001, 9999991, 16777213)), (13, (6500003, 6700001))):
+        for b in bs:
+            jobs.append((b, ln, 2, False))
     # server mixes: seeded b in [2^16, 2^20) at degrees 2^9..2^11
     rng = random.Random(5)
     for ln in (9, 10, 11):
