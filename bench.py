@@ -18,8 +18,9 @@ work cyclo::check does between two checkpoints (cyclo/src/cyclo.h:277-308).
 
 Two more workloads print their own line (not the default):
   --workload batch  4096 candidates of degree 2^k, k uniform in {12..15}, b uniform in
-         [2^16, 2^22) seed 3, resident in four pools (one per degree, autotuned split and
-         CSIZE); one step = one tick of every pool (B squarings + the Gerbicz-Li multiply
+         [2^16, 2^22) seed 3, resident in one pool per degree and prime class (b within
+         the degree's two-prime bound or above it; autotuned split and CSIZE per pool);
+         one step = one tick of every pool (B squarings + the Gerbicz-Li multiply
          of every candidate), the pools' graphs running side by side on their streams;
          compared per degree with the plain one-candidate-per-launch-sequence path
   --workload sieve  sieved b/s of the GPU sieve on n = 20, b < 2^30, p < 2^40 (and the
@@ -76,7 +77,7 @@ def workload(rank: int):
     return b, E, i0, B_GL, words
 
 
-TRAFFIC_PER_LAUNCH = 2.18e6     # bytes of DRAM traffic of one 651-squaring launch, from ncu
+TRAFFIC_PER_LAUNCH = 1.5872e6   # ncu dram read+write bytes of one 651-squaring two-prime launch at 2^16
 
 
 def hbm_line(traffic: float, seconds: float) -> dict:
@@ -263,20 +264,27 @@ def plain_rate(ln: int, b: int, reps: int = 2):
 
 def run_batch(args):
     import torch
-    from ctwin_gb300 import Pool, autotune
+    from ctwin_gb300 import Pool, autotune, two_primes
     from ctwin_gb300._native import lib
     L = lib()
     rng = random.Random(3)
     N = args.candidates
     ks = [rng.choice((12, 13, 14, 15)) for _ in range(N)]
     bs = [rng.randrange(1 << 16, 1 << 22) for _ in range(N)]
-    groups = {k: [b for kk, b in zip(ks, bs) if kk == k] for k in (12, 13, 14, 15)}
+    # one pool per (degree, prime class): b within the degree's two-prime bound,
+    # or above it ("w": three primes)
+    cls = [(k, 2 if two_primes(k, b) else 3) for k, b in zip(ks, bs)]
+    groups = {}
+    for c, b in zip(cls, bs):
+        groups.setdefault(c, []).append(b)
+    groups = dict(sorted(groups.items()))
+    name = {c: f"{c[0]}" + ("" if c[1] == 2 else "w") for c in groups}
     pools, tune = {}, {}
     t0 = time.perf_counter()
-    for k, bl in groups.items():
-        lg, cs, us = autotune(k, len(bl))
-        tune[k] = {"log2_ctas": lg, "csize": cs, "us_per_squaring_lane": us}
-        pools[k] = Pool(k, len(bl), log2_ctas=lg, csize=cs)
+    for c, bl in groups.items():
+        lg, cs, us = autotune(c[0], len(bl), c[1])
+        tune[c] = {"log2_ctas": lg, "csize": cs, "us_per_squaring_lane": us, "ntt_primes": c[1]}
+        pools[c] = Pool(c[0], len(bl), log2_ctas=lg, csize=cs)
     t_tune = time.perf_counter() - t0
     t0 = time.perf_counter()
     for k, bl in groups.items():
@@ -310,7 +318,7 @@ def run_batch(args):
     for p in pools.values():
         p.collect(wait=True)
     times = []
-    launches_per_step = sum(3 + (info[k]["gl_block"] + 63) // 64 for k in pools)   # moves x2, multiply, squarings
+    launches_per_step = sum(3 + (info[c]["gl_block"] + 63) // 64 for c in pools)   # moves x2, multiply, squarings
     with ClockSampler(0) as clk:
         torch.cuda.synchronize()
         for _ in range(args.steps):
@@ -321,7 +329,7 @@ def run_batch(args):
     t_dev = sum(times)
     total_sq = sum(sq_per_step.values()) * args.steps
     value = total_sq / t_dev
-    imad = sum(sq_per_step[k] * imad_per_squaring(1 << k) for k in pools) * args.steps / t_dev
+    imad = sum(sq_per_step[c] * imad_per_squaring(1 << c[0], c[1]) for c in pools) * args.steps / t_dev
 
     # e2e through the public API: host planning + graph launch + collect per step (wall clock)
     torch.cuda.synchronize()
@@ -336,23 +344,23 @@ def run_batch(args):
 
     # per degree: the pool alone vs the plain path (one candidate per launch sequence)
     per_degree = {}
-    for k, p in pools.items():
-        st = streams[k]
+    for c, p in pools.items():
+        k = c[0]
+        st = streams[c]
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(st)
         p.run(1)
         e1.record(st)
         e1.synchronize()
-        alone = sq_per_step[k] / (e0.elapsed_time(e1) / 1000.0)
-        plain = plain_rate(k, groups[k][0])
-        per_degree[str(k)] = {"candidates": info[k]["slots"], "gl_block": info[k]["gl_block"], **tune[k],
-                              "batched_alone_sq_per_s": alone, "plain_sq_per_s": plain,
-                              "batched_over_plain": alone / plain,
-                              "tests_per_s_projected": alone / ((1 << k) *
-                                                                statistics.mean(math.log2(b) for b in groups[k])),
-                              "plain_tests_per_s_projected": plain / ((1 << k) *
-                                                                      statistics.mean(math.log2(b) for b in groups[k]))}
+        alone = sq_per_step[c] / (e0.elapsed_time(e1) / 1000.0)
+        plain = plain_rate(k, groups[c][0])
+        bits = (1 << k) * statistics.mean(math.log2(b) for b in groups[c])
+        per_degree[name[c]] = {"candidates": info[c]["slots"], "gl_block": info[c]["gl_block"], **tune[c],
+                               "b_range": [min(groups[c]), max(groups[c])],
+                               "batched_alone_sq_per_s": alone, "plain_sq_per_s": plain,
+                               "batched_over_plain": alone / plain,
+                               "tests_per_s_projected": alone / bits, "plain_tests_per_s_projected": plain / bits}
     for p in pools.values():
         p.close()
     clocks = clk.summary()
@@ -361,7 +369,8 @@ def run_batch(args):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": f"{N} candidates, degree 2^k with k uniform in {{12..15}}, b uniform in [2^16, 2^22) "
-                               "seed 3, one pool per degree, one step = one tick of every pool",
+                               "seed 3, one pool per degree and prime class (b within the two-prime bound, or "
+                               "above it: 'w'), one step = one tick of every pool",
                    "l2": "inputs larger than L2 (registers of all candidates resident)",
                    "setup_s": {"autotune": t_tune, "admit": t_admit}},
         "per_degree": per_degree,
@@ -387,25 +396,33 @@ def run_serve(args):
     # 64-slot pool tick (squarings, multiply, register moves, graph launch)
     from ctwin_gb300 import Pool
     import torch
-    us = {}
+    from ctwin_gb300 import two_primes
+    us, frac2 = {}, {}
     for k in degrees:
-        lg, cs, _ = autotune(k, 64)
-        with Pool(k, 64, log2_ctas=lg, csize=cs) as p:
-            p.admit_many([rng.randrange(1 << 16, 1 << 24) for _ in range(64)])
-            p.run(1)
-            p.collect(wait=True)
-            B = p.info()["gl_block"]
-            st = torch.cuda.ExternalStream(p.stream)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            p.run(2)
-            e1.record(st)
-            e1.synchronize()
-            us[k] = e0.elapsed_time(e1) * 1e3 / (2 * (B + 1) * 64)
+        # the server keeps b within the degree's two-prime bound and b above it in
+        # pools of their own: time a 64-slot pool of each class
+        lim = max(b for b in range(1 << 16, 1 << 24, 1 << 12) if two_primes(k, b))
+        frac2[k] = (lim - (1 << 16)) / ((1 << 24) - (1 << 16))
+        for primes, (b_lo, b_hi) in ((2, (1 << 16, lim)), (3, (lim + (1 << 12), 1 << 24))):
+            lg, cs, _ = autotune(k, 64, primes)
+            with Pool(k, 64, log2_ctas=lg, csize=cs) as p:
+                p.admit_many([rng.randrange(b_lo, b_hi) for _ in range(64)])
+                assert p.prime_count == primes
+                p.run(1)
+                p.collect(wait=True)
+                B = p.info()["gl_block"]
+                st = torch.cuda.ExternalStream(p.stream)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                p.run(2)
+                e1.record(st)
+                e1.synchronize()
+                us[(k, primes)] = e0.elapsed_time(e1) * 1e3 / (2 * (B + 1) * 64)
     mean_bits = {k: (1 << k) * statistics.mean(math.log2(rng.randrange(1 << 16, 1 << 24)) for _ in range(2000))
                  for k in degrees}
     w = {k: (math.log(k + 1) - math.log(k)) / (hi - lo) for k in degrees}
-    demand = sum(w[k] * mean_bits[k] * us[k] * 1e-6 for k in degrees)
+    demand = sum(w[k] * mean_bits[k] * 1e-6 * (frac2[k] * us[(k, 2)] + (1 - frac2[k]) * us[(k, 3)])
+                 for k in degrees)
     lam = args.load / demand
     n = args.requests or max(50, int(lam * args.serve_seconds))
     reqs, t = [], 0.0
@@ -464,7 +481,8 @@ def run_serve(args):
         "config": {"workload": f"{n} Poisson arrivals (seed 11, rate {lam:.2f}/s = {args.load:.0%} of the capacity "
                                "measured on 64-slot pool ticks), degree 2^k, k log-uniform in [12, 15), "
                                "b uniform in [2^16, 2^24)",
-                   "us_per_lane_squaring": us,
+                   "us_per_lane_squaring": {f"{k}" + ("" if c == 2 else "w"): v for (k, c), v in us.items()},
+                   "two_prime_fraction": {str(k): v for k, v in frac2.items()},
                    "hbm_budget_gib": args.hbm_budget, "ticks_per_launch": 1},
         "latency_s": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
                       "max": lat[-1]},

@@ -91,6 +91,7 @@ def lib() -> ctypes.CDLL:
             "ctw_context_decode": ([i32, i32, i32, vp, ctypes.c_size_t, vp, vp, vp, vp], i32),
             "ctw_cyclo_check_file": ([i32, ctypes.c_char_p, ctypes.c_char_p, i32, ctypes.c_double, vp, i32], i32),
             "ctw_prp_autotune": ([i32, i32, vp, vp, vp], i32),
+            "ctw_prp_autotune_primes": ([i32, i32, i32, vp, vp, vp], i32),
             "ctw_pool_create": ([i32, i32, i32, i32, u32, i32, ctypes.POINTER(H)], i32),
             "ctw_pool_destroy": ([H], i32),
             "ctw_pool_create_minus": ([i32, i32, i32, u32, i32, ctypes.POINTER(H)], i32),

@@ -784,19 +784,28 @@ int ctw_pool_schedule(int log2_degree, uint32_t b, int gl_block, int32_t *ticks_
 // ---------------------------------------------------------------------------
 int ctw_prp_autotune(int log2_degree, int lanes, int *log2_ctas, int *csize, double *us_per_squaring)
 {
+	return ctw_prp_autotune_primes(log2_degree, lanes, 2, log2_ctas, csize, us_per_squaring);
+}
+
+int ctw_prp_autotune_primes(int log2_degree, int lanes, int primes, int *log2_ctas, int *csize,
+                            double *us_per_squaring)
+{
 	static std::mutex mu;
-	static std::map<std::pair<int, int>, std::tuple<int, int, double>> cache;
+	static std::map<std::tuple<int, int, int>, std::tuple<int, int, double>> cache;
 	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
 	if (lanes < 1) return fail(CTW_E_ARG, "lanes must be >= 1");
+	if (primes != 2 && primes != 3) return fail(CTW_E_ARG, "primes %d not in {2, 3}", primes);
 	const int tl = std::min(lanes, 512);
 	std::lock_guard<std::mutex> lk(mu);
-	auto it = cache.find({ log2_degree, tl });
+	auto it = cache.find({ log2_degree, tl, primes });
 	if (it == cache.end())
 	{
 		int best_lg = prp_lg_for(log2_degree), best_cs = 8;
 		double best = 1e300;
+		// b < 2^20 keeps every degree <= 2^16 within the two-prime bound; primes = 3
+		// holds the engine to three
 		std::vector<uint32_t> bv((size_t)tl);
-		for (int l = 0; l < tl; ++l) bv[(size_t)l] = (1u << 20) + 7919u * (uint32_t)l;
+		for (int l = 0; l < tl; ++l) bv[(size_t)l] = (1u << 16) + 1009u * (uint32_t)l;
 		const int nw = 4;
 		std::vector<uint32_t> ew((size_t)tl * nw);
 		for (size_t i = 0; i < ew.size(); ++i) ew[i] = 0x9E3779B9u * (uint32_t)(i + 1);
@@ -809,6 +818,7 @@ int ctw_prp_autotune(int log2_degree, int lanes, int *log2_ctas, int *csize, dou
 			for (int cs = 8; cs <= 64; cs *= 2)
 			{
 				if (ctw_prp_set_csize(h, cs) != CTW_OK) continue;
+				if (ctw_prp_set_prime_count(h, primes == 3 ? 3 : 0) != CTW_OK) break;
 				if (ctw_prp_set_b(h, bv.data(), tl) != CTW_OK || ctw_prp_set(h, 3) != CTW_OK) break;
 				const int count = 8;
 				cudaStream_t st = (cudaStream_t)ctw_prp_stream(h);
@@ -833,7 +843,7 @@ int ctw_prp_autotune(int log2_degree, int lanes, int *log2_ctas, int *csize, dou
 			ctw_prp_destroy(h);
 		}
 		if (best >= 1e300) return fail(CTW_E_CUDA, "autotune: no configuration ran");
-		it = cache.emplace(std::make_pair(log2_degree, tl), std::make_tuple(best_lg, best_cs, best)).first;
+		it = cache.emplace(std::make_tuple(log2_degree, tl, primes), std::make_tuple(best_lg, best_cs, best)).first;
 	}
 	if (log2_ctas) *log2_ctas = std::get<0>(it->second);
 	if (csize) *csize = std::get<1>(it->second);

@@ -4,11 +4,14 @@
 // Threads: the caller submits requests; a preparation thread computes each
 // request's exponent and Gerbicz-Li block sum on the host; the worker thread
 // owns the CUDA work.  Each worker iteration admits prepared requests into
-// free slots of the pool of their degree (allocating a new pool only while
+// free slots of the pool of their class (allocating a new pool only while
 // the pools' bytes stay within the budget, and releasing idle pools when a
 // request is blocked by the budget), keeps at most two graph launches queued
 // per pool, and retires finished tests.  Pools run on their own streams, so
-// ticks of different degrees overlap on the device.
+// ticks of different degrees overlap on the device.  A class is a degree and,
+// where the degree has a two-prime kernel, whether b lies within the two-prime
+// bound: tests above it get pools of their own, so that they never hold the
+// others' launches at three primes.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -55,7 +58,7 @@ struct ctw_server {
 	std::deque<Request> incoming;
 	std::deque<Prepared> ready;
 	std::deque<ctw_result> done;
-	std::deque<std::pair<int, int>> prepare_req;   // (degree, slots) pools to create ahead
+	std::deque<std::pair<int, int>> prepare_req;   // (class, slots) pools to create ahead
 	bool stop = false;
 	std::string error;
 	long long submitted = 0, finished = 0, active = 0, pending = 0;
@@ -63,12 +66,20 @@ struct ctw_server {
 
 	std::thread prep, worker;
 	// worker-owned
-	std::map<int, std::vector<ctw_pool *>> pools;
-	std::map<int, std::pair<int, int>> split;      // degree -> (log2 CTAs, csize)
+	std::map<int, std::vector<ctw_pool *>> pools;   // class -> pools
+	std::map<int, std::pair<int, int>> split;      // class -> (log2 CTAs, csize)
 	std::vector<Prepared> waiting;
 };
 
 namespace {
+
+// Class key 2 ln + w: w = 1 for b above the two-prime bound of a degree that has
+// a two-prime kernel.
+int class_of(int ln, uint32_t b)
+{
+	const bool capable = ctw_prp_two_primes(ln, 0, 64) != 0;
+	return 2 * ln + ((capable && !ctw_prp_two_primes(ln, 0, b)) ? 1 : 0);
+}
 
 int pool_slots_for(ctw_server *s, int ln)
 {
@@ -77,30 +88,31 @@ int pool_slots_for(ctw_server *s, int ln)
 	return (int)std::min<size_t>((size_t)s->max_slots, cap);
 }
 
-// Split and carry chunk of a degree: tuned once on first use, else the defaults.
-std::pair<int, int> split_for(ctw_server *s, int ln, int slots)
+// Split and carry chunk of a class: tuned once on first use, else the defaults.
+std::pair<int, int> split_for(ctw_server *s, int cls, int slots)
 {
-	auto it = s->split.find(ln);
+	auto it = s->split.find(cls);
 	if (it != s->split.end()) return it->second;
+	const int ln = cls / 2;
 	int lg = prp_lg_for(ln), cs = 8;
 	if (s->autotune)
 	{
 		double us = 0;
 		int tlg = 0, tcs = 0;
-		if (ctw_prp_autotune(ln, slots, &tlg, &tcs, &us) == CTW_OK) { lg = tlg; cs = tcs; }
+		if (ctw_prp_autotune_primes(ln, slots, (cls & 1) ? 3 : 2, &tlg, &tcs, &us) == CTW_OK) { lg = tlg; cs = tcs; }
 	}
-	return s->split[ln] = std::make_pair(lg, cs);
+	return s->split[cls] = std::make_pair(lg, cs);
 }
 
-size_t new_pool_bytes(ctw_server *s, int ln, int slots)
+size_t new_pool_bytes(ctw_server *s, int cls, int slots)
 {
-	return pool_bytes_estimate(ln, split_for(s, ln, slots).first, slots, default_gl_block(ln));
+	return pool_bytes_estimate(cls / 2, split_for(s, cls, slots).first, slots, default_gl_block(cls / 2));
 }
 
-int new_pool(ctw_server *s, int ln, int slots, ctw_pool **out)
+int new_pool(ctw_server *s, int cls, int slots, ctw_pool **out)
 {
-	const std::pair<int, int> sp = split_for(s, ln, slots);
-	return ctw_pool_create(ln, slots, sp.first, sp.second, s->base, 0, out);
+	const std::pair<int, int> sp = split_for(s, cls, slots);
+	return ctw_pool_create(cls / 2, slots, sp.first, sp.second, s->base, 0, out);
 }
 
 void prep_loop(ctw_server *s)
@@ -165,7 +177,7 @@ void worker_loop(ctw_server *s)
 		{
 			if (!s->pools[pr.first].empty()) continue;
 			ctw_pool *p = nullptr;
-			const int slots = pr.second > 0 ? std::min(pr.second, s->max_slots) : pool_slots_for(s, pr.first);
+			const int slots = pr.second > 0 ? std::min(pr.second, s->max_slots) : pool_slots_for(s, pr.first / 2);
 			if (new_pool(s, pr.first, slots, &p) == CTW_OK)
 			{
 				s->pools[pr.first].push_back(p);
@@ -176,14 +188,15 @@ void worker_loop(ctw_server *s)
 				set_error(s, "prepare");
 		}
 
-		// admission, first come first served within each degree
+		// admission, first come first served within each class
 		long long admitted = 0;
 		bool blocked_by_budget = false;
 		std::vector<Prepared> still;
 		std::vector<ctw_result> out;
 		for (Prepared &w : s->waiting)
 		{
-			if (new_pool_bytes(s, w.r.ln, 1) > s->budget)
+			const int cls = class_of(w.r.ln, w.r.b);
+			if (new_pool_bytes(s, cls, 1) > s->budget)
 			{
 				// not even a one-slot pool fits: the request fails instead of waiting forever
 				ctw_result r{};
@@ -197,17 +210,17 @@ void worker_loop(ctw_server *s)
 				out.push_back(r);
 				continue;
 			}
-			auto &vec = s->pools[w.r.ln];
+			auto &vec = s->pools[cls];
 			ctw_pool *target = nullptr;
 			for (ctw_pool *p : vec)
 				if (pool_free_slots(p) > 0) { target = p; break; }
 			if (!target)
 			{
 				const int slots = pool_slots_for(s, w.r.ln);
-				if (s->bytes + new_pool_bytes(s, w.r.ln, slots) <= s->budget)
+				if (s->bytes + new_pool_bytes(s, cls, slots) <= s->budget)
 				{
 					ctw_pool *p = nullptr;
-					if (new_pool(s, w.r.ln, slots, &p) == CTW_OK)
+					if (new_pool(s, cls, slots, &p) == CTW_OK)
 					{
 						vec.push_back(p);
 						std::lock_guard<std::mutex> lk(s->mu);
@@ -345,7 +358,8 @@ int ctw_server_prepare(ctw_server *s, int log2_degree, int slots)
 	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
 	{
 		std::lock_guard<std::mutex> lk(s->mu);
-		s->prepare_req.emplace_back(log2_degree, slots);
+		s->prepare_req.emplace_back(2 * log2_degree, slots);
+		if (ctw_prp_two_primes(log2_degree, 0, 64)) s->prepare_req.emplace_back(2 * log2_degree + 1, slots);
 	}
 	s->cv_ready.notify_one();
 	return CTW_OK;

@@ -22,11 +22,18 @@ def result_dict(r: CtwResult) -> dict:
             "t_submit": r.t_submit, "t_admit": r.t_admit, "t_done": r.t_done, "squarings": int(r.squarings)}
 
 
-def autotune(log2_degree: int, lanes: int):
-    """(log2_ctas, csize, us_per_squaring) the device picks for `lanes` candidates of degree 2^log2_degree."""
+def autotune(log2_degree: int, lanes: int, primes: int = 2):
+    """(log2_ctas, csize, us_per_squaring) the device picks for `lanes` candidates of
+    degree 2^log2_degree whose b runs on `primes` NTT primes (2: within the bound)."""
     lg, cs, us = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
-    check(lib().ctw_prp_autotune(log2_degree, lanes, ctypes.byref(lg), ctypes.byref(cs), ctypes.byref(us)))
+    check(lib().ctw_prp_autotune_primes(log2_degree, lanes, primes, ctypes.byref(lg), ctypes.byref(cs),
+                                        ctypes.byref(us)))
     return lg.value, cs.value, us.value
+
+
+def two_primes(log2_degree: int, b: int, minus: bool = False) -> bool:
+    """Whether a test of this degree and b runs on two NTT primes (default split; host only)."""
+    return bool(lib().ctw_prp_two_primes(log2_degree, 1 if minus else 0, b))
 
 
 def schedule(log2_degree: int, b: int, gl_block: int = 0):
@@ -224,3 +231,44 @@ class Server:
             elif time.monotonic() - last > timeout_s:
                 raise CtwError(-2, f"server drain: {len(out)} of {count} results after {timeout_s} s without progress")
         return out
+
+
+def _main(argv=None) -> int:
+    """Tick throughput of one pool: python -m ctwin_gb300.pool <log2_degree> <slots>
+    [--ticks T] [--b-min B] [--b-max B] [--seed S] [--primes 0|3].  Admits `slots`
+    tests with seeded b in [b_min, b_max), runs T ticks and prints squarings/s
+    (wall clock, one line of JSON)."""
+    import argparse
+    import json
+    import random
+    import time
+    ap = argparse.ArgumentParser(prog="python -m ctwin_gb300.pool")
+    ap.add_argument("log2_degree", type=int)
+    ap.add_argument("slots", type=int)
+    ap.add_argument("--ticks", type=int, default=4)
+    ap.add_argument("--b-min", type=int, default=1 << 16)
+    ap.add_argument("--b-max", type=int, default=1 << 22)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--primes", type=int, default=0, choices=(0, 3))
+    a = ap.parse_args(argv)
+    rng = random.Random(a.seed)
+    bs = [rng.randrange(a.b_min, a.b_max) for _ in range(a.slots)]
+    with Pool(a.log2_degree, a.slots) as p:
+        p.set_prime_count(a.primes)
+        p.admit_many(bs)
+        p.run(1)
+        p.collect(wait=True)
+        t0 = time.perf_counter()
+        p.run(a.ticks)
+        p.collect(wait=True)
+        dt = time.perf_counter() - t0
+        info = p.info()
+        print(json.dumps({"log2_degree": a.log2_degree, "slots": a.slots, "ticks": a.ticks,
+                          "ntt_primes": p.prime_count, "log2_ctas": info["log2_ctas"], "csize": info["csize"],
+                          "squarings_per_s": a.slots * a.ticks * (info["gl_block"] + 1) / dt}))
+    return 0
+
+
+if __name__ == "__main__":
+    import sys
+    sys.exit(_main())

@@ -204,9 +204,14 @@ int ctw_prp_mul_noalloc(int log2_degree, int lanes, const uint32_t *b, const int
 /* Pick the cluster split and carry chunk of degree 2^log2_degree for `lanes`
  * resident candidates by timing every supported (split, csize) pair on the
  * device (the reference times its CSIZE candidates the same way,
- * cyclo/src/transform.h:383-419).  Results are cached per (degree, lanes) for
- * the life of the process.  Outputs may be NULL. */
+ * cyclo/src/transform.h:383-419) with b inside the two-prime bound.  Results
+ * are cached per (degree, lanes) for the life of the process.  Outputs may be NULL. */
 int ctw_prp_autotune(int log2_degree, int lanes, int *log2_ctas, int *csize, double *us_per_squaring);
+/* The same for tests on `primes` NTT primes: 2 (b within the two-prime bound,
+ * what ctw_prp_autotune tunes for) or 3 (b above it).  Cached per (degree,
+ * lanes, primes). */
+int ctw_prp_autotune_primes(int log2_degree, int lanes, int primes, int *log2_ctas, int *csize,
+                            double *us_per_squaring);
 
 /* ------------------------------------------------------------------------ */
 /* Pools: many resident tests of one degree, each at its own bit position.  */
@@ -293,15 +298,18 @@ int ctw_pool_schedule(int log2_degree, uint32_t b, int gl_block, int32_t *ticks_
 typedef struct ctw_server ctw_server;
 
 /* Start a server thread.  hbm_budget_bytes bounds the pools' device memory
- * (0: 80 % of the free memory); a request waits until its degree has a free
- * slot, and a new pool is allocated only while the budget allows.
+ * (0: 80 % of the free memory); a request waits until its class has a free
+ * slot, and a new pool is allocated only while the budget allows.  A class is
+ * a degree and whether b is within the degree's two-prime bound
+ * (ctw_prp_two_primes), so tests above the bound have pools of their own.
  * max_slots caps one pool; ticks_per_launch sets the graph length (1..8);
- * autotune != 0 picks split and csize per degree on first use. */
+ * autotune != 0 picks split and csize per class on first use. */
 int ctw_server_create(size_t hbm_budget_bytes, int max_slots, uint32_t base, int ticks_per_launch, int autotune,
                       ctw_server **out);
 /* Queue a test (thread-safe).  8 <= log2_degree <= 18. */
 int ctw_server_submit(ctw_server *s, int log2_degree, uint32_t b, uint64_t tag);
-/* Create (and tune) the pool of a degree ahead of its first request. */
+/* Create (and tune) the pools of a degree (one per prime class where the degree
+ * has a two-prime kernel) ahead of its first request. */
 int ctw_server_prepare(ctw_server *s, int log2_degree, int slots);
 /* Take up to max finished tests, waiting up to timeout_ms for the first. */
 int ctw_server_poll(ctw_server *s, ctw_result *out, int max, int timeout_ms);

@@ -150,3 +150,22 @@ def test_minus_two_primes_match_three(native):
         for a, c in zip(res[0], res[3]):
             assert list(a) == list(c)
         assert all(res[0][2])
+
+
+def test_server_separates_prime_classes(native):
+    """Degree-2^12 requests on both sides of the bound, interleaved: every result
+    equals GMP's; the server holds them in pools of their own class (b above
+    the bound never holds the others at three primes)."""
+    from ctwin_gb300 import Server, two_primes
+    g = gold()
+    bs = [65537, 9999991, 70001, 16777213, 100003, 9000001]
+    assert [two_primes(12, b) for b in bs] == [True, False, True, False, True, True]
+    with Server(hbm_budget_bytes=1 << 30, max_slots=8, ticks_per_launch=2) as s:
+        for i, b in enumerate(bs):
+            s.submit(12, b, tag=i)
+        res = s.drain(len(bs), timeout_s=300)
+    assert sorted(r["tag"] for r in res) == list(range(len(bs)))
+    for r in res:
+        want = g[(r["b"], 12, 2)]
+        assert r["status"] == 0 and r["gl_ok"], r
+        assert (r["is_prp"], r["res64"]) == (want["prp"], int(want["res64"], 16)), r
