@@ -189,7 +189,7 @@ def cpu_squarings_per_s(threads: int, seconds: float = 12.0):
     tabs.close()
     total = sum(per)
     return total / dt, {"value": total / dt, "unit": UNIT, "cores": threads, "kind": "port",
-                        "sample": f"{threads} candidates of degree 2^16 (b in [2^20,2^21)), "
+                        "sample": f"{threads} candidates of degree 2^{LOG2_D} (b in [2^20,2^21)), "
                                   f"{total} squarings in {dt:.1f} s with the oracle C restatement"}
 
 
@@ -210,7 +210,7 @@ def run_reference(args, rank, world):
             "warmup": args.warmup, "ms_per_step": 1000.0 * B_GL / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "single large PRP, degree 2^16, b in [2^20, 2^21), one candidate per core",
+            "config": {"workload": f"single large PRP, degree 2^{LOG2_D}, b in [2^20, 2^21), one candidate per core",
                        "degree": 1 << LOG2_D, "squarings_per_step": B_GL},
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -694,7 +694,11 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--load", type=float, default=0.8, help="serve: offered load / tuned capacity")
     ap.add_argument("--hbm-budget", type=int, default=64, help="serve: pool budget in GiB")
+    ap.add_argument("--log2-degree", type=int, default=16, choices=range(12, 19),
+                    help="single: degree of the candidate (2^16 is the headline configuration)")
     args = ap.parse_args()
+    global LOG2_D
+    LOG2_D = args.log2_degree
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -834,8 +838,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": "single large PRP, degree 2^16 (N = b^65536 - b^32768 + 1), b uniform in "
-                               "[2^20, 2^21) seed 1, one candidate per launch sequence",
+        "config": {"workload": f"single large PRP, degree 2^{LOG2_D} (N = b^{1 << LOG2_D} - b^{1 << (LOG2_D - 1)} + 1), "
+                               "b uniform in [2^20, 2^21) seed 1, one candidate per launch sequence",
                    "degree": D, "b": b, "exponent_bits": i0 + 1, "squarings_per_step": B_GL,
                    "step": "one Gerbicz-Li block: B_GL resident squarings + one multiply",
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}",
@@ -845,14 +849,14 @@ def main():
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": peak_imad / 1e12, "unit": "T IMAD/s",
                      "frac": achieved / peak_imad if peak_imad else None,
-                     "traffic": TRAFFIC_PER_LAUNCH,
+                     "traffic": TRAFFIC_PER_LAUNCH if LOG2_D == 16 else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 651-squaring launch "
                                        "(profiles/prp_kernel_d65536_full.md)",
                      "peak_source": "32-bit IMAD probe kernel run on this GPU in this process",
                      "sms_used": geo["ctas_per_lane"],
                      "frac_of_used_sms": (achieved / peak_imad) * 152 / geo["ctas_per_lane"] if peak_imad else None,
                      "kernel_ms": t_launch * 1000.0,
-                     "hbm": hbm_line(TRAFFIC_PER_LAUNCH, t_launch)},
+                     "hbm": hbm_line(TRAFFIC_PER_LAUNCH, t_launch) if LOG2_D == 16 else None},
         "cpu_baseline": cpu,
         "gpu_launches": int(launches),
         "clocks": clocks,

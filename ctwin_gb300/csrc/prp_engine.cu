@@ -178,6 +178,10 @@ struct ctw_prp {
 	uint32_t *d_exp = nullptr;        // resident exponent words [lanes][exp_nwords]
 	int exp_nwords = 0;
 	uint32_t *d_status = nullptr;
+	int grid = 0;                     // 1: grid kernel (2^lg CTAs of one cooperative launch per lane)
+	uint32_t *d_gx = nullptr, *d_gr = nullptr, *d_xr = nullptr;
+	long long *d_gc = nullptr;
+	unsigned *d_bar = nullptr;
 	std::vector<uint32_t> b;
 	PrpKernelArgs proto{};
 	long long launches = 0;
@@ -197,9 +201,14 @@ int check_handle(ctw_prp *h)
 int build_tables(ctw_prp *h)
 {
 	const size_t words = h->G * 3 * h->M, swords = h->G * 3 * 256 * 2;
-	std::vector<uint32_t> tf(words), ti(words), tfs(swords), tis(swords);
-	prp_build_tables(h->ln, h->lg, tf.data(), ti.data(), h->proto, tfs.data(), tis.data());
+	std::vector<uint32_t> tf(words), ti(words), tfs(swords), tis(swords), xr(3 * 2 * 64);
+	prp_build_tables(h->ln, h->lg, tf.data(), ti.data(), h->proto, tfs.data(), tis.data(), xr.data());
 	const size_t bytes = words * sizeof(uint32_t);
+	if (h->grid)
+	{
+		CTW_CUDA(cudaMalloc(&h->d_xr, xr.size() * 4));
+		CTW_CUDA(cudaMemcpy(h->d_xr, xr.data(), xr.size() * 4, cudaMemcpyHostToDevice));
+	}
 	CTW_CUDA(cudaMalloc(&h->d_tf, bytes));
 	CTW_CUDA(cudaMalloc(&h->d_ti, bytes));
 	CTW_CUDA(cudaMemcpy(h->d_tf, tf.data(), bytes, cudaMemcpyHostToDevice));
@@ -239,13 +248,25 @@ PrpKernelArgs make_args(ctw_prp *h)
 void choose_primes(ctw_prp *h)
 {
 	const double terms = h->minus ? (double)h->Dn : 1.5 * (double)h->D;
-	h->nprime = (h->prime_mode != 3 && h->bmax > 0 && prp_two_prime_split(h->lm, h->lg) &&
+	h->nprime = (h->prime_mode != 3 && h->bmax > 0 && (h->grid || prp_two_prime_split(h->lm, h->lg)) &&
 	             prp_two_primes_exact(terms, h->bmax)) ? 2 : 3;
 }
 
 int launch(ctw_prp *h, const PrpKernelArgs &a)
 {
-	const cudaError_t e = prp_launch(a, h->lg, h->lanes, h->stream);
+	cudaError_t e;
+	if (h->grid)
+	{
+		// barrier counters start at zero in every launch
+		e = cudaMemsetAsync(h->d_bar, 0, (size_t)h->lanes * 32 * sizeof(unsigned), h->stream);
+		if (e == cudaSuccess)
+		{
+			const PrpGridArgs ga{ h->d_gx, h->d_gr, h->d_gc, h->d_bar, h->d_xr };
+			e = prp_grid_launch(a, ga, h->lg, h->lanes, h->stream);
+		}
+	}
+	else
+		e = prp_launch(a, h->lg, h->lanes, h->stream);
 	if (e != cudaSuccess) return fail(CTW_E_CUDA, "PRP kernel launch: %s", cudaGetErrorString(e));
 	++h->launches;
 	return CTW_OK;
@@ -383,22 +404,47 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	*out = nullptr;
 	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
 	if (lanes < 1 || lanes > MAX_INLINE_LANES) return fail(CTW_E_ARG, "lanes %d outside [1, %d]", lanes, MAX_INLINE_LANES);
-	const int lg = log2_ctas < 0 ? prp_lg_for(log2_degree) : log2_ctas;
-	if (!prp_split_supported(log2_degree - lg, lg))
-		return fail(CTW_E_ARG, "no kernel for degree 2^%d on 2^%d CTAs", log2_degree, lg);
 	if (ctw_device_count() == 0) return fail(CTW_E_CUDA, "no CUDA device");
+	// Degrees 2^17 and 2^18 default to the grid kernel (2^(ln-12) CTAs of 4096
+	// coefficients per lane) when the lanes fit in one cooperative launch.
+	int lg = log2_ctas < 0 ? prp_lg_for(log2_degree) : log2_ctas;
+	bool grid = false;
+	if (log2_ctas < 0 && prp_grid_supported(log2_degree - 12) && lanes <= prp_grid_max_lanes(log2_degree - 12, 3))
+	{
+		lg = log2_degree - 12;
+		grid = true;
+	}
+	else if (log2_ctas >= 0 && prp_grid_supported(lg))
+	{
+		if (log2_degree - lg != 12) return fail(CTW_E_ARG, "no kernel for degree 2^%d on 2^%d CTAs", log2_degree, lg);
+		const int cap = prp_grid_max_lanes(lg, 3);
+		if (lanes > cap) return fail(CTW_E_ARG, "%d lanes of degree 2^%d exceed one grid launch (%d)", lanes, log2_degree, cap);
+		grid = true;
+	}
+	else if (!prp_split_supported(log2_degree - lg, lg))
+		return fail(CTW_E_ARG, "no kernel for degree 2^%d on 2^%d CTAs", log2_degree, lg);
 	ctw_prp *h = new ctw_prp();
 	h->ln = log2_degree;
 	h->lanes = lanes;
+	h->grid = grid ? 1 : 0;
 	h->lg = lg;
 	h->lm = log2_degree - h->lg;
 	h->D = (size_t)1 << log2_degree;
 	h->Dn = h->D;
 	h->G = (size_t)1 << h->lg;
 	h->M = h->D / h->G;
-	h->tw_smem = prp_smem_bytes(h->lm, h->lg, 1) <= 227 * 1024 ? 1 : 0;
-	h->smem = prp_smem_bytes(h->lm, h->lg, h->tw_smem);
-	h->threads = prp_threads(h->lm);
+	if (h->grid)
+	{
+		h->tw_smem = prp_grid_smem_bytes(h->lg, 1, 3) <= 227 * 1024 ? 1 : 0;
+		h->smem = prp_grid_smem_bytes(h->lg, h->tw_smem, 3);
+		h->threads = 3 * 256;
+	}
+	else
+	{
+		h->tw_smem = prp_smem_bytes(h->lm, h->lg, 1) <= 227 * 1024 ? 1 : 0;
+		h->smem = prp_smem_bytes(h->lm, h->lg, h->tw_smem);
+		h->threads = prp_threads(h->lm);
+	}
 	h->b.assign((size_t)lanes, 0);
 	int rc = CTW_OK;
 	auto cleanup = [&](int code) { ctw_prp_destroy(h); return code; };
@@ -411,6 +457,15 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	if (cudaMalloc(&h->d_laneb, (size_t)lanes * 4 * sizeof(uint32_t)) != cudaSuccess)
 		return cleanup(fail(CTW_E_NOMEM, "lane allocation"));
 	if (cudaMalloc(&h->d_status, sizeof(uint32_t)) != cudaSuccess) return cleanup(fail(CTW_E_NOMEM, "status"));
+	if (h->grid)
+	{
+		const size_t xw = (size_t)lanes * 3 * h->D;        // [lanes][G][3][M] words
+		if (cudaMalloc(&h->d_gx, xw * 4) != cudaSuccess || cudaMalloc(&h->d_gr, xw * 4) != cudaSuccess ||
+		    cudaMalloc(&h->d_gc, (size_t)lanes * h->G * h->G * sizeof(long long)) != cudaSuccess ||
+		    cudaMalloc(&h->d_bar, (size_t)lanes * 32 * sizeof(unsigned)) != cudaSuccess)
+			return cleanup(fail(CTW_E_NOMEM, "grid exchange buffers"));
+		cudaMemset(h->d_bar, 0, (size_t)lanes * 32 * sizeof(unsigned));
+	}
 	cudaMemset(h->d_regs, 0, rbytes);
 	cudaMemset(h->d_status, 0, sizeof(uint32_t));
 	cudaMemset(h->d_laneb, 0, (size_t)lanes * 4 * sizeof(uint32_t));
@@ -434,6 +489,11 @@ int ctw_prp_destroy(ctw_prp *h)
 	cudaFree(h->d_bits);
 	cudaFree(h->d_exp);
 	cudaFree(h->d_status);
+	cudaFree(h->d_gx);
+	cudaFree(h->d_gr);
+	cudaFree(h->d_gc);
+	cudaFree(h->d_bar);
+	cudaFree(h->d_xr);
 	if (h->stream) cudaStreamDestroy(h->stream);
 	delete h;
 	return CTW_OK;
@@ -492,7 +552,9 @@ int ctw_prp_two_primes(int log2_degree, int minus, uint32_t b)
 	const int ln = minus ? log2_degree + 1 : log2_degree;
 	const int lg = minus ? (ln <= 12 ? 0 : std::max(2, prp_lg_for(ln))) : prp_lg_for(ln);
 	const double Dn = (double)((size_t)1 << log2_degree);
-	return (prp_two_prime_split(ln - lg, lg) && prp_two_primes_exact(minus ? Dn : 1.5 * Dn, b)) ? 1 : 0;
+	// one N+ candidate of degree 2^17 or 2^18 runs on the grid kernel, which has both
+	const bool split = prp_two_prime_split(ln - lg, lg) || (!minus && prp_grid_supported(ln - 12));
+	return (split && prp_two_primes_exact(minus ? Dn : 1.5 * Dn, b)) ? 1 : 0;
 }
 
 int ctw_prp_set_prime_count(ctw_prp *h, int count)
@@ -772,8 +834,15 @@ int ctw_prp_geometry(ctw_prp *h, int *ctas, int *threads, int *smem)
 	if (int rc = check_handle(h)) return rc;
 	// the launch shape of the current prime count
 	const int np = h->nprime;
-	const int tw = np == 2 ? (prp_smem_bytes(h->lm, h->lg, 1, 2) <= 227 * 1024 ? 1 : 0) : h->tw_smem;
 	if (ctas) *ctas = (int)h->G;
+	if (h->grid)
+	{
+		const int tw = prp_grid_smem_bytes(h->lg, 1, np) <= 227 * 1024 ? 1 : 0;
+		if (threads) *threads = np * 256;
+		if (smem) *smem = (int)prp_grid_smem_bytes(h->lg, tw, np);
+		return CTW_OK;
+	}
+	const int tw = np == 2 ? (prp_smem_bytes(h->lm, h->lg, 1, 2) <= 227 * 1024 ? 1 : 0) : h->tw_smem;
 	if (threads) *threads = prp_threads(h->lm, np);
 	if (smem) *smem = (int)prp_smem_bytes(h->lm, h->lg, tw, np);
 	return CTW_OK;

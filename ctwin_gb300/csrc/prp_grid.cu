@@ -1,0 +1,429 @@
+// Grid kernel: one candidate of degree D = G * 4096 spread over G = 2^LG CTAs
+// of one cooperative launch (G = 32 for D = 2^17, 64 for D = 2^18), more SMs
+// than a thread-block cluster (at most 16) can give one candidate.
+//
+// The residue rests in shared memory in the column layout of the cluster
+// kernel: CTA g keeps, for every row block h < G, the run of coefficients
+// [h*4096 + g*MG, h*4096 + (g+1)*MG), MG = 4096/G.  Per squaring:
+//   digits -> residues; the LG cross levels of every column (radix-8/4 passes
+//   in shared memory); publish the columns to L2; grid barrier A; gather row
+//   block g (16-byte loads that bypass L1); the 4096-coefficient local
+//   transform, pointwise square and inverse; publish the row; grid barrier B;
+//   gather the columns; inverse cross levels; Garner; carry over the runs;
+//   publish the run-end carries; grid barrier C; chunk carries.
+// Registers after every squaring equal the cluster kernel's (and the
+// reference's) for the same CSIZE: the same transform, carry and wrap rules.
+//
+// Grid barriers are counters in global memory (zeroed by the host before each
+// launch).  The cooperative launch guarantees that all CTAs are resident; every
+// wait is still bounded by a %globaltimer budget, after which the CTA records
+// ST_GRID_WAIT and stops waiting, so a launch always ends.
+#include "prp_device.cuh"
+
+namespace ctw {
+
+namespace {
+
+constexpr unsigned long long GRID_WAIT_NS = 50ull * 1000 * 1000;   // 50 ms per barrier
+
+__device__ __forceinline__ unsigned long long grid_timer()
+{
+#if defined(CTW_EMU)
+	return emu_timer_ns();
+#elif defined(__CUDA_ARCH__)
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+#else
+	return 0;
+#endif
+}
+
+__device__ __forceinline__ unsigned grid_load_acquire(const unsigned *p)
+{
+#if defined(CTW_EMU)
+	return __atomic_load_n(p, __ATOMIC_ACQUIRE);
+#elif defined(__CUDA_ARCH__)
+	unsigned v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+#else
+	return *p;
+#endif
+}
+
+// 16-byte global load / store at L2 (not L1: another CTA rewrites these words
+// every squaring).
+__device__ __forceinline__ uint4 ld_l2(const uint32_t *p)
+{
+#if !defined(CTW_EMU)
+	return __ldcg(reinterpret_cast<const uint4 *>(p));
+#else
+	return *reinterpret_cast<const uint4 *>(p);
+#endif
+}
+__device__ __forceinline__ void st_l2(uint32_t *p, uint4 v)
+{
+#if !defined(CTW_EMU)
+	__stcg(reinterpret_cast<uint4 *>(p), v);
+#else
+	*reinterpret_cast<uint4 *>(p) = v;
+#endif
+}
+__device__ __forceinline__ long long ld_l2_ll(const long long *p)
+{
+#if !defined(CTW_EMU)
+	return __ldcg(p);
+#else
+	return *p;
+#endif
+}
+
+// Barrier k of the launch over the G CTAs of one lane: arrive, then wait until
+// k * G arrivals.  A CTA whose wait ran out (*dead) no longer waits.
+__device__ __forceinline__ void grid_sync(unsigned *cnt, unsigned target, uint32_t &err, int *dead)
+{
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		__threadfence();
+		atomicAdd(cnt, 1u);
+		if (!*dead)
+		{
+			const unsigned long long t0 = grid_timer();
+			while ((int)(grid_load_acquire(cnt) - target) < 0)
+				if (grid_timer() - t0 > GRID_WAIT_NS)
+				{
+					err |= ST_GRID_WAIT;
+					*dead = 1;
+					break;
+				}
+		}
+		__threadfence();
+	}
+	__syncthreads();
+}
+
+// Radix-R pass over cross levels [l0, l0 + log2 R) of the G-point transform of
+// every (prime, column) of this CTA; items (prime, group, column) with the
+// column fastest, so that a warp touches consecutive words of a row.  The
+// roots XRT[pi][dir][k] (Montgomery form) of level L, block j sit at k = 2^L + j.
+template <int LG, int R, int NP>
+__device__ __forceinline__ void cross_pass(uint32_t *XC, const uint32_t *XRT, int l0, int dir, int cb,
+                                           const PrpKernelArgs &a, int tid, int nt)
+{
+	constexpr int G = 1 << LG, MG = M12 >> LG, r = Log2<R>::v, NGR = G >> r;
+	const int lsh = LG - l0 - r, stride = 1 << lsh;
+	for (int it = tid; it < NP * NGR * MG; it += nt)
+	{
+		const int pi = it / (NGR * MG);
+		const int rem = it - pi * NGR * MG;
+		const int gam = rem / MG, tt = rem - gam * MG;
+		const int jblk = gam >> lsh, i = gam & (stride - 1);
+		const int hbase = (jblk << (LG - l0)) + i;
+		const uint32_t q = qv(pi), qi = qiv(pi);
+		uint32_t *S = XC + pi * M12 + (swz(cb + tt, 3) - cb);
+		const uint32_t *tw = XRT + (pi * 2 + dir) * G;
+		auto idx = [&](int t, int kk) { return (1 << (l0 + t)) + (jblk << t) + kk; };
+		uint32_t u[R];
+#pragma unroll
+		for (int k = 0; k < R; ++k) u[k] = S[(hbase + k * stride) * MG];
+		if (dir == 0) group_fwd<R>(u, tw, idx, q, qi, l0 == 0, a.omega[pi]);
+		else group_inv<R>(u, tw, idx, q, qi, l0 == 0, a.omega[pi], a.k1[pi], a.sc[pi]);
+#pragma unroll
+		for (int k = 0; k < R; ++k) S[(hbase + k * stride) * MG] = u[k];
+	}
+}
+
+// The LG cross levels as passes of at most 3 levels, larger first.
+template <int LG, int NP>
+__device__ __forceinline__ void cross_all(uint32_t *XC, const uint32_t *XRT, int dir, int cb, const PrpKernelArgs &a,
+                                          int tid, int nt)
+{
+	constexpr int R0 = LG == 1 ? 2 : LG == 2 ? 4 : LG == 4 ? 4 : 8;   // first pass: levels [0, log2 R0)
+	constexpr int L0 = Log2<R0>::v, L1 = LG - L0;                     // second pass: levels [L0, LG)
+	constexpr int R1 = L1 == 3 ? 8 : L1 == 2 ? 4 : 2;
+	if (dir == 0)
+	{
+		cross_pass<LG, R0, NP>(XC, XRT, 0, 0, cb, a, tid, nt);
+		__syncthreads();
+		if constexpr (L1 > 0)
+		{
+			cross_pass<LG, R1, NP>(XC, XRT, L0, 0, cb, a, tid, nt);
+			__syncthreads();
+		}
+	}
+	else
+	{
+		if constexpr (L1 > 0)
+		{
+			cross_pass<LG, R1, NP>(XC, XRT, L0, 1, cb, a, tid, nt);
+			__syncthreads();
+		}
+		cross_pass<LG, R0, NP>(XC, XRT, 0, 1, cb, a, tid, nt);
+		__syncthreads();
+	}
+}
+
+}  // namespace
+
+__host__ __device__ __forceinline__ size_t grid_words(int lg, int tw_smem, int np)
+{
+	const size_t M = M12, G = (size_t)1 << lg;
+	return 2 * np * M + M / 4 + 2 * G + 2 * np * G + (tw_smem ? 2 * np * M : 0) + 2 * (size_t)np * 512;
+}
+
+template <int LG, int NP>
+__global__ void __launch_bounds__(NP * 256, 1) prp_kernel_grid(const PrpKernelArgs a, const PrpGridArgs ga)
+{
+	static_assert(LG >= 1 && LG <= 6, "2..64 CTAs per candidate");
+	constexpr int G = 1 << LG, M = M12, MG = M >> LG, D = M * G, sb = 3;
+	extern __shared__ __align__(16) uint32_t sm[];
+	__shared__ int dead;
+	const int tid = threadIdx.x, nt = blockDim.x;
+	const int lane = blockIdx.x / G, g = blockIdx.x % G;
+	const int csz = a.csize, runc = MG / csz, ncl = G * runc, cb = g * MG;
+
+	uint32_t *XC = sm;                                          // [NP][G][MG] column runs
+	uint32_t *XR = sm + NP * M;                                 // [NP][M] row block g
+	int64_t *fch = reinterpret_cast<int64_t *>(sm + 2 * NP * M);   // [M/8] chunk carries
+	int64_t *xch = fch + M / 8;                                 // [G] run-end carries
+	uint32_t *XRT = reinterpret_cast<uint32_t *>(xch + G);      // [NP][2][G] cross-level roots
+	uint32_t *TF = XRT + NP * 2 * G;                            // [NP][M] roots of row block g
+	uint32_t *TI = TF + NP * M;
+	if (tid == 0) dead = 0;
+
+	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
+	const int b_s = (int)a.lane_b[4 * lane + 2];
+	const bool narrow = NP == 2 || (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;
+	uint32_t err = 0;
+
+	const uint32_t *tfg = a.tf + (size_t)g * 3 * M, *tig = a.ti + (size_t)g * 3 * M;
+	if (a.tw_smem)
+	{
+		for (int i = tid; i < NP * M; i += nt) { TF[i] = tfg[i]; TI[i] = tig[i]; }
+	}
+	const uint32_t *TFl = a.tw_smem ? TF : tfg;
+	const uint32_t *TIl = a.tw_smem ? TI : tig;
+	uint32_t *SF = a.tw_smem ? TI + NP * M : TF, *SI = SF + NP * 256 * 2;   // Shoup roots of levels 0..7
+	{
+		const uint32_t *sfg = a.tfs + (size_t)g * 3 * 256 * 2, *sig = a.tis + (size_t)g * 3 * 256 * 2;
+		for (int i = tid; i < NP * 256 * 2; i += nt) { SF[i] = sfg[i]; SI[i] = sig[i]; }
+	}
+	for (int i = tid; i < NP * 2 * G; i += nt) XRT[i] = ga.xr[(i / G) * 64 + i % G];
+
+	uint32_t *gx = ga.gx + (size_t)lane * G * 3 * M;             // [G][3][M]: CTA c's column planes at c*3M
+	uint32_t *gr = ga.gr + (size_t)lane * G * 3 * M;             // [G][3][M]: CTA h's row planes at h*3M
+	long long *gc = ga.gc + (size_t)lane * G * G;                // [G][G]: run-end carries of CTA c at c*G
+	unsigned *bar = ga.bar + (size_t)lane * 32;
+	unsigned nbar = 0;
+	auto gsync = [&]() {
+		++nbar;
+		grid_sync(bar, nbar * (unsigned)G, err, &dead);
+	};
+	uint32_t *scr = a.scratch ? a.scratch + ((size_t)lane * G + g) * 3 * M : nullptr;
+	const size_t lane_base = (size_t)lane * D;
+	constexpr int MG4 = MG / 4, M4 = M / 4;
+
+	auto pc = [&](int h, int tt) { return h * MG + (swz(cb + tt, sb) - cb); };
+	auto load_digits = [&](const int32_t *src) {
+		for (int e = tid; e < M; e += nt)
+		{
+			const int h = e / MG, tt = e - h * MG;
+			XC[pc(h, tt)] = (uint32_t)src[lane_base + (size_t)h * M + cb + tt];
+		}
+	};
+
+	auto transform_and_normalize = [&](int mode, int mult) {
+		__syncthreads();
+		for (int e = tid; e < M; e += nt)
+		{
+			const int p = (e / MG) * MG + (swz(cb + e % MG, sb) - cb);
+			to_residues<NP>(XC, M, p, (int32_t)XC[p]);
+		}
+		__syncthreads();
+		cross_all<LG, NP>(XC, XRT, 0, cb, a, tid, nt);
+		// publish the columns, gather row block g
+		for (int v = tid; v < NP * M4; v += nt)
+			st_l2(gx + (size_t)g * 3 * M + 4 * v, *reinterpret_cast<const uint4 *>(XC + 4 * v));
+		gsync();
+		for (int v = tid; v < NP * G * MG4; v += nt)
+		{
+			const int pcx = v / MG4, o = (v - pcx * MG4) * 4;
+			const int pi = pcx / G, c = pcx - pi * G;
+			*reinterpret_cast<uint4 *>(XR + pi * M + c * MG + o) = ld_l2(gx + (size_t)c * 3 * M + pi * M + g * MG + o);
+		}
+		__syncthreads();
+		local_transform12<NP>(XR, TFl, TIl, SF, SI, mode, false, a, scr, scr, tid, nt);
+		if (mode == LM_FWD_ONLY) return;
+		// publish the row, gather the columns
+		for (int v = tid; v < NP * M4; v += nt)
+			st_l2(gr + (size_t)g * 3 * M + 4 * v, *reinterpret_cast<const uint4 *>(XR + 4 * v));
+		gsync();
+		for (int v = tid; v < NP * G * MG4; v += nt)
+		{
+			const int ph = v / MG4, o = (v - ph * MG4) * 4;
+			const int pi = ph / G, h = ph - pi * G;
+			*reinterpret_cast<uint4 *>(XC + pi * M + h * MG + o) = ld_l2(gr + (size_t)h * 3 * M + pi * M + g * MG + o);
+		}
+		__syncthreads();
+		cross_all<LG, NP>(XC, XRT, 1, cb, a, tid, nt);
+		for (int e = tid; e < M; e += nt) garner_at<NP>(XC, M, (e / MG) * MG + (swz(cb + e % MG, sb) - cb), a, narrow);
+		__syncthreads();
+		// normalize1 over the runs; the last chunk of run h publishes its carry
+		for (int c = tid; c < ncl; c += nt)
+		{
+			const int h = c / runc, j = c - h * runc;
+			uint32_t *Xh = XC + h * MG;
+			const int base = cb + j * csz;
+			int64_t acc_f = 0;
+			if (narrow)
+			{
+				int64_t acc = 0;
+				for (int i = 0; i < csz; ++i)
+				{
+					const int p = swz(base + i, sb) - cb;
+					acc += load64(Xh, M, p) * (int64_t)mult;
+					Xh[p] = (uint32_t)reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+				}
+				acc_f = acc;
+			}
+			else if constexpr (NP == 3)
+			{
+				i128 acc = 0;
+				for (int i = 0; i < csz; ++i)
+				{
+					const int p = swz(base + i, sb) - cb;
+					acc += load96(Xh, M, p) * (i128)mult;
+					Xh[p] = (uint32_t)reduce_b<i128>(acc, b, b_inv, b_s, err);
+				}
+				acc_f = (int64_t)acc;
+				if ((i128)acc_f != acc) err |= ST_DIGIT_RANGE;
+			}
+			fch[c] = acc_f;
+			if (j == runc - 1) xch[h] = acc_f;
+		}
+		__syncthreads();
+		for (int h = tid; h < G; h += nt) gc[(size_t)g * G + h] = xch[h];
+		gsync();
+		// normalize2: chunk j of run (h, g) takes the carry of the chunk before it
+		// in natural order; -f of the last chunk goes to coefficient 0, +f to D/2
+		for (int c = tid; c < ncl; c += nt)
+		{
+			const int h = c / runc, j = c - h * runc;
+			int64_t acc;          // a chunk carry plus digits: 64-bit arithmetic is exact
+			if (j > 0) acc = fch[c - 1];
+			else if (g > 0) acc = ld_l2_ll(gc + (size_t)(g - 1) * G + h);
+			else
+			{
+				const int64_t last = ld_l2_ll(gc + (size_t)(G - 1) * G + (G - 1));
+				if (h == 0) acc = -last;
+				else
+				{
+					acc = ld_l2_ll(gc + (size_t)(G - 1) * G + (h - 1));
+					if (h == G / 2) acc += last;
+				}
+			}
+			uint32_t *Xh = XC + h * MG;
+			const int base = cb + j * csz;
+			int i = 0;
+			bool done = false;
+			for (; i < csz - 1; ++i)
+			{
+				const int p = swz(base + i, sb) - cb;
+				acc += (int32_t)Xh[p];
+				Xh[p] = (uint32_t)reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+				if (acc == 0) { done = true; break; }
+			}
+			if (!done)
+			{
+				const int p = swz(base + csz - 1, sb) - cb;
+				const int64_t s = (int64_t)(int32_t)Xh[p] + (int64_t)(int32_t)(int64_t)acc;
+				if (s != (int32_t)s) err |= ST_DIGIT_RANGE;
+				Xh[p] = (uint32_t)(int32_t)s;
+			}
+		}
+		__syncthreads();
+	};
+
+	if (a.op == OP_MUL)
+	{
+		load_digits(a.reg_y);
+		transform_and_normalize(LM_FWD_ONLY, 1);
+		gsync();              // every CTA has gathered y's row block before the columns are rewritten
+		load_digits(a.reg_in);
+		transform_and_normalize(LM_MUL, 1);
+	}
+	else
+	{
+		load_digits(a.reg_in);
+		for (int it = 0; it < a.count; ++it)
+		{
+			const long long i = a.i_hi - it;
+			int bit = 0;
+			if (a.use_dupmask) bit = (int)((a.dupmask[lane >> 6] >> (lane & 63)) & 1);
+			else if (i >= 0 && (i >> 5) < a.nwords) bit = (a.bits[(size_t)lane * a.nwords + (i >> 5)] >> (i & 31)) & 1;
+			transform_and_normalize(LM_SQUARE, bit ? a.mult : 1);
+		}
+	}
+	__syncthreads();
+	for (int e = tid; e < M; e += nt)
+	{
+		const int h = e / MG, tt = e - h * MG;
+		a.reg_out[lane_base + (size_t)h * M + cb + tt] = (int32_t)XC[pc(h, tt)];
+	}
+	if (err) atomicOr(a.status, err);
+}
+
+size_t prp_grid_smem_bytes(int lg, int tw_smem, int np) { return grid_words(lg, tw_smem, np) * 4; }
+
+template <int LG, int NP>
+static cudaError_t grid_launch_t(const PrpKernelArgs &a, const PrpGridArgs &ga, int lanes, cudaStream_t stream)
+{
+	void (*kern)(const PrpKernelArgs, const PrpGridArgs) = prp_kernel_grid<LG, NP>;
+	PrpKernelArgs a2 = a;
+	a2.tw_smem = prp_grid_smem_bytes(LG, 1, NP) <= 227 * 1024 ? 1 : 0;
+	const size_t smem = prp_grid_smem_bytes(LG, a2.tw_smem, NP);
+	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess) return e;
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(lanes << LG);
+	cfg.blockDim = dim3(NP * 256);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = stream;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeCooperative;   // all CTAs resident: the grid barriers can complete
+	at[0].val.cooperative = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, kern, a2, ga);
+}
+
+cudaError_t prp_grid_launch(const PrpKernelArgs &a, const PrpGridArgs &ga, int lg, int lanes, cudaStream_t stream)
+{
+	if (a.lm != 12 || !prp_grid_supported(lg)) return cudaErrorInvalidValue;
+	if (a.csize > (M12 >> lg)) return cudaErrorInvalidValue;
+	const bool two = a.nprime == 2;
+	switch (lg)
+	{
+	case 5: return two ? grid_launch_t<5, 2>(a, ga, lanes, stream) : grid_launch_t<5, 3>(a, ga, lanes, stream);
+	default: return two ? grid_launch_t<6, 2>(a, ga, lanes, stream) : grid_launch_t<6, 3>(a, ga, lanes, stream);
+	}
+}
+
+int prp_grid_max_lanes(int lg, int np)
+{
+	void (*kern)(const PrpKernelArgs, const PrpGridArgs) =
+	    np == 2 ? (lg == 5 ? prp_kernel_grid<5, 2> : prp_kernel_grid<6, 2>)
+	            : (lg == 5 ? prp_kernel_grid<5, 3> : prp_kernel_grid<6, 3>);
+	const int tw = prp_grid_smem_bytes(lg, 1, np) <= 227 * 1024 ? 1 : 0;
+	const size_t smem = prp_grid_smem_bytes(lg, tw, np);
+	if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+	int per_sm = 0, dev = 0, sms = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, np * 256, smem) != cudaSuccess) return 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	return (per_sm * sms) >> lg;
+}
+
+}  // namespace ctw

@@ -71,7 +71,25 @@ enum PrpStatus : uint32_t {
 	ST_OK = 0,
 	ST_BARRETT_RANGE = 1,       // quotient outside the two-step Barrett range
 	ST_DIGIT_RANGE = 2,         // a digit left the int32 range
+	ST_GRID_WAIT = 4,           // a grid barrier wait ran out (the launch's results are void)
 };
+
+// Buffers of the grid kernel (prp_grid.cu): one candidate on G = 2^lg CTAs of a
+// cooperative launch, transposes and run-end carries through L2.
+struct PrpGridArgs {
+	uint32_t *gx;               // [lanes][G][3][M] published column planes
+	uint32_t *gr;               // [lanes][G][3][M] published row planes
+	long long *gc;              // [lanes][G][G] run-end carries
+	unsigned *bar;              // [lanes][32] barrier counters (word 0 used), zero at launch
+	const uint32_t *xr;         // [3][2][64] cross-level roots (Montgomery): forward, inverse
+};
+constexpr int GRID_MIN_LG = 5, GRID_MAX_LG = 6;
+// Grid splits with a kernel: 2^lg CTAs of 4096 coefficients, lg = 5, 6 (D = 2^17, 2^18).
+inline bool prp_grid_supported(int lg) { return lg >= GRID_MIN_LG && lg <= GRID_MAX_LG; }
+size_t prp_grid_smem_bytes(int lg, int tw_smem, int np);
+cudaError_t prp_grid_launch(const PrpKernelArgs &a, const PrpGridArgs &ga, int lg, int lanes, cudaStream_t stream);
+// Lanes of degree 2^(12 + lg) one cooperative grid launch can hold on this device.
+int prp_grid_max_lanes(int lg, int np);
 
 size_t prp_smem_bytes(int lm, int lg, int tw_smem, int np = 3);
 // Words of the Shoup root tables of one CTA (both directions), 0 unless M = 4096.

@@ -77,8 +77,9 @@ namespace {
 // a two-prime kernel.
 int class_of(int ln, uint32_t b)
 {
-	const bool capable = ctw_prp_two_primes(ln, 0, 64) != 0;
-	return 2 * ln + ((capable && !ctw_prp_two_primes(ln, 0, b)) ? 1 : 0);
+	const int lg = prp_lg_for(ln);        // the pools' default split
+	const bool capable = prp_two_prime_split(ln - lg, lg);
+	return 2 * ln + ((capable && !prp_two_primes_exact(1.5 * (double)((size_t)1 << ln), b)) ? 1 : 0);
 }
 
 int pool_slots_for(ctw_server *s, int ln)
@@ -359,7 +360,8 @@ int ctw_server_prepare(ctw_server *s, int log2_degree, int slots)
 	{
 		std::lock_guard<std::mutex> lk(s->mu);
 		s->prepare_req.emplace_back(2 * log2_degree, slots);
-		if (ctw_prp_two_primes(log2_degree, 0, 64)) s->prepare_req.emplace_back(2 * log2_degree + 1, slots);
+		if (prp_two_prime_split(log2_degree - prp_lg_for(log2_degree), prp_lg_for(log2_degree)))
+			s->prepare_req.emplace_back(2 * log2_degree + 1, slots);
 	}
 	s->cv_ready.notify_one();
 	return CTW_OK;

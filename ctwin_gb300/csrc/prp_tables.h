@@ -65,8 +65,10 @@ inline int prp_stage_cols(int lm, int lg)
 // tfs/tis (lm == 12 only, else may be null): [G][3][256][2] Shoup pairs
 // (w, floor(w 2^32 / q)) of the plain roots at indices 1..255 (local levels 0..7).
 // lg is the cluster split (2^lg CTAs per candidate; prp_lg_for(ln) by default).
+// xr (optional, [3][2][64] words): the cross-level roots in Montgomery form,
+// forward then inverse, for the grid kernel (2^lg <= 64).
 inline void prp_build_tables(int ln, int lg, uint32_t *tf, uint32_t *ti, PrpKernelArgs &proto, uint32_t *tfs = nullptr,
-                             uint32_t *tis = nullptr)
+                             uint32_t *tis = nullptr, uint32_t *xr = nullptr)
 {
 	using namespace tables_detail;
 	static const uint32_t kQ[3] = { Q0, Q1, Q2 };
@@ -117,7 +119,7 @@ inline void prp_build_tables(int ln, int lg, uint32_t *tf, uint32_t *ti, PrpKern
 						tis[s + 1] = (uint32_t)(((uint64_t)wi << 32) / q);
 					}
 				}
-		for (size_t k = 1; k < G; ++k)
+		for (size_t k = 1; k < G && k < (size_t)MAX_G; ++k)
 		{
 			const uint32_t w = W[k], wi = invmod(W[k], q);
 			proto.tcf[pi][k] = w;
@@ -125,6 +127,13 @@ inline void prp_build_tables(int ln, int lg, uint32_t *tf, uint32_t *ti, PrpKern
 			proto.tci[pi][k] = wi;
 			proto.tciq[pi][k] = (uint32_t)(((uint64_t)wi << 32) / q);
 		}
+		if (xr)
+			for (size_t k = 0; k < 64; ++k)
+			{
+				const bool in = k >= 1 && k < G;
+				xr[(pi * 2 + 0) * 64 + k] = in ? mont(W[k], q) : 0;
+				xr[(pi * 2 + 1) * 64 + k] = in ? mont(invmod(W[k], q), q) : 0;
+			}
 		const uint32_t w1 = W[1];
 		const uint32_t S = mulmod((uint32_t)(((uint64_t)1 << 32) % q), mulmod(2, invmod((uint32_t)(D % q), q), q), q);
 		const uint32_t K1 = mulmod(S, invmod((mulmod(2, w1, q) + q - 1) % q, q), q);

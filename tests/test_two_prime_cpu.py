@@ -76,9 +76,10 @@ def _rule(ln, minus, b):
 
 def test_library_decision_matches_the_bound(native_lib):
     """ctw_prp_two_primes follows 2 terms (b + 1)^2 < q0 q1 on the splits with a
-    two-prime kernel (one CTA, or 4096 coefficients per CTA)."""
+    two-prime kernel (one CTA, or 4096 coefficients per CTA, clusters or grid)."""
     L = native_lib
-    for ln in range(8, 17):
+    # N+: every degree; 2^17 and 2^18 run one candidate on the grid kernel, which has both counts
+    for ln in range(8, 19):
         for b in (64, 65537, 1 << 20, (1 << 21) - 1, 2330079, 2330081, 6590461, 9320320, 9320322, (1 << 31) - 1):
             assert L.ctw_prp_two_primes(ln, 0, b) == int(_rule(ln, False, b)), (ln, b)
     # N-: transform degree 2^(ln+1) on one CTA up to 2^12 coefficients, else on
@@ -87,8 +88,6 @@ def test_library_decision_matches_the_bound(native_lib):
         split = ln <= 11 or ln in (13, 14, 15)
         for b in (64, 300000, 1 << 21, 3 << 20, (1 << 31) - 1):
             assert L.ctw_prp_two_primes(ln, 1, b) == int(split and _rule(ln, True, b)), (ln, b)
-    # degrees 2^17 and 2^18 have no two-prime kernel
-    assert L.ctw_prp_two_primes(17, 0, 64) == 0 and L.ctw_prp_two_primes(18, 0, 64) == 0
 
 
 def test_workloads_that_take_two_primes(native_lib):

@@ -73,9 +73,12 @@ def test_engine_takes_three_primes_above_the_bound(native):
         assert eng.prime_count == 2
         eng.set_b([1 << 20, b_limit(16) + 1])
         assert eng.prime_count == 3
-    with PrpEngine(17, 1) as eng:          # no two-prime kernel for 8192 coefficients per CTA
+    with PrpEngine(17, 1, log2_ctas=4) as eng:    # no two-prime kernel for 8192 coefficients per CTA
         eng.set_b([1000])
         assert eng.prime_count == 3
+    with PrpEngine(17, 1) as eng:                 # the grid kernel has one
+        eng.set_b([1000])
+        assert eng.prime_count == 2
 
 
 @pytest.mark.parametrize("ln", [12, 13])
