@@ -79,15 +79,22 @@ __device__ __forceinline__ long long ld_l2_ll(const long long *p)
 #endif
 }
 
-// Barrier k of the launch over the G CTAs of one lane: arrive, then wait until
-// k * G arrivals.  A CTA whose wait ran out (*dead) no longer waits.
-__device__ __forceinline__ void grid_sync(unsigned *cnt, unsigned target, uint32_t &err, int *dead)
+// Barrier k of the launch over the G CTAs of one lane, in two halves: arrive
+// (after every thread's global writes), then wait until k * G arrivals.  A CTA
+// whose wait ran out (*dead) no longer waits.
+__device__ __forceinline__ void grid_arrive(unsigned *cnt)
 {
 	__syncthreads();
 	if (threadIdx.x == 0)
 	{
 		__threadfence();
 		atomicAdd(cnt, 1u);
+	}
+}
+__device__ __forceinline__ void grid_wait(unsigned *cnt, unsigned target, uint32_t &err, int *dead)
+{
+	if (threadIdx.x == 0)
+	{
 		if (!*dead)
 		{
 			const unsigned long long t0 = grid_timer();
@@ -217,9 +224,14 @@ __global__ void __launch_bounds__(NP * 256, 1) prp_kernel_grid(const PrpKernelAr
 	long long *gc = ga.gc + (size_t)lane * G * G;                // [G][G]: run-end carries of CTA c at c*G
 	unsigned *bar = ga.bar + (size_t)lane * 32;
 	unsigned nbar = 0;
-	auto gsync = [&]() {
+	auto garrive = [&]() {
 		++nbar;
-		grid_sync(bar, nbar * (unsigned)G, err, &dead);
+		grid_arrive(bar);
+	};
+	auto gwait = [&]() { grid_wait(bar, nbar * (unsigned)G, err, &dead); };
+	auto gsync = [&]() {
+		garrive();
+		gwait();
 	};
 	uint32_t *scr = a.scratch ? a.scratch + ((size_t)lane * G + g) * 3 * M : nullptr;
 	const size_t lane_base = (size_t)lane * D;
@@ -305,25 +317,12 @@ __global__ void __launch_bounds__(NP * 256, 1) prp_kernel_grid(const PrpKernelAr
 		}
 		__syncthreads();
 		for (int h = tid; h < G; h += nt) gc[(size_t)g * G + h] = xch[h];
-		gsync();
 		// normalize2: chunk j of run (h, g) takes the carry of the chunk before it
-		// in natural order; -f of the last chunk goes to coefficient 0, +f to D/2
-		for (int c = tid; c < ncl; c += nt)
-		{
-			const int h = c / runc, j = c - h * runc;
-			int64_t acc;          // a chunk carry plus digits: 64-bit arithmetic is exact
-			if (j > 0) acc = fch[c - 1];
-			else if (g > 0) acc = ld_l2_ll(gc + (size_t)(g - 1) * G + h);
-			else
-			{
-				const int64_t last = ld_l2_ll(gc + (size_t)(G - 1) * G + (G - 1));
-				if (h == 0) acc = -last;
-				else
-				{
-					acc = ld_l2_ll(gc + (size_t)(G - 1) * G + (h - 1));
-					if (h == G / 2) acc += last;
-				}
-			}
+		// in natural order; -f of the last chunk goes to coefficient 0, +f to D/2.
+		// Chunks j > 0 need only this CTA's carries and run while the barrier
+		// completes; the first chunk of each run follows it.
+		auto carry_in = [&](int h, int j, int64_t acc) {
+			// a chunk carry plus digits: 64-bit arithmetic is exact
 			uint32_t *Xh = XC + h * MG;
 			const int base = cb + j * csz;
 			int i = 0;
@@ -342,6 +341,29 @@ __global__ void __launch_bounds__(NP * 256, 1) prp_kernel_grid(const PrpKernelAr
 				if (s != (int32_t)s) err |= ST_DIGIT_RANGE;
 				Xh[p] = (uint32_t)(int32_t)s;
 			}
+		};
+		garrive();
+		for (int k = tid; k < ncl - G; k += nt)
+		{
+			const int h = k / (runc - 1), j = k - h * (runc - 1) + 1;
+			carry_in(h, j, fch[h * runc + j - 1]);
+		}
+		gwait();
+		for (int h = tid; h < G; h += nt)
+		{
+			int64_t acc;
+			if (g > 0) acc = ld_l2_ll(gc + (size_t)(g - 1) * G + h);
+			else
+			{
+				const int64_t last = ld_l2_ll(gc + (size_t)(G - 1) * G + (G - 1));
+				if (h == 0) acc = -last;
+				else
+				{
+					acc = ld_l2_ll(gc + (size_t)(G - 1) * G + (h - 1));
+					if (h == G / 2) acc += last;
+				}
+			}
+			carry_in(h, 0, acc);
 		}
 		__syncthreads();
 	};

@@ -39,7 +39,7 @@ __host__ __device__ __forceinline__ size_t smem_stage_words(int lm, int lg, int 
 }
 
 template <int LG, bool M12, int NP>
-__global__ void __launch_bounds__(M12 ? NP * 256 : NT_MAX, 1) prp_kernel(const PrpKernelArgs a)
+__global__ void __launch_bounds__(M12 ? NP * 256 : NT_MAX, (M12 && NP == 2 && LG == 0) ? 2 : 1) prp_kernel(const PrpKernelArgs a)
 {
 	constexpr int G = 1 << LG;
 	static_assert(NP == 3 || LG == 0, "two-prime launches use one CTA or the column layout");
