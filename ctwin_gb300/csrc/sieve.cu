@@ -275,6 +275,25 @@ struct PosPrime {
 	uint64_t p, k;
 };
 
+// Generator of one prime: c (Montgomery form) and, in plain form with their
+// Shoup quotients floor(w 2^64 / p), the steps c^2 and c^4 of the root walk.
+struct PosGen {
+	uint64_t c, c2, c2q, c4, c4q;
+};
+
+// x * w mod p for any x < 2^64, w < p < 2^62 and wq = floor(w 2^64 / p), in
+// plain form (V. Shoup's precomputed-quotient multiplication: x w - q p < 2p).
+__device__ __forceinline__ uint64_t shoup64(uint64_t x, uint64_t w, uint64_t wq, uint64_t p)
+{
+	const uint64_t q = __umul64hi(x, wq);
+	const uint64_t r = x * w - q * p;
+	return r >= p ? r - p : r;
+}
+__device__ __forceinline__ uint64_t shoup64_quot(uint64_t w, uint64_t p)
+{
+	return (uint64_t)(((unsigned __int128)w << 64) / p);
+}
+
 // k in [k0, k0 + nk): filters of ctsieve.cpp:683-701, compaction of primes.
 __global__ void pos_candidates(int n, uint64_t k0, uint64_t nk, PosPrime *out, uint32_t *count,
                                unsigned long long *p_last, uint32_t cap)
@@ -296,7 +315,7 @@ __global__ void pos_candidates(int n, uint64_t k0, uint64_t nk, PosPrime *out, u
 }
 
 // Generator c = a^k with c^(3*2^(n-1)) = -1 and c^(2^n) != 1, i.e. of order 3*2^n.
-__global__ void pos_generators(int n, const PosPrime *pr, const uint32_t *count, uint32_t cap, uint64_t *gen,
+__global__ void pos_generators(int n, const PosPrime *pr, const uint32_t *count, uint32_t cap, PosGen *gen,
                                uint32_t *status)
 {
 	const uint32_t cnt = min(*count, cap);
@@ -318,14 +337,24 @@ __global__ void pos_generators(int n, const PosPrime *pr, const uint32_t *count,
 			break;
 		}
 		if (c == 0) atomicOr(status, 1u);
-		gen[i] = c;
+		PosGen gv{ c, 0, 0, 0, 0 };
+		if (c)
+		{
+			const uint64_t c2m = mp_mul(m, c, c);
+			gv.c2 = mp_toint(m, c2m);
+			gv.c4 = mp_toint(m, mp_mul(m, c2m, c2m));
+			gv.c2q = shoup64_quot(gv.c2, p);
+			gv.c4q = shoup64_quot(gv.c4, p);
+		}
+		gen[i] = gv;
 	}
 }
 
 // Root chunks: task = (prime, chunk of t), t in [0, 2^(n-2)), four roots per t:
-// +-c^(6t+1), +-c^(6t+5).
+// +-c^(6t+1), +-c^(6t+5).  The walk stays in plain form (two Shoup products by
+// c^4 and c^2 per four roots), so no root leaves Montgomery form.
 __global__ void pos_roots(int n, int lchunk, const PosPrime *pr, const uint32_t *count, uint32_t cap,
-                          const uint64_t *gen, StrikeTarget T)
+                          const PosGen *gen, StrikeTarget T)
 {
 	extern __shared__ uint32_t sbits[];
 	uint32_t *sb = T.smem_words > 0 ? sbits : nullptr;
@@ -346,24 +375,24 @@ __global__ void pos_roots(int n, int lchunk, const PosPrime *pr, const uint32_t 
 		const uint32_t ip = (uint32_t)(task >> (lt - lc));
 		const uint64_t t0 = (task & (tasks_per_prime - 1)) << lc;
 		const uint64_t p = pr[ip].p;
-		const uint64_t c = gen[ip];
+		const PosGen gv = gen[ip];
+		const uint64_t c = gv.c;
 		if (c == 0) continue;
 		const Mp m = mp_make(p);
 		const uint64_t c2 = mp_mul(m, c, c), c4 = mp_mul(m, c2, c2), c6 = mp_mul(m, c4, c2);
-		uint64_t x = mp_mul(m, mp_pow(m, c6, t0), c);        // c^(6 t0 + 1)
+		uint64_t x = mp_toint(m, mp_mul(m, mp_pow(m, c6, t0), c));   // c^(6 t0 + 1), plain
 		const bool small_p = p <= bspan;
 		for (uint64_t t = 0; t < (1ull << lc); ++t)
 		{
-			const uint64_t y = mp_mul(m, x, c4);               // c^(6t+5)
-			const uint64_t rx = mp_toint(m, x), ry = mp_toint(m, y);
-			const uint64_t r4[4] = { rx, p - rx, ry, p - ry };
+			const uint64_t y = shoup64(x, gv.c4, gv.c4q, p);   // c^(6t+5)
+			const uint64_t r4[4] = { x, p - x, y, p - y };
 #pragma unroll
 			for (int j = 0; j < 4; ++j)
 			{
 				const uint64_t r = r4[j];
 				if (small_p || (r >= T.b_min && r <= T.b_max)) strike_root(T, sb, r, p);
 			}
-			x = mp_mul(m, y, c2);                              // c^(6t+7)
+			x = shoup64(y, gv.c2, gv.c2q, p);                  // c^(6t+7)
 		}
 	}
 	if (sb) flush_smem_bits(T, sb);
@@ -483,7 +512,7 @@ constexpr int SMEM_BITMAP_MAX_WORDS = 48 * 1024;     // 192 KB shared bitmap seg
 struct SieveDev {
 	uint32_t *bits = nullptr;
 	void *primes = nullptr;
-	uint64_t *gen = nullptr;
+	PosGen *gen = nullptr;
 	uint32_t *count = nullptr;
 	unsigned long long *p_last = nullptr;
 	uint32_t *status = nullptr;
@@ -530,7 +559,7 @@ extern "C" int ctw_sieve_run(int n, uint64_t b_min, uint64_t b_max, uint64_t p_m
 	SV_CUDA(cudaMalloc(&d.bits, words * 4));
 	SV_CUDA(cudaMemcpy(d.bits, struck_words, words * 4, cudaMemcpyHostToDevice));
 	SV_CUDA(cudaMalloc(&d.primes, (size_t)PRIME_CAP * 16));
-	SV_CUDA(cudaMalloc(&d.gen, (size_t)PRIME_CAP * 8));
+	SV_CUDA(cudaMalloc(&d.gen, (size_t)PRIME_CAP * sizeof(PosGen)));
 	SV_CUDA(cudaMalloc(&d.count, 4));
 	SV_CUDA(cudaMalloc(&d.p_last, 8));
 	SV_CUDA(cudaMalloc(&d.status, 4));
@@ -597,7 +626,7 @@ extern "C" int ctw_sieve_factors(int n, uint64_t k_begin, uint64_t k_end, int mo
 	SieveDev d;
 	unsigned long long *dpairs = nullptr;
 	SV_CUDA(cudaMalloc(&d.primes, (size_t)PRIME_CAP * 16));
-	SV_CUDA(cudaMalloc(&d.gen, (size_t)PRIME_CAP * 8));
+	SV_CUDA(cudaMalloc(&d.gen, (size_t)PRIME_CAP * sizeof(PosGen)));
 	SV_CUDA(cudaMalloc(&d.count, 8));
 	SV_CUDA(cudaMalloc(&d.p_last, 8));
 	SV_CUDA(cudaMalloc(&d.status, 4));
