@@ -135,24 +135,43 @@ __device__ bool sprp(const Mp &m, uint32_t a)
 	return false;
 }
 
-// Deterministic for p < 2^64 with the first twelve prime bases.
+// Deterministic Miller-Rabin: bases {2, 7, 61} for p < 4,759,123,141 (Jaeschke
+// 1993), the primes up to 17 for p < 341,550,071,728,321 and up to 37 for
+// p < 2^64 (Sorenson and Webster 2015).  p is odd; a base equal to p passes.
 __device__ bool is_prime(const Mp &m)
 {
 	const uint64_t p = m.p;
 	if (p < 2) return false;
+	if (p < 38) return p == 2 || p == 3 || p == 5 || p == 7 || p == 11 || p == 13 || p == 17 || p == 19 ||
+	                   p == 23 || p == 29 || p == 31 || p == 37;
+	if (!(p & 1)) return false;
+	if (p < 4759123141ull) return sprp(m, 2) && sprp(m, 7) && (p == 61 || sprp(m, 61));
 	const uint32_t bases[12] = { 2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37 };
-	for (int i = 0; i < 12; ++i)
-	{
-		if (p == bases[i]) return true;
-		if (p % bases[i] == 0) return false;
-	}
-	for (int i = 0; i < 12; ++i)
+	const int nb = p < 341550071728321ull ? 7 : 12;
+	for (int i = 0; i < nb; ++i)
 		if (!sprp(m, bases[i])) return false;
 	return true;
 }
 
+__device__ int jacobi32(uint32_t a, uint32_t n)
+{
+	int k = 1;
+	a %= n;
+	while (a != 0)
+	{
+		int tz = __ffs((int)a) - 1;
+		a >>= tz;
+		if ((tz & 1) && ((n & 7) == 3 || (n & 7) == 5)) k = -k;
+		if ((a & 3) == 3 && (n & 3) == 3) k = -k;
+		const uint32_t t = a; a = n; n = t;
+		a %= n;
+	}
+	return (n == 1) ? k : 0;
+}
+
 __device__ int jacobi(uint64_t a, uint64_t n)
 {
+	if (n < (1ull << 32)) return jacobi32((uint32_t)(a % n), (uint32_t)n);   // 32-bit divisions
 	int k = 1;
 	a %= n;
 	while (a != 0)
@@ -295,22 +314,47 @@ __device__ __forceinline__ uint64_t shoup64_quot(uint64_t w, uint64_t p)
 }
 
 // k in [k0, k0 + nk): filters of ctsieve.cpp:683-701, compaction of primes.
-__global__ void pos_candidates(int n, uint64_t k0, uint64_t nk, PosPrime *out, uint32_t *count,
-                               unsigned long long *p_last, uint32_t cap)
+// Candidates pass three filters of growing cost; the survivors of each are
+// compacted in shared memory so that the next, more expensive test runs on
+// full warps (a warp of raw candidates almost always holds a prime).
+constexpr int CAND_THREADS = 256;
+
+__global__ void __launch_bounds__(CAND_THREADS) pos_candidates(int n, uint64_t k0, uint64_t nk, PosPrime *out,
+                                                               uint32_t *count, unsigned long long *p_last,
+                                                               uint32_t cap)
 {
-	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nk; i += (uint64_t)gridDim.x * blockDim.x)
+	__shared__ uint64_t q1[CAND_THREADS], q2[CAND_THREADS];
+	__shared__ uint32_t n1, n2;
+	for (uint64_t base = blockIdx.x * (uint64_t)CAND_THREADS; base < nk; base += (uint64_t)gridDim.x * CAND_THREADS)
 	{
-		const uint64_t k = k0 + i;
-		const uint64_t p = 3 * (k << n) + 1;
-		if ((p % 5 == 0) || (p % 7 == 0) || (p % 11 == 0) || (p % 13 == 0) || (p % 17 == 0) || (p % 19 == 0) ||
-		    (p % 23 == 0) || (p % 29 == 0) || (p % 31 == 0))
-			continue;
-		const Mp m = mp_make(p);
-		if (!euler2(m)) continue;
-		atomicMax(p_last, (unsigned long long)p);
-		if (!is_prime(m)) continue;
-		const uint32_t idx = atomicAdd(count, 1u);
-		if (idx < cap) out[idx] = PosPrime{ p, k };
+		if (threadIdx.x == 0) { n1 = 0; n2 = 0; }
+		__syncthreads();
+		const uint64_t i = base + threadIdx.x;
+		if (i < nk)
+		{
+			const uint64_t k = k0 + i;
+			const uint64_t p = 3 * (k << n) + 1;
+			if (!((p % 5 == 0) || (p % 7 == 0) || (p % 11 == 0) || (p % 13 == 0) || (p % 17 == 0) || (p % 19 == 0) ||
+			      (p % 23 == 0) || (p % 29 == 0) || (p % 31 == 0)))
+				q1[atomicAdd(&n1, 1u)] = k;
+		}
+		__syncthreads();
+		for (uint32_t j = threadIdx.x; j < n1; j += CAND_THREADS)
+		{
+			const uint64_t k = q1[j], p = 3 * (k << n) + 1;
+			if (!euler2(mp_make(p))) continue;
+			atomicMax(p_last, (unsigned long long)p);
+			q2[atomicAdd(&n2, 1u)] = k;
+		}
+		__syncthreads();
+		for (uint32_t j = threadIdx.x; j < n2; j += CAND_THREADS)
+		{
+			const uint64_t k = q2[j], p = 3 * (k << n) + 1;
+			if (!is_prime(mp_make(p))) continue;
+			const uint32_t idx = atomicAdd(count, 1u);
+			if (idx < cap) out[idx] = PosPrime{ p, k };
+		}
+		__syncthreads();
 	}
 }
 
@@ -403,23 +447,45 @@ __global__ void pos_roots(int n, int lchunk, const PosPrime *pr, const uint32_t 
 // ---------------------------------------------------------------------------
 
 // k in [k0, k0+nk), p = 10k - 1 and 10k + 1, filters of ctsieve.cpp:741-755.
-__global__ void neg_candidates(uint64_t k0, uint64_t nk, uint64_t *out, uint32_t *count,
-                               unsigned long long *p_last, uint32_t cap)
+__global__ void __launch_bounds__(CAND_THREADS) neg_candidates(uint64_t k0, uint64_t nk, uint64_t *out,
+                                                               uint32_t *count, unsigned long long *p_last,
+                                                               uint32_t cap)
 {
-	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < 2 * nk; i += (uint64_t)gridDim.x * blockDim.x)
+	__shared__ uint64_t q1[CAND_THREADS], q2[CAND_THREADS];
+	__shared__ uint32_t n1, n2;
+	const uint64_t total = 2 * nk;
+	for (uint64_t base = blockIdx.x * (uint64_t)CAND_THREADS; base < total; base += (uint64_t)gridDim.x * CAND_THREADS)
 	{
-		const uint64_t k = k0 + (i >> 1);
-		const uint64_t p = 10 * k + 2 * (i & 1) - 1;
-		if ((p % 3 == 0) || (p % 7 == 0)) continue;
-		if (p > 31 && ((p % 11 == 0) || (p % 13 == 0) || (p % 17 == 0) || (p % 19 == 0) || (p % 23 == 0) ||
-		               (p % 29 == 0) || (p % 31 == 0)))
-			continue;
-		const Mp m = mp_make(p);
-		if (!euler2(m) || p == 1093ull * 1093 || p == 3511ull * 3511) continue;
-		atomicMax(p_last, (unsigned long long)p);
-		if (!is_prime(m)) continue;
-		const uint32_t idx = atomicAdd(count, 1u);
-		if (idx < cap) out[idx] = p;
+		if (threadIdx.x == 0) { n1 = 0; n2 = 0; }
+		__syncthreads();
+		const uint64_t i = base + threadIdx.x;
+		if (i < total)
+		{
+			const uint64_t k = k0 + (i >> 1);
+			const uint64_t p = 10 * k + 2 * (i & 1) - 1;
+			bool ok = !((p % 3 == 0) || (p % 7 == 0));
+			if (ok && p > 31 && ((p % 11 == 0) || (p % 13 == 0) || (p % 17 == 0) || (p % 19 == 0) || (p % 23 == 0) ||
+			                     (p % 29 == 0) || (p % 31 == 0)))
+				ok = false;
+			if (ok) q1[atomicAdd(&n1, 1u)] = p;
+		}
+		__syncthreads();
+		for (uint32_t j = threadIdx.x; j < n1; j += CAND_THREADS)
+		{
+			const uint64_t p = q1[j];
+			if (!euler2(mp_make(p)) || p == 1093ull * 1093 || p == 3511ull * 3511) continue;
+			atomicMax(p_last, (unsigned long long)p);
+			q2[atomicAdd(&n2, 1u)] = p;
+		}
+		__syncthreads();
+		for (uint32_t j = threadIdx.x; j < n2; j += CAND_THREADS)
+		{
+			const uint64_t p = q2[j];
+			if (!is_prime(mp_make(p))) continue;
+			const uint32_t idx = atomicAdd(count, 1u);
+			if (idx < cap) out[idx] = p;
+		}
+		__syncthreads();
 	}
 }
 
@@ -587,14 +653,14 @@ extern "C" int ctw_sieve_run(int n, uint64_t b_min, uint64_t b_max, uint64_t p_m
 		SV_CUDA(cudaMemset(d.count, 0, 4));
 		if (mode > 0)
 		{
-			pos_candidates<<<sms * 8, 256>>>(n, k0, nk, (PosPrime *)d.primes, d.count, d.p_last, PRIME_CAP);
+			pos_candidates<<<sms * 8, CAND_THREADS>>>(n, k0, nk, (PosPrime *)d.primes, d.count, d.p_last, PRIME_CAP);
 			pos_generators<<<sms * 4, 128>>>(n, (PosPrime *)d.primes, d.count, PRIME_CAP, d.gen, d.status);
 			pos_roots<<<roots_grid, 256, smem>>>(n, lchunk, (PosPrime *)d.primes, d.count, PRIME_CAP, d.gen, T);
 			g_sieve_launches += 3;
 		}
 		else
 		{
-			neg_candidates<<<sms * 8, 256>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
+			neg_candidates<<<sms * 8, CAND_THREADS>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
 			neg_roots<<<roots_grid, 128, smem>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
 			g_sieve_launches += 2;
 		}
@@ -645,14 +711,14 @@ extern "C" int ctw_sieve_factors(int n, uint64_t k_begin, uint64_t k_end, int mo
 		SV_CUDA(cudaMemset(d.count, 0, 8));
 		if (mode > 0)
 		{
-			pos_candidates<<<sms * 8, 256>>>(n, k0, nk, (PosPrime *)d.primes, d.count, d.p_last, PRIME_CAP);
+			pos_candidates<<<sms * 8, CAND_THREADS>>>(n, k0, nk, (PosPrime *)d.primes, d.count, d.p_last, PRIME_CAP);
 			pos_generators<<<sms * 4, 128>>>(n, (PosPrime *)d.primes, d.count, PRIME_CAP, d.gen, d.status);
 			pos_roots<<<sms * 8, 256, 0>>>(n, 6, (PosPrime *)d.primes, d.count, PRIME_CAP, d.gen, T);
 			g_sieve_launches += 3;
 		}
 		else
 		{
-			neg_candidates<<<sms * 8, 256>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
+			neg_candidates<<<sms * 8, CAND_THREADS>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
 			neg_roots<<<sms * 8, 128, 0>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
 			g_sieve_launches += 2;
 		}
