@@ -252,8 +252,10 @@ __host__ __device__ __forceinline__ size_t cols_words(int lm, int lg, int tw_sme
 	return 2 * np * M + M / 4 + 2 * G + 8 + (tw_smem ? 2 * np * M : 0);
 }
 
-template <int LG, bool M12, int NP>
-__global__ void __launch_bounds__(M12 ? NP * 256 : NT_MAX, 1) prp_kernel_cols(const PrpKernelArgs a)
+// DENSE: compiled for two CTAs per SM (64 registers) and launched with the
+// root tables in global memory, for pools whose many lanes fill the GPU.
+template <int LG, bool M12, int NP, bool DENSE = false>
+__global__ void __launch_bounds__(M12 ? NP * 256 : NT_MAX, DENSE ? 2 : 1) prp_kernel_cols(const PrpKernelArgs a)
 {
 	constexpr int G = 1 << LG;
 	extern __shared__ __align__(16) uint32_t sm[];
@@ -591,12 +593,12 @@ int prp_threads(int lm, int np)
 	return (nt + 31) / 32 * 32;
 }
 
-template <int LG, bool M12, bool COLS, int NP>
+template <int LG, bool M12, bool COLS, int NP, bool DENSE = false>
 static cudaError_t launch_lg(const PrpKernelArgs &a, int lanes, cudaStream_t stream)
 {
 	constexpr int G = 1 << LG;
 	void (*kern)(const PrpKernelArgs);
-	if constexpr (COLS) kern = prp_kernel_cols<LG, M12, NP>;
+	if constexpr (COLS) kern = prp_kernel_cols<LG, M12, NP, DENSE>;
 	else kern = prp_kernel<LG, M12, NP>;
 	const size_t smem = prp_smem_bytes(a.lm, LG, a.tw_smem, NP);
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -634,6 +636,17 @@ bool prp_split_supported(int lm, int lg)
 	return lg == 4;
 }
 
+// SM count of the current device (cached per device).
+static int device_sms()
+{
+	static int cache[16] = {};
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+	if (dev < 0 || dev >= 16) return 0;
+	if (!cache[dev]) cudaDeviceGetAttribute(&cache[dev], cudaDevAttrMultiProcessorCount, dev);
+	return cache[dev];
+}
+
 bool prp_two_prime_split(int lm, int lg)
 {
 	return prp_split_supported(lm, lg) && (lm == 12 || lg == 0);
@@ -648,6 +661,19 @@ cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t s
 		PrpKernelArgs a2 = a;     // two planes of roots may fit where three do not
 		a2.tw_smem = prp_smem_bytes(a.lm, lg, 1, 2) <= 227 * 1024 ? 1 : 0;
 		if (a.lm != 12) return launch_lg<0, false, false, 2>(a2, lanes, stream);
+		// dense: two CTAs per SM once the launch fills the SMs at one per SM
+		const bool dense = a.dense > 0 || (a.dense == 0 && lg > 0 && (lanes << lg) >= device_sms());
+		if (dense && lg > 0)
+		{
+			a2.tw_smem = 0;       // two CTAs per SM: roots from L1 / L2
+			switch (lg)
+			{
+			case 1: return launch_lg<1, true, true, 2, true>(a2, lanes, stream);
+			case 2: return launch_lg<2, true, true, 2, true>(a2, lanes, stream);
+			case 3: return launch_lg<3, true, true, 2, true>(a2, lanes, stream);
+			default: return launch_lg<4, true, true, 2, true>(a2, lanes, stream);
+			}
+		}
 		switch (lg)
 		{
 		case 0: return launch_lg<0, true, false, 2>(a2, lanes, stream);

@@ -55,6 +55,7 @@ struct PrpKernelArgs {
 	int narrow;                 // 1: |coefficients| * 3 + carries < 2^62, carry in 64-bit arithmetic
 	int minus;                  // 1: arithmetic mod N- = b^Dn - b^{Dn/2} - 1 on the transform of degree 2 Dn
 	int nprime;                 // NTT primes: 3, or 2 when every product coefficient fits (prp_two_primes_exact)
+	int dense;                  // two-prime cluster launches at two CTAs per SM: 0 when lanes x CTAs fill the SMs, 1 always, -1 never
 	uint32_t omega[3];          // 6th root w1 (Montgomery form)
 	uint32_t k1[3];             // S / (2 w1 - 1)
 	uint32_t sc[3];             // S = 2^32 * 2 / D   (Montgomery form)

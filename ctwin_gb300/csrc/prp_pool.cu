@@ -261,6 +261,7 @@ int pool_init(ctw_pool *p)
 	a.narrow = 0;                 // per lane (lane_b[3])
 	a.minus = p->minus;
 	a.nprime = 3;                 // per launch (pool_primes)
+	a.dense = 0;                  // two CTAs per SM when the lanes fill the GPU
 	a.scratch = p->d_scratch;
 	a.use_dupmask = 0;
 	POOL_CUDA(cudaDeviceSynchronize());

@@ -124,12 +124,14 @@ def test_pool_switches_prime_count(native):
 
 
 def test_pool_two_and_three_primes_agree(native):
-    """The same tests at degree 2^14 on two primes and held to three."""
+    """The same 40 tests at degree 2^14 on two primes and held to three.  40
+    lanes of 4 CTAs fill the GPU, so the two-prime launches run at two CTAs per
+    SM (roots from L2) while the three-prime ones keep one."""
     from ctwin_gb300 import Pool
-    bs = [1 << 21, (1 << 21) + 17, 4000037]
+    bs = [(1 << 21) + 2 * i + 1 for i in range(38)] + [4000037, 4600003]
     out = {}
     for count in (0, 3):
-        with Pool(14, 4) as p:
+        with Pool(14, 40) as p:
             p.set_prime_count(count)
             p.admit_many(bs)
             assert p.prime_count == (2 if count == 0 else 3)
