@@ -174,3 +174,26 @@ def test_server_separates_prime_classes(native):
         want = g[(r["b"], 12, 2)]
         assert r["status"] == 0 and r["gl_ok"], r
         assert (r["is_prp"], r["res64"]) == (want["prp"], int(want["res64"], 16)), r
+
+
+@pytest.mark.parametrize("minus,ln,csize", [(True, 13, 16), (False, 15, 32)])
+def test_dense_pool_matches_single_engine(native, minus, ln, csize):
+    """A pool whose lanes fill the GPU (40 lanes of 4 or 8 CTAs: the dense
+    two-CTA-per-SM build, roots from L2) gives every test the verdict and
+    RES64 of the same test alone in an engine (one lane: the one-CTA-per-SM
+    build), for N- at 2^13 and N+ at 2^15 with a longer carry chunk."""
+    from ctwin_gb300 import Pool, PrpEngine
+    rng = random.Random(ln + (100 if minus else 0))
+    bs = sorted({rng.randrange(1 << 17, 1 << 20) for _ in range(40)})
+    with Pool(ln, len(bs), csize=csize, minus=minus) as p:
+        assert p.admit_many(bs) == len(bs)
+        assert p.prime_count == 2
+        res = {r["b"]: r for r in p.run_to_completion()}
+    assert sorted(res) == bs
+    for b in bs[:1] + bs[-1:]:
+        with PrpEngine(ln, 1, csize=csize, minus=minus) as eng:
+            prp, r64, ok = eng.run([b])
+        r = res[b]
+        assert r["status"] == 0 and r["gl_ok"] and ok[0], r
+        assert (r["is_prp"], r["res64"]) == (bool(prp[0]), int(r64[0])), r
+    assert all(r["status"] == 0 and r["gl_ok"] for r in res.values())
