@@ -649,7 +649,7 @@ static int device_sms()
 
 bool prp_two_prime_split(int lm, int lg)
 {
-	return prp_split_supported(lm, lg) && (lm == 12 || lg == 0);
+	return prp_split_supported(lm, lg) && (lm == 12 || lg == 0 || (lm == 13 && lg == 4));
 }
 
 cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t stream)
@@ -660,6 +660,7 @@ cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t s
 		if (!prp_two_prime_split(a.lm, lg)) return cudaErrorInvalidValue;
 		PrpKernelArgs a2 = a;     // two planes of roots may fit where three do not
 		a2.tw_smem = prp_smem_bytes(a.lm, lg, 1, 2) <= 227 * 1024 ? 1 : 0;
+		if (a.lm == 13 && lg == 4) return launch_lg<4, false, true, 2>(a2, lanes, stream);   // 2^17 on 16 CTAs
 		if (a.lm != 12) return launch_lg<0, false, false, 2>(a2, lanes, stream);
 		// dense: two CTAs per SM once the launch fills the SMs at one per SM
 		const bool dense = a.dense > 0 || (a.dense == 0 && lg > 0 && (lanes << lg) >= device_sms());

@@ -83,9 +83,10 @@ def test_library_decision_matches_the_bound(native_lib):
         for b in (64, 65537, 1 << 20, (1 << 21) - 1, 2330079, 2330081, 6590461, 9320320, 9320322, (1 << 31) - 1):
             assert L.ctw_prp_two_primes(ln, 0, b) == int(_rule(ln, False, b)), (ln, b)
     # N-: transform degree 2^(ln+1) on one CTA up to 2^12 coefficients, else on
-    # >= 4 CTAs; 4096 coefficients per CTA for ln = 13..15, 2048 for ln = 12, 8192 for ln = 16
+    # >= 4 CTAs; 4096 coefficients per CTA for ln = 13..15, 8192 on 16 CTAs for
+    # ln = 16 (both have two-prime kernels), 2048 for ln = 12 (none)
     for ln in range(8, 17):
-        split = ln <= 11 or ln in (13, 14, 15)
+        split = ln != 12
         for b in (64, 300000, 1 << 21, 3 << 20, (1 << 31) - 1):
             assert L.ctw_prp_two_primes(ln, 1, b) == int(split and _rule(ln, True, b)), (ln, b)
 

@@ -32,7 +32,8 @@ def gold():
 
 
 @pytest.mark.parametrize("ln,lg,csize", [(8, 0, 8), (10, 0, 16), (11, 0, 8), (12, 0, 8), (12, 0, 16), (13, 0, 8),
-                                         (13, 1, 8), (14, 0, 32), (14, 2, 16), (15, 3, 8), (16, 4, 8), (16, 4, 16)])
+                                         (13, 1, 8), (14, 0, 32), (14, 2, 16), (15, 3, 8), (16, 4, 8), (16, 4, 16),
+                                         (17, 4, 16)])
 def test_two_prime_registers_bit_exact(native, ln, lg, csize):
     """square_dup and mul on two primes give the reference's registers, with b up
     to the bound (digits at the bound's extreme included)."""
@@ -73,7 +74,7 @@ def test_engine_takes_three_primes_above_the_bound(native):
         assert eng.prime_count == 2
         eng.set_b([1 << 20, b_limit(16) + 1])
         assert eng.prime_count == 3
-    with PrpEngine(17, 1, log2_ctas=4) as eng:    # no two-prime kernel for 8192 coefficients per CTA
+    with PrpEngine(18, 1, log2_ctas=4) as eng:    # no two-prime kernel for 16384 coefficients per CTA
         eng.set_b([1000])
         assert eng.prime_count == 3
     with PrpEngine(17, 1) as eng:                 # the grid kernel has one
