@@ -291,6 +291,8 @@ int check_status(ctw_prp *h)
 	if (st != 0)
 	{
 		cudaMemsetAsync(h->d_status, 0, sizeof(uint32_t), h->stream);
+		if (st & ST_GRID_WAIT)
+			return fail(CTW_E_COMPUTE, "grid kernel: a barrier wait ran out, the launch's results are void (status 0x%x)", st);
 		return fail(CTW_E_COMPUTE, "device arithmetic range check failed (status 0x%x)", st);
 	}
 	return CTW_OK;
