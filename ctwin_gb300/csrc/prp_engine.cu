@@ -445,7 +445,7 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	{
 		h->tw_smem = prp_smem_bytes(h->lm, h->lg, 1) <= 227 * 1024 ? 1 : 0;
 		h->smem = prp_smem_bytes(h->lm, h->lg, h->tw_smem);
-		h->threads = prp_threads(h->lm);
+		h->threads = prp_threads(h->lm, 3, h->lg);
 	}
 	h->b.assign((size_t)lanes, 0);
 	int rc = CTW_OK;
@@ -845,7 +845,7 @@ int ctw_prp_geometry(ctw_prp *h, int *ctas, int *threads, int *smem)
 		return CTW_OK;
 	}
 	const int tw = np == 2 ? (prp_smem_bytes(h->lm, h->lg, 1, 2) <= 227 * 1024 ? 1 : 0) : h->tw_smem;
-	if (threads) *threads = prp_threads(h->lm, np);
+	if (threads) *threads = prp_threads(h->lm, np, h->lg);
 	if (smem) *smem = (int)prp_smem_bytes(h->lm, h->lg, tw, np);
 	return CTW_OK;
 }

@@ -38,8 +38,17 @@ __host__ __device__ __forceinline__ size_t smem_stage_words(int lm, int lg, int 
 	return stage > fch ? stage : fch;
 }
 
+// Occupancy of the one-CTA two-prime builds: 2 CTAs per SM for the
+// 4096-coefficient path (512 threads, 64 registers), 3 for the generic path
+// (at most 256 threads, 80 registers).
+template <bool M12, int NP, int LG> struct PrpBounds {
+	static constexpr int threads = M12 ? NP * 256 : ((NP == 2 && LG == 0) ? 256 : NT_MAX);
+	static constexpr int blocks = (NP == 2 && LG == 0) ? (M12 ? 2 : 3) : 1;
+};
+
 template <int LG, bool M12, int NP>
-__global__ void __launch_bounds__(M12 ? NP * 256 : NT_MAX, (M12 && NP == 2 && LG == 0) ? 2 : 1) prp_kernel(const PrpKernelArgs a)
+__global__ void __launch_bounds__(PrpBounds<M12, NP, LG>::threads, PrpBounds<M12, NP, LG>::blocks)
+    prp_kernel(const PrpKernelArgs a)
 {
 	constexpr int G = 1 << LG;
 	static_assert(NP == 3 || LG == 0, "two-prime launches use one CTA or the column layout");
@@ -583,12 +592,13 @@ size_t prp_smem_bytes(int lm, int lg, int tw_smem, int np)
 	return (words + prp_shoup_words(lm, np)) * 4;
 }
 
-int prp_threads(int lm, int np)
+int prp_threads(int lm, int np, int lg)
 {
 	if (lm == 12) return np * 256;  // one thread per (prime, radix-16 group)
 	const int M = 1 << lm;
 	int nt = np * M / 16;
-	if (nt > NT_MAX) nt = NT_MAX;
+	const int cap = (np == 2 && lg == 0) ? 256 : NT_MAX;   // the two-prime one-CTA build is bounded to 256 threads
+	if (nt > cap) nt = cap;
 	if (nt < 64) nt = 64;
 	return (nt + 31) / 32 * 32;
 }
@@ -610,7 +620,7 @@ static cudaError_t launch_lg(const PrpKernelArgs &a, int lanes, cudaStream_t str
 	}
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(lanes * G);
-	cfg.blockDim = dim3(prp_threads(a.lm, NP));
+	cfg.blockDim = dim3(prp_threads(a.lm, NP, LG));
 	cfg.dynamicSmemBytes = smem;
 	cfg.stream = stream;
 	cudaLaunchAttribute at[1];

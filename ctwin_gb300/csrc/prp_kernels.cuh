@@ -95,7 +95,7 @@ int prp_grid_max_lanes(int lg, int np);
 size_t prp_smem_bytes(int lm, int lg, int tw_smem, int np = 3);
 // Words of the Shoup root tables of one CTA (both directions), 0 unless M = 4096.
 inline size_t prp_shoup_words(int lm, int np = 3) { return lm == 12 ? 2 * (size_t)np * 256 * 2 : 0; }
-int prp_threads(int lm, int np = 3);
+int prp_threads(int lm, int np = 3, int lg = 0);
 // Whether a cluster split D = 2^lg CTAs x 2^lm coefficients has a kernel.
 bool prp_split_supported(int lm, int lg);
 // Whether that split also has a two-prime kernel (one CTA, or 4096 coefficients per CTA).
