@@ -113,6 +113,10 @@ inline bool prp_two_primes_exact(double terms, uint32_t bmax)
 	return 2.0 * terms * bb * bb * (1.0 + 1e-12) < (double)Q0 * (double)Q1;
 }
 cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t stream);
+// The two-prime branch of prp_launch (prp_kernels_np2.cu).
+cudaError_t prp_launch_np2(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t stream);
+// SM count of the current device (cached).
+int prp_device_sms();
 // Register moves of a pool tick (PrpLaneAux) for lanes of degree 2^ln; six
 // register planes `reg_stride` words apart.
 cudaError_t prp_aux_launch(const PrpLaneAux *aux, int32_t *regs, long long reg_stride, int ln, int lanes,
