@@ -16,16 +16,21 @@ __host__ __device__ __forceinline__ size_t smem_stage_words(int lm, int lg, int 
 	return stage > fch ? stage : fch;
 }
 
-// Occupancy of the one-CTA two-prime builds: 2 CTAs per SM for the
-// 4096-coefficient path (512 threads, 64 registers), 3 for the generic path
-// (at most 256 threads, 80 registers).
-template <bool M12, int NP, int LG> struct PrpBounds {
-	static constexpr int threads = M12 ? NP * 256 : ((NP == 2 && LG == 0) ? 256 : NT_MAX);
-	static constexpr int blocks = (NP == 2 && LG == 0) ? (M12 ? 2 : 3) : 1;
+// Occupancy of the one-CTA builds: two primes run 2 CTAs per SM on the
+// 4096-coefficient path (512 threads, 64 registers) and 3 on the generic path
+// (at most 256 threads, 80 registers); the DENSE three-prime build of the
+// 4096-coefficient path runs 2 CTAs per SM of 384 threads (80 registers).
+template <bool M12, int NP, int LG, bool DENSE> struct PrpBounds {
+	static constexpr int threads =
+	    M12 ? ((DENSE && NP == 3) ? 384 : NP * 256) : ((NP == 2 && LG == 0) ? 256 : NT_MAX);
+	static constexpr int blocks = DENSE ? 2 : ((NP == 2 && LG == 0) ? (M12 ? 2 : 3) : 1);
 };
 
-template <int LG, bool M12, int NP>
-__global__ void __launch_bounds__(PrpBounds<M12, NP, LG>::threads, PrpBounds<M12, NP, LG>::blocks)
+// DENSE (M12, three primes): launched with the root tables and the Shoup
+// tables in global memory, so that two CTAs fit an SM; for pools whose lanes
+// fill the GPU.
+template <int LG, bool M12, int NP, bool DENSE = false>
+__global__ void __launch_bounds__(PrpBounds<M12, NP, LG, DENSE>::threads, PrpBounds<M12, NP, LG, DENSE>::blocks)
     prp_kernel(const PrpKernelArgs a)
 {
 	constexpr int G = 1 << LG;
@@ -61,11 +66,20 @@ __global__ void __launch_bounds__(PrpBounds<M12, NP, LG>::threads, PrpBounds<M12
 	}
 	const uint32_t *TFl = a.tw_smem ? TF : tfg;
 	const uint32_t *TIl = a.tw_smem ? TI : tig;
-	uint32_t *SF = a.tw_smem ? TI + NP * M : TF, *SI = SF + NP * 256 * 2;   // Shoup roots of levels 0..7 (M12)
+	// Shoup roots of levels 0..7 (M12): in shared memory, or read through L1 by
+	// the dense three-prime build, which has no room for them
+	uint32_t *SFs = a.tw_smem ? TI + NP * M : TF, *SIs = SFs + NP * 256 * 2;
+	const uint32_t *SF = SFs, *SI = SIs;
 	if constexpr (M12)
 	{
 		const uint32_t *sfg = a.tfs + (size_t)g * 3 * 256 * 2, *sig = a.tis + (size_t)g * 3 * 256 * 2;
-		for (int i = tid; i < NP * 256 * 2; i += nt) { SF[i] = sfg[i]; SI[i] = sig[i]; }
+		if constexpr (DENSE && NP == 3)
+		{
+			SF = sfg;
+			SI = sig;
+		}
+		else
+			for (int i = tid; i < NP * 256 * 2; i += nt) { SFs[i] = sfg[i]; SIs[i] = sig[i]; }
 	}
 
 	const size_t lane_off = (size_t)lane * D + (size_t)g * M;
@@ -242,7 +256,8 @@ __host__ __device__ __forceinline__ size_t cols_words(int lm, int lg, int tw_sme
 // DENSE: compiled for two CTAs per SM (64 registers) and launched with the
 // root tables in global memory, for pools whose many lanes fill the GPU.
 template <int LG, bool M12, int NP, bool DENSE = false>
-__global__ void __launch_bounds__(M12 ? NP * 256 : NT_MAX, DENSE ? 2 : 1) prp_kernel_cols(const PrpKernelArgs a)
+__global__ void __launch_bounds__(M12 ? ((DENSE && NP == 3) ? 384 : NP * 256) : NT_MAX, DENSE ? 2 : 1)
+    prp_kernel_cols(const PrpKernelArgs a)
 {
 	constexpr int G = 1 << LG;
 	extern __shared__ __align__(16) uint32_t sm[];
@@ -276,11 +291,20 @@ __global__ void __launch_bounds__(M12 ? NP * 256 : NT_MAX, DENSE ? 2 : 1) prp_ke
 	}
 	const uint32_t *TFl = a.tw_smem ? TF : tfg;
 	const uint32_t *TIl = a.tw_smem ? TI : tig;
-	uint32_t *SF = a.tw_smem ? TI + NP * M : TF, *SI = SF + NP * 256 * 2;   // Shoup roots of levels 0..7 (M12)
+	// Shoup roots of levels 0..7 (M12): in shared memory, or read through L1 by
+	// the dense three-prime build, which has no room for them
+	uint32_t *SFs = a.tw_smem ? TI + NP * M : TF, *SIs = SFs + NP * 256 * 2;
+	const uint32_t *SF = SFs, *SI = SIs;
 	if constexpr (M12)
 	{
 		const uint32_t *sfg = a.tfs + (size_t)g * 3 * 256 * 2, *sig = a.tis + (size_t)g * 3 * 256 * 2;
-		for (int i = tid; i < NP * 256 * 2; i += nt) { SF[i] = sfg[i]; SI[i] = sig[i]; }
+		if constexpr (DENSE && NP == 3)
+		{
+			SF = sfg;
+			SI = sig;
+		}
+		else
+			for (int i = tid; i < NP * 256 * 2; i += nt) { SFs[i] = sfg[i]; SIs[i] = sig[i]; }
 	}
 	uint32_t *scr = a.scratch ? a.scratch + ((size_t)lane * G + g) * 3 * M : nullptr;
 	const size_t lane_base = (size_t)lane * D;
@@ -564,8 +588,9 @@ static cudaError_t launch_lg(const PrpKernelArgs &a, int lanes, cudaStream_t str
 	constexpr int G = 1 << LG;
 	void (*kern)(const PrpKernelArgs);
 	if constexpr (COLS) kern = prp_kernel_cols<LG, M12, NP, DENSE>;
-	else kern = prp_kernel<LG, M12, NP>;
-	const size_t smem = prp_smem_bytes(a.lm, LG, a.tw_smem, NP);
+	else kern = prp_kernel<LG, M12, NP, DENSE>;
+	constexpr bool SHOUP_L2 = M12 && DENSE && NP == 3;     // Shoup tables read from global memory
+	const size_t smem = prp_smem_bytes(a.lm, LG, a.tw_smem, NP) - (SHOUP_L2 ? prp_shoup_words(12, 3) * 4 : 0);
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
 	if (G > 8)
@@ -575,7 +600,7 @@ static cudaError_t launch_lg(const PrpKernelArgs &a, int lanes, cudaStream_t str
 	}
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(lanes * G);
-	cfg.blockDim = dim3(prp_threads(a.lm, NP, LG));
+	cfg.blockDim = dim3(SHOUP_L2 ? 384 : prp_threads(a.lm, NP, LG));
 	cfg.dynamicSmemBytes = smem;
 	cfg.stream = stream;
 	cudaLaunchAttribute at[1];

@@ -85,6 +85,20 @@ cudaError_t prp_launch(const PrpKernelArgs &a, int lg, int lanes, cudaStream_t s
 {
 	if (!prp_split_supported(a.lm, lg)) return cudaErrorInvalidValue;
 	if (a.nprime == 2) return prp_launch_np2(a, lg, lanes, stream);
+	if (a.lm == 12 && (a.dense > 0 || (a.dense == 0 && (lanes << lg) >= prp_device_sms())))
+	{
+		// dense: two CTAs of 384 threads per SM, roots and Shoup tables from L1 / L2
+		PrpKernelArgs a3 = a;
+		a3.tw_smem = 0;
+		switch (lg)
+		{
+		case 0: return launch_lg<0, true, false, 3, true>(a3, lanes, stream);
+		case 1: return launch_lg<1, true, true, 3, true>(a3, lanes, stream);
+		case 2: return launch_lg<2, true, true, 3, true>(a3, lanes, stream);
+		case 3: return launch_lg<3, true, true, 3, true>(a3, lanes, stream);
+		default: return launch_lg<4, true, true, 3, true>(a3, lanes, stream);
+		}
+	}
 	if (a.lm == 12)
 	{
 		switch (lg)
