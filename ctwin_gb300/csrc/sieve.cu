@@ -80,7 +80,56 @@ __device__ __forceinline__ Mp mp_make(uint64_t p)
 	m.one = (0 - p) % p;
 	return m;
 }
-__device__ __forceinline__ uint64_t mp_pow(const Mp &m, uint64_t a, uint64_t e)
+// The same Montgomery arithmetic for p < 2^32 on 32-bit words (values travel
+// as uint64_t so that the root routines below serve both widths).
+struct Mp32 {
+	uint32_t p, q, one;
+};
+__host__ __device__ __forceinline__ Mp32 mp_make32(uint32_t p)
+{
+	Mp32 m;
+	m.p = p;
+	uint32_t x = p;                      // p*p = 1 mod 8: 3 bits
+	for (int i = 0; i < 4; ++i) x *= 2 - p * x;
+	m.q = x;
+	m.one = (0u - p) % p;
+	return m;
+}
+__host__ __device__ __forceinline__ uint64_t mp_mul(const Mp32 &m, uint64_t a, uint64_t b)
+{
+	const uint64_t ab = (uint64_t)(uint32_t)a * (uint32_t)b;
+	const uint32_t lo = (uint32_t)ab, hi = (uint32_t)(ab >> 32);
+	const uint32_t mq = (uint32_t)(((uint64_t)(lo * m.q) * m.p) >> 32);
+	const uint32_t r = hi - mq;
+	return (hi < mq) ? r + m.p : r;
+}
+__host__ __device__ __forceinline__ uint64_t mp_add(const Mp32 &m, uint64_t a, uint64_t b)
+{
+	const uint32_t x = (uint32_t)a, y = (uint32_t)b;
+	const uint32_t c = (x >= m.p - y) ? m.p : 0;
+	return (uint32_t)(x + y - c);
+}
+__host__ __device__ __forceinline__ uint64_t mp_sub(const Mp32 &m, uint64_t a, uint64_t b)
+{
+	const uint32_t x = (uint32_t)a, y = (uint32_t)b;
+	const uint32_t c = (x < y) ? m.p : 0;
+	return (uint32_t)(x - y + c);
+}
+__host__ __device__ __forceinline__ uint64_t mp_half(const Mp32 &m, uint64_t a)
+{
+	return (a & 1) ? (a >> 1) + (m.p >> 1) + 1 : a >> 1;
+}
+__host__ __device__ __forceinline__ uint64_t mp_toint(const Mp32 &m, uint64_t r)
+{
+	const uint32_t mq = (uint32_t)(((uint64_t)((uint32_t)r * m.q) * m.p) >> 32);
+	return mq ? m.p - mq : 0;
+}
+template <class M> __device__ __forceinline__ M mp_make_t(uint64_t p);
+template <> __device__ __forceinline__ Mp mp_make_t<Mp>(uint64_t p) { return mp_make(p); }
+template <> __device__ __forceinline__ Mp32 mp_make_t<Mp32>(uint64_t p) { return mp_make32((uint32_t)p); }
+
+template <class M>
+__device__ __forceinline__ uint64_t mp_pow(const M &m, uint64_t a, uint64_t e)
 {
 	uint64_t r = m.one;
 	if (e == 0) return r;
@@ -94,7 +143,8 @@ __device__ __forceinline__ uint64_t mp_pow(const Mp &m, uint64_t a, uint64_t e)
 	return r;
 }
 // Montgomery form of a small integer by doubling/adding from one.
-__device__ __forceinline__ uint64_t mp_small(const Mp &m, uint32_t v)
+template <class M>
+__device__ __forceinline__ uint64_t mp_small(const M &m, uint32_t v)
 {
 	uint64_t r = 0, t = m.one;
 	while (v)
@@ -188,7 +238,8 @@ __device__ int jacobi(uint64_t a, uint64_t n)
 
 // Square root of a quadratic residue am (Montgomery form); 0 if none found.
 // p = 3 mod 4: am^((p+1)/4); p = 5 mod 8: Atkin; otherwise Tonelli-Shanks.
-__device__ uint64_t mp_sqrt(const Mp &m, uint64_t am)
+template <class M>
+__device__ uint64_t mp_sqrt(const M &m, uint64_t am)
 {
 	const uint64_t p = m.p;
 	if (am == 0 || am == m.one) return am;
@@ -211,16 +262,16 @@ __device__ uint64_t mp_sqrt(const Mp &m, uint64_t am)
 		uint64_t c = mp_pow(m, mp_small(m, z), q);
 		uint64_t t = mp_pow(m, am, q);
 		x = mp_pow(m, am, (q + 1) >> 1);
-		int M = s;
+		int Ms = s;
 		for (int guard = 0; guard < 70 && t != m.one; ++guard)
 		{
 			int i = 0;
 			uint64_t tt = t;
-			while (tt != m.one && i < M) { tt = mp_mul(m, tt, tt); ++i; }
-			if (i == M) return 0;
+			while (tt != m.one && i < Ms) { tt = mp_mul(m, tt, tt); ++i; }
+			if (i == Ms) return 0;
 			uint64_t bb = c;
-			for (int j = 0; j < M - i - 1; ++j) bb = mp_mul(m, bb, bb);
-			M = i;
+			for (int j = 0; j < Ms - i - 1; ++j) bb = mp_mul(m, bb, bb);
+			Ms = i;
 			c = mp_mul(m, bb, bb);
 			t = mp_mul(m, t, c);
 			x = mp_mul(m, x, bb);
@@ -490,7 +541,8 @@ __global__ void __launch_bounds__(CAND_THREADS) neg_candidates(uint64_t k0, uint
 }
 
 // All roots of b^(2^N) = a (Montgomery form), N = n - 1, struck directly.
-__device__ void neg_sqrtn_strike(const Mp &m, uint64_t a, int N, const StrikeTarget &T, uint32_t *sb,
+template <class M>
+__device__ void neg_sqrtn_strike(const M &m, uint64_t a, int N, const StrikeTarget &T, uint32_t *sb,
                                  uint32_t *status)
 {
 	const uint64_t p = m.p;
@@ -516,10 +568,14 @@ __device__ void neg_sqrtn_strike(const Mp &m, uint64_t a, int N, const StrikeTar
 	}
 	if (mm > 1) r = mp_pow(m, r, mm);
 	if (r == 0) { atomicOr(status, 2u); return; }
-	// primitive 2^e-th root of unity from a quadratic non-residue
-	uint32_t d = 2;
-	while (jacobi(d, p) != -1 && d < 1000000u) ++d;
-	const uint64_t u = mp_pow(m, mp_small(m, d), (p - 1) >> e);
+	// primitive 2^e-th root of unity from a quadratic non-residue (-1 for e = 1)
+	uint64_t u = p - m.one;
+	if (e > 1)
+	{
+		uint32_t d = 2;
+		while (jacobi(d, p) != -1 && d < 1000000u) ++d;
+		u = mp_pow(m, mp_small(m, d), (p - 1) >> e);
+	}
 	const uint64_t bspan = T.b_max;
 	const bool small_p = p <= bspan;
 	for (uint64_t i = 0; i < (1ull << e); i += 2)
@@ -533,6 +589,8 @@ __device__ void neg_sqrtn_strike(const Mp &m, uint64_t a, int N, const StrikeTar
 	}
 }
 
+// M = Mp32 when every prime of the launch is below 2^32.
+template <class M>
 __global__ void neg_roots(int n, const uint64_t *primes, const uint32_t *count, uint32_t cap, StrikeTarget T,
                           uint32_t *status)
 {
@@ -548,7 +606,7 @@ __global__ void neg_roots(int n, const uint64_t *primes, const uint32_t *count, 
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
 	{
 		const uint64_t p = primes[i];
-		const Mp m = mp_make(p);
+		const M m = mp_make_t<M>(p);
 		const uint64_t five = mp_small(m, 5);
 		const uint64_t s5 = mp_sqrt(m, five);
 		if (s5 == 0) { atomicOr(status, 4u); continue; }
@@ -641,7 +699,8 @@ extern "C" int ctw_sieve_run(int n, uint64_t b_min, uint64_t b_max, uint64_t p_m
 	if (use_smem)
 	{
 		SV_CUDA(cudaFuncSetAttribute(pos_roots, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		SV_CUDA(cudaFuncSetAttribute(neg_roots, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		SV_CUDA(cudaFuncSetAttribute(neg_roots<Mp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		SV_CUDA(cudaFuncSetAttribute(neg_roots<Mp32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	}
 	// With a shared bitmap, one CTA per SM amortises its clear and flush.
 	const int roots_grid = use_smem ? sms : sms * 8;
@@ -661,7 +720,10 @@ extern "C" int ctw_sieve_run(int n, uint64_t b_min, uint64_t b_max, uint64_t p_m
 		else
 		{
 			neg_candidates<<<sms * 8, CAND_THREADS>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
-			neg_roots<<<roots_grid, 128, smem>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
+			if (10 * (k0 + nk) + 1 < (1ull << 32))   // every prime of the block fits 32-bit arithmetic
+				neg_roots<Mp32><<<roots_grid, 128, smem>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
+			else
+				neg_roots<Mp><<<roots_grid, 128, smem>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
 			g_sieve_launches += 2;
 		}
 		SV_CUDA(cudaGetLastError());
@@ -719,7 +781,10 @@ extern "C" int ctw_sieve_factors(int n, uint64_t k_begin, uint64_t k_end, int mo
 		else
 		{
 			neg_candidates<<<sms * 8, CAND_THREADS>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
-			neg_roots<<<sms * 8, 128, 0>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
+			if (10 * (k0 + nk) + 1 < (1ull << 32))
+				neg_roots<Mp32><<<sms * 8, 128, 0>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
+			else
+				neg_roots<Mp><<<sms * 8, 128, 0>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
 			g_sieve_launches += 2;
 		}
 		SV_CUDA(cudaGetLastError());
