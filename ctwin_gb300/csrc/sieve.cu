@@ -157,7 +157,8 @@ __device__ __forceinline__ uint64_t mp_small(const M &m, uint32_t v)
 }
 
 // The reference's base-2 filter: 2^((p-1)/2) == +-1 (ctsieve.cpp:368-381).
-__device__ __forceinline__ bool euler2(const Mp &m)
+template <class M>
+__device__ __forceinline__ bool euler2(const M &m)
 {
 	const uint64_t e = (m.p - 1) >> 1;
 	const uint64_t two = mp_add(m, m.one, m.one);
@@ -166,7 +167,8 @@ __device__ __forceinline__ bool euler2(const Mp &m)
 }
 
 // Strong probable-prime test to base a.
-__device__ bool sprp(const Mp &m, uint32_t a)
+template <class M>
+__device__ bool sprp(const M &m, uint32_t a)
 {
 	uint64_t d = m.p - 1;
 	int s = 0;
@@ -188,7 +190,8 @@ __device__ bool sprp(const Mp &m, uint32_t a)
 // Deterministic Miller-Rabin: bases {2, 7, 61} for p < 4,759,123,141 (Jaeschke
 // 1993), the primes up to 17 for p < 341,550,071,728,321 and up to 37 for
 // p < 2^64 (Sorenson and Webster 2015).  p is odd; a base equal to p passes.
-__device__ bool is_prime(const Mp &m)
+template <class M>
+__device__ bool is_prime(const M &m)
 {
 	const uint64_t p = m.p;
 	if (p < 2) return false;
@@ -498,6 +501,8 @@ __global__ void pos_roots(int n, int lchunk, const PosPrime *pr, const uint32_t 
 // ---------------------------------------------------------------------------
 
 // k in [k0, k0+nk), p = 10k - 1 and 10k + 1, filters of ctsieve.cpp:741-755.
+// M = Mp32 when every candidate of the launch is below 2^32.
+template <class M>
 __global__ void __launch_bounds__(CAND_THREADS) neg_candidates(uint64_t k0, uint64_t nk, uint64_t *out,
                                                                uint32_t *count, unsigned long long *p_last,
                                                                uint32_t cap)
@@ -524,7 +529,7 @@ __global__ void __launch_bounds__(CAND_THREADS) neg_candidates(uint64_t k0, uint
 		for (uint32_t j = threadIdx.x; j < n1; j += CAND_THREADS)
 		{
 			const uint64_t p = q1[j];
-			if (!euler2(mp_make(p)) || p == 1093ull * 1093 || p == 3511ull * 3511) continue;
+			if (!euler2(mp_make_t<M>(p)) || p == 1093ull * 1093 || p == 3511ull * 3511) continue;
 			atomicMax(p_last, (unsigned long long)p);
 			q2[atomicAdd(&n2, 1u)] = p;
 		}
@@ -532,7 +537,7 @@ __global__ void __launch_bounds__(CAND_THREADS) neg_candidates(uint64_t k0, uint
 		for (uint32_t j = threadIdx.x; j < n2; j += CAND_THREADS)
 		{
 			const uint64_t p = q2[j];
-			if (!is_prime(mp_make(p))) continue;
+			if (!is_prime(mp_make_t<M>(p))) continue;
 			const uint32_t idx = atomicAdd(count, 1u);
 			if (idx < cap) out[idx] = p;
 		}
@@ -719,7 +724,10 @@ extern "C" int ctw_sieve_run(int n, uint64_t b_min, uint64_t b_max, uint64_t p_m
 		}
 		else
 		{
-			neg_candidates<<<sms * 8, CAND_THREADS>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
+			if (10 * (k0 + nk) + 1 < (1ull << 32))   // 32-bit arithmetic for the whole block
+				neg_candidates<Mp32><<<sms * 8, CAND_THREADS>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
+			else
+				neg_candidates<Mp><<<sms * 8, CAND_THREADS>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
 			if (10 * (k0 + nk) + 1 < (1ull << 32))   // every prime of the block fits 32-bit arithmetic
 				neg_roots<Mp32><<<roots_grid, 128, smem>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
 			else
@@ -780,7 +788,10 @@ extern "C" int ctw_sieve_factors(int n, uint64_t k_begin, uint64_t k_end, int mo
 		}
 		else
 		{
-			neg_candidates<<<sms * 8, CAND_THREADS>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
+			if (10 * (k0 + nk) + 1 < (1ull << 32))   // 32-bit arithmetic for the whole block
+				neg_candidates<Mp32><<<sms * 8, CAND_THREADS>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
+			else
+				neg_candidates<Mp><<<sms * 8, CAND_THREADS>>>(k0, nk, (uint64_t *)d.primes, d.count, d.p_last, PRIME_CAP);
 			if (10 * (k0 + nk) + 1 < (1ull << 32))
 				neg_roots<Mp32><<<sms * 8, 128, 0>>>(n, (uint64_t *)d.primes, d.count, PRIME_CAP, T, d.status);
 			else
