@@ -696,6 +696,8 @@ def main():
     ap.add_argument("--hbm-budget", type=int, default=64, help="serve: pool budget in GiB")
     ap.add_argument("--log2-degree", type=int, default=16, choices=range(12, 19),
                     help="single: degree of the candidate (2^16 is the headline configuration)")
+    ap.add_argument("--log2-ctas", type=int, default=-1,
+                    help="single: CTAs per candidate as a power of two (-1: the library's default split)")
     args = ap.parse_args()
     global LOG2_D
     LOG2_D = args.log2_degree
@@ -732,7 +734,7 @@ def main():
 
     b, E, i0, B_GL, words = workload(rank)
     D = 1 << LOG2_D
-    eng = PrpEngine(LOG2_D, 1)
+    eng = PrpEngine(LOG2_D, 1, log2_ctas=args.log2_ctas)
     eng.set_b([b])
     eng.set(1)
     eng.copy(1, 0)

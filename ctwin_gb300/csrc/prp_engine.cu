@@ -407,19 +407,22 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
 	if (lanes < 1 || lanes > MAX_INLINE_LANES) return fail(CTW_E_ARG, "lanes %d outside [1, %d]", lanes, MAX_INLINE_LANES);
 	if (ctw_device_count() == 0) return fail(CTW_E_CUDA, "no CUDA device");
-	// Degrees 2^17 and 2^18 default to the grid kernel (2^(ln-12) CTAs of 4096
-	// coefficients per lane) when the lanes fit in one cooperative launch.
+	// Degrees 2^17 and 2^18 default to the grid kernel on 64 CTAs per lane (2048
+	// coefficients each at 2^17, 4096 at 2^18) when the lanes fit in one
+	// cooperative launch.
 	int lg = log2_ctas < 0 ? prp_lg_for(log2_degree) : log2_ctas;
 	bool grid = false;
-	if (log2_ctas < 0 && prp_grid_supported(log2_degree - 12) && lanes <= prp_grid_max_lanes(log2_degree - 12, 3))
+	if (log2_ctas < 0 && log2_degree >= 17 && prp_grid_supported(6, log2_degree - 6) &&
+	    lanes <= prp_grid_max_lanes(6, log2_degree - 6, 3))
 	{
-		lg = log2_degree - 12;
+		lg = 6;
 		grid = true;
 	}
-	else if (log2_ctas >= 0 && prp_grid_supported(lg))
+	else if (log2_ctas > MAX_LG)
 	{
-		if (log2_degree - lg != 12) return fail(CTW_E_ARG, "no kernel for degree 2^%d on 2^%d CTAs", log2_degree, lg);
-		const int cap = prp_grid_max_lanes(lg, 3);
+		if (!prp_grid_supported(lg, log2_degree - lg))
+			return fail(CTW_E_ARG, "no kernel for degree 2^%d on 2^%d CTAs", log2_degree, lg);
+		const int cap = prp_grid_max_lanes(lg, log2_degree - lg, 3);
 		if (lanes > cap) return fail(CTW_E_ARG, "%d lanes of degree 2^%d exceed one grid launch (%d)", lanes, log2_degree, cap);
 		grid = true;
 	}
@@ -437,9 +440,9 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	h->M = h->D / h->G;
 	if (h->grid)
 	{
-		h->tw_smem = prp_grid_smem_bytes(h->lg, 1, 3) <= 227 * 1024 ? 1 : 0;
-		h->smem = prp_grid_smem_bytes(h->lg, h->tw_smem, 3);
-		h->threads = 3 * 256;
+		h->tw_smem = prp_grid_smem_bytes(h->lg, h->lm, 1, 3) <= 227 * 1024 ? 1 : 0;
+		h->smem = prp_grid_smem_bytes(h->lg, h->lm, h->tw_smem, 3);
+		h->threads = 3 * (1 << h->lm) / 16;
 	}
 	else
 	{
@@ -555,7 +558,7 @@ int ctw_prp_two_primes(int log2_degree, int minus, uint32_t b)
 	const int lg = minus ? (ln <= 12 ? 0 : std::max(2, prp_lg_for(ln))) : prp_lg_for(ln);
 	const double Dn = (double)((size_t)1 << log2_degree);
 	// one N+ candidate of degree 2^17 or 2^18 runs on the grid kernel, which has both
-	const bool split = prp_two_prime_split(ln - lg, lg) || (!minus && prp_grid_supported(ln - 12));
+	const bool split = prp_two_prime_split(ln - lg, lg) || (!minus && prp_grid_supported(ln - 12, 12));
 	return (split && prp_two_primes_exact(minus ? Dn : 1.5 * Dn, b)) ? 1 : 0;
 }
 
@@ -839,9 +842,9 @@ int ctw_prp_geometry(ctw_prp *h, int *ctas, int *threads, int *smem)
 	if (ctas) *ctas = (int)h->G;
 	if (h->grid)
 	{
-		const int tw = prp_grid_smem_bytes(h->lg, 1, np) <= 227 * 1024 ? 1 : 0;
-		if (threads) *threads = np * 256;
-		if (smem) *smem = (int)prp_grid_smem_bytes(h->lg, tw, np);
+		const int tw = prp_grid_smem_bytes(h->lg, h->lm, 1, np) <= 227 * 1024 ? 1 : 0;
+		if (threads) *threads = np * (1 << h->lm) / 16;
+		if (smem) *smem = (int)prp_grid_smem_bytes(h->lg, h->lm, tw, np);
 		return CTW_OK;
 	}
 	const int tw = np == 2 ? (prp_smem_bytes(h->lm, h->lg, 1, 2) <= 227 * 1024 ? 1 : 0) : h->tw_smem;

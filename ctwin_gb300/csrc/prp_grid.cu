@@ -115,11 +115,11 @@ __device__ __forceinline__ void grid_wait(unsigned *cnt, unsigned target, uint32
 // every (prime, column) of this CTA; items (prime, group, column) with the
 // column fastest, so that a warp touches consecutive words of a row.  The
 // roots XRT[pi][dir][k] (Montgomery form) of level L, block j sit at k = 2^L + j.
-template <int LG, int R, int NP>
+template <int LG, int LM, int R, int NP>
 __device__ __forceinline__ void cross_pass(uint32_t *XC, const uint32_t *XRT, int l0, int dir, int cb,
                                            const PrpKernelArgs &a, int tid, int nt)
 {
-	constexpr int G = 1 << LG, MG = M12 >> LG, r = Log2<R>::v, NGR = G >> r;
+	constexpr int G = 1 << LG, M = 1 << LM, MG = M >> LG, r = Log2<R>::v, NGR = G >> r, SB = LM == 12 ? 3 : 2;
 	const int lsh = LG - l0 - r, stride = 1 << lsh;
 	for (int it = tid; it < NP * NGR * MG; it += nt)
 	{
@@ -129,7 +129,7 @@ __device__ __forceinline__ void cross_pass(uint32_t *XC, const uint32_t *XRT, in
 		const int jblk = gam >> lsh, i = gam & (stride - 1);
 		const int hbase = (jblk << (LG - l0)) + i;
 		const uint32_t q = qv(pi), qi = qiv(pi);
-		uint32_t *S = XC + pi * M12 + (swz(cb + tt, 3) - cb);
+		uint32_t *S = XC + pi * M + (swz(cb + tt, SB) - cb);
 		const uint32_t *tw = XRT + (pi * 2 + dir) * G;
 		auto idx = [&](int t, int kk) { return (1 << (l0 + t)) + (jblk << t) + kk; };
 		uint32_t u[R];
@@ -143,7 +143,7 @@ __device__ __forceinline__ void cross_pass(uint32_t *XC, const uint32_t *XRT, in
 }
 
 // The LG cross levels as passes of at most 3 levels, larger first.
-template <int LG, int NP>
+template <int LG, int LM, int NP>
 __device__ __forceinline__ void cross_all(uint32_t *XC, const uint32_t *XRT, int dir, int cb, const PrpKernelArgs &a,
                                           int tid, int nt)
 {
@@ -152,11 +152,11 @@ __device__ __forceinline__ void cross_all(uint32_t *XC, const uint32_t *XRT, int
 	constexpr int R1 = L1 == 3 ? 8 : L1 == 2 ? 4 : 2;
 	if (dir == 0)
 	{
-		cross_pass<LG, R0, NP>(XC, XRT, 0, 0, cb, a, tid, nt);
+		cross_pass<LG, LM, R0, NP>(XC, XRT, 0, 0, cb, a, tid, nt);
 		__syncthreads();
 		if constexpr (L1 > 0)
 		{
-			cross_pass<LG, R1, NP>(XC, XRT, L0, 0, cb, a, tid, nt);
+			cross_pass<LG, LM, R1, NP>(XC, XRT, L0, 0, cb, a, tid, nt);
 			__syncthreads();
 		}
 	}
@@ -164,27 +164,29 @@ __device__ __forceinline__ void cross_all(uint32_t *XC, const uint32_t *XRT, int
 	{
 		if constexpr (L1 > 0)
 		{
-			cross_pass<LG, R1, NP>(XC, XRT, L0, 1, cb, a, tid, nt);
+			cross_pass<LG, LM, R1, NP>(XC, XRT, L0, 1, cb, a, tid, nt);
 			__syncthreads();
 		}
-		cross_pass<LG, R0, NP>(XC, XRT, 0, 1, cb, a, tid, nt);
+		cross_pass<LG, LM, R0, NP>(XC, XRT, 0, 1, cb, a, tid, nt);
 		__syncthreads();
 	}
 }
 
 }  // namespace
 
-__host__ __device__ __forceinline__ size_t grid_words(int lg, int tw_smem, int np)
+__host__ __device__ __forceinline__ size_t grid_words(int lg, int lm, int tw_smem, int np)
 {
-	const size_t M = M12, G = (size_t)1 << lg;
-	return 2 * np * M + M / 4 + 2 * G + 2 * np * G + (tw_smem ? 2 * np * M : 0) + 2 * (size_t)np * 512;
+	const size_t M = (size_t)1 << lm, G = (size_t)1 << lg;
+	return 2 * np * M + M / 4 + 2 * G + 2 * np * G + (tw_smem ? 2 * np * M : 0) + (lm == 12 ? 2 * (size_t)np * 512 : 0);
 }
 
-template <int LG, int NP>
-__global__ void __launch_bounds__(NP * 256, 1) prp_kernel_grid(const PrpKernelArgs a, const PrpGridArgs ga)
+// LM: 12 (4096 coefficients per CTA, the dedicated radix-16 path) or 11 (2048,
+// the generic passes); column runs stay >= 32 words (G <= M / 32).
+template <int LG, int NP, int LM>
+__global__ void __launch_bounds__(NP * (1 << LM) / 16, 1) prp_kernel_grid(const PrpKernelArgs a, const PrpGridArgs ga)
 {
-	static_assert(LG >= 1 && LG <= 6, "2..64 CTAs per candidate");
-	constexpr int G = 1 << LG, M = M12, MG = M >> LG, D = M * G, sb = 3;
+	static_assert(LG >= 1 && LG <= 6 && (LM == 12 || LM == 11) && ((1 << LM) >> LG) >= 32, "grid shape");
+	constexpr int G = 1 << LG, M = 1 << LM, MG = M >> LG, D = M * G, sb = LM == 12 ? 3 : 2;
 	extern __shared__ __align__(16) uint32_t sm[];
 	__shared__ int dead;
 	const int tid = threadIdx.x, nt = blockDim.x;
@@ -212,7 +214,8 @@ __global__ void __launch_bounds__(NP * 256, 1) prp_kernel_grid(const PrpKernelAr
 	}
 	const uint32_t *TFl = a.tw_smem ? TF : tfg;
 	const uint32_t *TIl = a.tw_smem ? TI : tig;
-	uint32_t *SF = a.tw_smem ? TI + NP * M : TF, *SI = SF + NP * 256 * 2;   // Shoup roots of levels 0..7
+	uint32_t *SF = a.tw_smem ? TI + NP * M : TF, *SI = SF + NP * 256 * 2;   // Shoup roots of levels 0..7 (LM 12)
+	if constexpr (LM == 12)
 	{
 		const uint32_t *sfg = a.tfs + (size_t)g * 3 * 256 * 2, *sig = a.tis + (size_t)g * 3 * 256 * 2;
 		for (int i = tid; i < NP * 256 * 2; i += nt) { SF[i] = sfg[i]; SI[i] = sig[i]; }
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(NP * 256, 1) prp_kernel_grid(const PrpKernelAr
 			to_residues<NP>(XC, M, p, (int32_t)XC[p]);
 		}
 		__syncthreads();
-		cross_all<LG, NP>(XC, XRT, 0, cb, a, tid, nt);
+		cross_all<LG, LM, NP>(XC, XRT, 0, cb, a, tid, nt);
 		// publish the columns, gather row block g
 		for (int v = tid; v < NP * M4; v += nt)
 			st_l2(gx + (size_t)g * 3 * M + 4 * v, *reinterpret_cast<const uint4 *>(XC + 4 * v));
@@ -266,7 +269,8 @@ __global__ void __launch_bounds__(NP * 256, 1) prp_kernel_grid(const PrpKernelAr
 			*reinterpret_cast<uint4 *>(XR + pi * M + c * MG + o) = ld_l2(gx + (size_t)c * 3 * M + pi * M + g * MG + o);
 		}
 		__syncthreads();
-		local_transform12<NP>(XR, TFl, TIl, SF, SI, mode, false, a, scr, scr, tid, nt);
+		if constexpr (LM == 12) local_transform12<NP>(XR, TFl, TIl, SF, SI, mode, false, a, scr, scr, tid, nt);
+		else local_transform<NP>(XR, TFl, TIl, M, LM, mode, false, a, scr, scr, tid, nt);
 		if (mode == LM_FWD_ONLY) return;
 		// publish the row, gather the columns
 		for (int v = tid; v < NP * M4; v += nt)
@@ -279,7 +283,7 @@ __global__ void __launch_bounds__(NP * 256, 1) prp_kernel_grid(const PrpKernelAr
 			*reinterpret_cast<uint4 *>(XC + pi * M + h * MG + o) = ld_l2(gr + (size_t)h * 3 * M + pi * M + g * MG + o);
 		}
 		__syncthreads();
-		cross_all<LG, NP>(XC, XRT, 1, cb, a, tid, nt);
+		cross_all<LG, LM, NP>(XC, XRT, 1, cb, a, tid, nt);
 		for (int e = tid; e < M; e += nt) garner_at<NP>(XC, M, (e / MG) * MG + (swz(cb + e % MG, sb) - cb), a, narrow);
 		__syncthreads();
 		// normalize1 over the runs; the last chunk of run h publishes its carry
@@ -397,20 +401,20 @@ __global__ void __launch_bounds__(NP * 256, 1) prp_kernel_grid(const PrpKernelAr
 	if (err) atomicOr(a.status, err);
 }
 
-size_t prp_grid_smem_bytes(int lg, int tw_smem, int np) { return grid_words(lg, tw_smem, np) * 4; }
+size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np) { return grid_words(lg, lm, tw_smem, np) * 4; }
 
-template <int LG, int NP>
+template <int LG, int NP, int LM>
 static cudaError_t grid_launch_t(const PrpKernelArgs &a, const PrpGridArgs &ga, int lanes, cudaStream_t stream)
 {
-	void (*kern)(const PrpKernelArgs, const PrpGridArgs) = prp_kernel_grid<LG, NP>;
+	void (*kern)(const PrpKernelArgs, const PrpGridArgs) = prp_kernel_grid<LG, NP, LM>;
 	PrpKernelArgs a2 = a;
-	a2.tw_smem = prp_grid_smem_bytes(LG, 1, NP) <= 227 * 1024 ? 1 : 0;
-	const size_t smem = prp_grid_smem_bytes(LG, a2.tw_smem, NP);
+	a2.tw_smem = prp_grid_smem_bytes(LG, LM, 1, NP) <= 227 * 1024 ? 1 : 0;
+	const size_t smem = prp_grid_smem_bytes(LG, LM, a2.tw_smem, NP);
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(lanes << LG);
-	cfg.blockDim = dim3(NP * 256);
+	cfg.blockDim = dim3(NP * (1 << LM) / 16);
 	cfg.dynamicSmemBytes = smem;
 	cfg.stream = stream;
 	cudaLaunchAttribute at[1];
@@ -421,28 +425,47 @@ static cudaError_t grid_launch_t(const PrpKernelArgs &a, const PrpGridArgs &ga, 
 	return cudaLaunchKernelEx(&cfg, kern, a2, ga);
 }
 
-cudaError_t prp_grid_launch(const PrpKernelArgs &a, const PrpGridArgs &ga, int lg, int lanes, cudaStream_t stream)
+typedef cudaError_t (*GridLaunch)(const PrpKernelArgs &, const PrpGridArgs &, int, cudaStream_t);
+typedef void (*GridKernel)(const PrpKernelArgs, const PrpGridArgs);
+
+// Instances: 2^17 / 2^18 on 32 / 64 CTAs of 4096, 2^16 / 2^17 on 32 / 64 CTAs of 2048.
+static bool grid_pick(int lg, int lm, int np, GridLaunch *launch, GridKernel *kern)
 {
-	if (a.lm != 12 || !prp_grid_supported(lg)) return cudaErrorInvalidValue;
-	if (a.csize > (M12 >> lg)) return cudaErrorInvalidValue;
-	const bool two = a.nprime == 2;
-	switch (lg)
-	{
-	case 5: return two ? grid_launch_t<5, 2>(a, ga, lanes, stream) : grid_launch_t<5, 3>(a, ga, lanes, stream);
-	default: return two ? grid_launch_t<6, 2>(a, ga, lanes, stream) : grid_launch_t<6, 3>(a, ga, lanes, stream);
+	const bool two = np == 2;
+#define CTW_GRID_CASE(LG_, LM_)                                                                                  \
+	if (lg == LG_ && lm == LM_)                                                                                  \
+	{                                                                                                          \
+		if (launch) *launch = two ? grid_launch_t<LG_, 2, LM_> : grid_launch_t<LG_, 3, LM_>;                     \
+		if (kern) *kern = two ? prp_kernel_grid<LG_, 2, LM_> : prp_kernel_grid<LG_, 3, LM_>;                     \
+		return true;                                                                                           \
 	}
+	CTW_GRID_CASE(5, 12)
+	CTW_GRID_CASE(6, 12)
+	CTW_GRID_CASE(5, 11)
+	CTW_GRID_CASE(6, 11)
+#undef CTW_GRID_CASE
+	return false;
 }
 
-int prp_grid_max_lanes(int lg, int np)
+bool prp_grid_supported(int lg, int lm) { return grid_pick(lg, lm, 3, nullptr, nullptr); }
+
+cudaError_t prp_grid_launch(const PrpKernelArgs &a, const PrpGridArgs &ga, int lg, int lanes, cudaStream_t stream)
 {
-	void (*kern)(const PrpKernelArgs, const PrpGridArgs) =
-	    np == 2 ? (lg == 5 ? prp_kernel_grid<5, 2> : prp_kernel_grid<6, 2>)
-	            : (lg == 5 ? prp_kernel_grid<5, 3> : prp_kernel_grid<6, 3>);
-	const int tw = prp_grid_smem_bytes(lg, 1, np) <= 227 * 1024 ? 1 : 0;
-	const size_t smem = prp_grid_smem_bytes(lg, tw, np);
+	GridLaunch launch = nullptr;
+	if (!grid_pick(lg, a.lm, a.nprime == 2 ? 2 : 3, &launch, nullptr)) return cudaErrorInvalidValue;
+	if (a.csize > ((1 << a.lm) >> lg)) return cudaErrorInvalidValue;
+	return launch(a, ga, lanes, stream);
+}
+
+int prp_grid_max_lanes(int lg, int lm, int np)
+{
+	GridKernel kern = nullptr;
+	if (!grid_pick(lg, lm, np, nullptr, &kern)) return 0;
+	const int tw = prp_grid_smem_bytes(lg, lm, 1, np) <= 227 * 1024 ? 1 : 0;
+	const size_t smem = prp_grid_smem_bytes(lg, lm, tw, np);
 	if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
 	int per_sm = 0, dev = 0, sms = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, np * 256, smem) != cudaSuccess) return 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, np * (1 << lm) / 16, smem) != cudaSuccess) return 0;
 	if (cudaGetDevice(&dev) != cudaSuccess) return 0;
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 	return (per_sm * sms) >> lg;

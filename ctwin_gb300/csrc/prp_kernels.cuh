@@ -84,13 +84,13 @@ struct PrpGridArgs {
 	unsigned *bar;              // [lanes][32] barrier counters (word 0 used), zero at launch
 	const uint32_t *xr;         // [3][2][64] cross-level roots (Montgomery): forward, inverse
 };
-constexpr int GRID_MIN_LG = 5, GRID_MAX_LG = 6;
-// Grid splits with a kernel: 2^lg CTAs of 4096 coefficients, lg = 5, 6 (D = 2^17, 2^18).
-inline bool prp_grid_supported(int lg) { return lg >= GRID_MIN_LG && lg <= GRID_MAX_LG; }
-size_t prp_grid_smem_bytes(int lg, int tw_smem, int np);
+// Grid splits with a kernel: 2^lg CTAs of 2^lm coefficients for (lg, lm) =
+// (5, 12), (6, 12) (D = 2^17, 2^18) and (5, 11), (6, 11) (D = 2^16, 2^17).
+bool prp_grid_supported(int lg, int lm);
+size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np);
 cudaError_t prp_grid_launch(const PrpKernelArgs &a, const PrpGridArgs &ga, int lg, int lanes, cudaStream_t stream);
-// Lanes of degree 2^(12 + lg) one cooperative grid launch can hold on this device.
-int prp_grid_max_lanes(int lg, int np);
+// Lanes of degree 2^(lm + lg) one cooperative grid launch can hold on this device.
+int prp_grid_max_lanes(int lg, int lm, int np);
 
 size_t prp_smem_bytes(int lm, int lg, int tw_smem, int np = 3);
 // Words of the Shoup root tables of one CTA (both directions), 0 unless M = 4096.
