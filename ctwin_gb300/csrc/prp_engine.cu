@@ -201,7 +201,7 @@ int check_handle(ctw_prp *h)
 int build_tables(ctw_prp *h)
 {
 	const size_t words = h->G * 3 * h->M, swords = h->G * 3 * 256 * 2;
-	std::vector<uint32_t> tf(words), ti(words), tfs(swords), tis(swords), xr(3 * 2 * 64);
+	std::vector<uint32_t> tf(words), ti(words), tfs(swords), tis(swords), xr(3 * 2 * 128);
 	prp_build_tables(h->ln, h->lg, tf.data(), ti.data(), h->proto, tfs.data(), tis.data(), xr.data());
 	const size_t bytes = words * sizeof(uint32_t);
 	if (h->grid)
@@ -407,16 +407,21 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
 	if (lanes < 1 || lanes > MAX_INLINE_LANES) return fail(CTW_E_ARG, "lanes %d outside [1, %d]", lanes, MAX_INLINE_LANES);
 	if (ctw_device_count() == 0) return fail(CTW_E_CUDA, "no CUDA device");
-	// Degrees 2^17 and 2^18 default to the grid kernel on 64 CTAs per lane (2048
-	// coefficients each at 2^17, 4096 at 2^18) when the lanes fit in one
-	// cooperative launch.
+	// Degrees 2^17 and 2^18 default to the grid kernel with 2048 coefficients per
+	// CTA (64 / 128 CTAs per lane) when the lanes fit in one cooperative launch,
+	// else with 4096 per CTA (32 / 64 CTAs), else 16-CTA clusters.
 	int lg = log2_ctas < 0 ? prp_lg_for(log2_degree) : log2_ctas;
 	bool grid = false;
-	if (log2_ctas < 0 && log2_degree >= 17 && prp_grid_supported(6, log2_degree - 6) &&
-	    lanes <= prp_grid_max_lanes(6, log2_degree - 6, 3))
+	if (log2_ctas < 0 && log2_degree >= 17)
 	{
-		lg = 6;
-		grid = true;
+		for (int lm = 11; lm <= 12 && !grid; ++lm)
+			if (prp_grid_supported(log2_degree - lm, lm) && lanes <= prp_grid_max_lanes(log2_degree - lm, lm, 3))
+			{
+				lg = log2_degree - lm;
+				grid = true;
+			}
+		if (!grid && !prp_split_supported(log2_degree - lg, lg))
+			return fail(CTW_E_ARG, "no kernel for degree 2^%d on 2^%d CTAs", log2_degree, lg);
 	}
 	else if (log2_ctas > MAX_LG)
 	{

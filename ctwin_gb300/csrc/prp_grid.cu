@@ -115,11 +115,17 @@ __device__ __forceinline__ void grid_wait(unsigned *cnt, unsigned target, uint32
 // every (prime, column) of this CTA; items (prime, group, column) with the
 // column fastest, so that a warp touches consecutive words of a row.  The
 // roots XRT[pi][dir][k] (Montgomery form) of level L, block j sit at k = 2^L + j.
+// Swizzle selector of a grid shape: the one-CTA / cluster choice, or 20 (no
+// bit-4 term, so a 16-column run stays in place) when the runs are 16 words.
+template <int LG, int LM> struct GridSwz {
+	static constexpr int v = LM == 12 ? 3 : (((1 << LM) >> LG) >= 32 ? 2 : 20);
+};
+
 template <int LG, int LM, int R, int NP>
 __device__ __forceinline__ void cross_pass(uint32_t *XC, const uint32_t *XRT, int l0, int dir, int cb,
                                            const PrpKernelArgs &a, int tid, int nt)
 {
-	constexpr int G = 1 << LG, M = 1 << LM, MG = M >> LG, r = Log2<R>::v, NGR = G >> r, SB = LM == 12 ? 3 : 2;
+	constexpr int G = 1 << LG, M = 1 << LM, MG = M >> LG, r = Log2<R>::v, NGR = G >> r, SB = GridSwz<LG, LM>::v;
 	const int lsh = LG - l0 - r, stride = 1 << lsh;
 	for (int it = tid; it < NP * NGR * MG; it += nt)
 	{
@@ -142,33 +148,42 @@ __device__ __forceinline__ void cross_pass(uint32_t *XC, const uint32_t *XRT, in
 	}
 }
 
-// The LG cross levels as passes of at most 3 levels, larger first.
+// The LG cross levels as passes of at most 3 levels, larger first: pass P
+// covers levels [l0, l0 + r).
+template <int LG, int P> struct XPass {
+	static constexpr int np = (LG + 2) / 3, base = LG / np, extra = LG % np;
+	static constexpr int r = base + (P < extra ? 1 : 0);
+	static constexpr int l0 = P * base + (P < extra ? P : extra);
+	static constexpr int R = 1 << r;
+};
+
+template <int LG, int LM, int NP, int P>
+__device__ __forceinline__ void cross_one(uint32_t *XC, const uint32_t *XRT, int dir, int cb, const PrpKernelArgs &a,
+                                          int tid, int nt)
+{
+	if constexpr (P < XPass<LG, 0>::np)
+	{
+		cross_pass<LG, LM, XPass<LG, P>::R, NP>(XC, XRT, XPass<LG, P>::l0, dir, cb, a, tid, nt);
+		__syncthreads();
+	}
+}
+
 template <int LG, int LM, int NP>
 __device__ __forceinline__ void cross_all(uint32_t *XC, const uint32_t *XRT, int dir, int cb, const PrpKernelArgs &a,
                                           int tid, int nt)
 {
-	constexpr int R0 = LG == 1 ? 2 : LG == 2 ? 4 : LG == 4 ? 4 : 8;   // first pass: levels [0, log2 R0)
-	constexpr int L0 = Log2<R0>::v, L1 = LG - L0;                     // second pass: levels [L0, LG)
-	constexpr int R1 = L1 == 3 ? 8 : L1 == 2 ? 4 : 2;
+	static_assert(XPass<LG, 0>::np <= 3, "at most three cross passes");
 	if (dir == 0)
 	{
-		cross_pass<LG, LM, R0, NP>(XC, XRT, 0, 0, cb, a, tid, nt);
-		__syncthreads();
-		if constexpr (L1 > 0)
-		{
-			cross_pass<LG, LM, R1, NP>(XC, XRT, L0, 0, cb, a, tid, nt);
-			__syncthreads();
-		}
+		cross_one<LG, LM, NP, 0>(XC, XRT, 0, cb, a, tid, nt);
+		cross_one<LG, LM, NP, 1>(XC, XRT, 0, cb, a, tid, nt);
+		cross_one<LG, LM, NP, 2>(XC, XRT, 0, cb, a, tid, nt);
 	}
 	else
 	{
-		if constexpr (L1 > 0)
-		{
-			cross_pass<LG, LM, R1, NP>(XC, XRT, L0, 1, cb, a, tid, nt);
-			__syncthreads();
-		}
-		cross_pass<LG, LM, R0, NP>(XC, XRT, 0, 1, cb, a, tid, nt);
-		__syncthreads();
+		cross_one<LG, LM, NP, 2>(XC, XRT, 1, cb, a, tid, nt);
+		cross_one<LG, LM, NP, 1>(XC, XRT, 1, cb, a, tid, nt);
+		cross_one<LG, LM, NP, 0>(XC, XRT, 1, cb, a, tid, nt);
 	}
 }
 
@@ -181,12 +196,14 @@ __host__ __device__ __forceinline__ size_t grid_words(int lg, int lm, int tw_sme
 }
 
 // LM: 12 (4096 coefficients per CTA, the dedicated radix-16 path) or 11 (2048,
-// the generic passes); column runs stay >= 32 words (G <= M / 32).
+// the generic passes); column runs of 16 words (G = 128) take the swizzle
+// without its bit-4 term (GridSwz).
 template <int LG, int NP, int LM>
 __global__ void __launch_bounds__(NP * (1 << LM) / 16, 1) prp_kernel_grid(const PrpKernelArgs a, const PrpGridArgs ga)
 {
-	static_assert(LG >= 1 && LG <= 6 && (LM == 12 || LM == 11) && ((1 << LM) >> LG) >= 32, "grid shape");
-	constexpr int G = 1 << LG, M = 1 << LM, MG = M >> LG, D = M * G, sb = LM == 12 ? 3 : 2;
+	static_assert(LG >= 1 && LG <= 7 && (LM == 12 || LM == 11) && ((1 << LM) >> LG) >= (LM == 12 ? 32 : 16),
+	              "grid shape");
+	constexpr int G = 1 << LG, M = 1 << LM, MG = M >> LG, D = M * G, sb = GridSwz<LG, LM>::v;
 	extern __shared__ __align__(16) uint32_t sm[];
 	__shared__ int dead;
 	const int tid = threadIdx.x, nt = blockDim.x;
@@ -220,7 +237,7 @@ __global__ void __launch_bounds__(NP * (1 << LM) / 16, 1) prp_kernel_grid(const 
 		const uint32_t *sfg = a.tfs + (size_t)g * 3 * 256 * 2, *sig = a.tis + (size_t)g * 3 * 256 * 2;
 		for (int i = tid; i < NP * 256 * 2; i += nt) { SF[i] = sfg[i]; SI[i] = sig[i]; }
 	}
-	for (int i = tid; i < NP * 2 * G; i += nt) XRT[i] = ga.xr[(i / G) * 64 + i % G];
+	for (int i = tid; i < NP * 2 * G; i += nt) XRT[i] = ga.xr[(i / G) * 128 + i % G];
 
 	uint32_t *gx = ga.gx + (size_t)lane * G * 3 * M;             // [G][3][M]: CTA c's column planes at c*3M
 	uint32_t *gr = ga.gr + (size_t)lane * G * 3 * M;             // [G][3][M]: CTA h's row planes at h*3M
@@ -409,6 +426,7 @@ static cudaError_t grid_launch_t(const PrpKernelArgs &a, const PrpGridArgs &ga, 
 	void (*kern)(const PrpKernelArgs, const PrpGridArgs) = prp_kernel_grid<LG, NP, LM>;
 	PrpKernelArgs a2 = a;
 	a2.tw_smem = prp_grid_smem_bytes(LG, LM, 1, NP) <= 227 * 1024 ? 1 : 0;
+	a2.swz_b = GridSwz<LG, LM>::v;          // the generic local passes read it
 	const size_t smem = prp_grid_smem_bytes(LG, LM, a2.tw_smem, NP);
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return e;
@@ -428,7 +446,7 @@ static cudaError_t grid_launch_t(const PrpKernelArgs &a, const PrpGridArgs &ga, 
 typedef cudaError_t (*GridLaunch)(const PrpKernelArgs &, const PrpGridArgs &, int, cudaStream_t);
 typedef void (*GridKernel)(const PrpKernelArgs, const PrpGridArgs);
 
-// Instances: 2^17 / 2^18 on 32 / 64 CTAs of 4096, 2^16 / 2^17 on 32 / 64 CTAs of 2048.
+// Instances: 2^17 / 2^18 on 32 / 64 CTAs of 4096, 2^16 / 2^17 / 2^18 on 32 / 64 / 128 CTAs of 2048.
 static bool grid_pick(int lg, int lm, int np, GridLaunch *launch, GridKernel *kern)
 {
 	const bool two = np == 2;
@@ -443,6 +461,7 @@ static bool grid_pick(int lg, int lm, int np, GridLaunch *launch, GridKernel *ke
 	CTW_GRID_CASE(6, 12)
 	CTW_GRID_CASE(5, 11)
 	CTW_GRID_CASE(6, 11)
+	CTW_GRID_CASE(7, 11)
 #undef CTW_GRID_CASE
 	return false;
 }

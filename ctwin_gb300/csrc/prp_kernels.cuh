@@ -82,10 +82,10 @@ struct PrpGridArgs {
 	uint32_t *gr;               // [lanes][G][3][M] published row planes
 	long long *gc;              // [lanes][G][G] run-end carries
 	unsigned *bar;              // [lanes][32] barrier counters (word 0 used), zero at launch
-	const uint32_t *xr;         // [3][2][64] cross-level roots (Montgomery): forward, inverse
+	const uint32_t *xr;         // [3][2][128] cross-level roots (Montgomery): forward, inverse
 };
 // Grid splits with a kernel: 2^lg CTAs of 2^lm coefficients for (lg, lm) =
-// (5, 12), (6, 12) (D = 2^17, 2^18) and (5, 11), (6, 11) (D = 2^16, 2^17).
+// (5, 12), (6, 12) (D = 2^17, 2^18) and (5, 11), (6, 11), (7, 11) (D = 2^16..2^18).
 bool prp_grid_supported(int lg, int lm);
 size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np);
 cudaError_t prp_grid_launch(const PrpKernelArgs &a, const PrpGridArgs &ga, int lg, int lanes, cudaStream_t stream);

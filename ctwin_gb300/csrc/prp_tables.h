@@ -65,8 +65,8 @@ inline int prp_stage_cols(int lm, int lg)
 // tfs/tis (lm == 12 only, else may be null): [G][3][256][2] Shoup pairs
 // (w, floor(w 2^32 / q)) of the plain roots at indices 1..255 (local levels 0..7).
 // lg is the cluster split (2^lg CTAs per candidate; prp_lg_for(ln) by default).
-// xr (optional, [3][2][64] words): the cross-level roots in Montgomery form,
-// forward then inverse, for the grid kernel (2^lg <= 64).
+// xr (optional, [3][2][128] words): the cross-level roots in Montgomery form,
+// forward then inverse, for the grid kernel (2^lg <= 128).
 inline void prp_build_tables(int ln, int lg, uint32_t *tf, uint32_t *ti, PrpKernelArgs &proto, uint32_t *tfs = nullptr,
                              uint32_t *tis = nullptr, uint32_t *xr = nullptr)
 {
@@ -128,11 +128,11 @@ inline void prp_build_tables(int ln, int lg, uint32_t *tf, uint32_t *ti, PrpKern
 			proto.tciq[pi][k] = (uint32_t)(((uint64_t)wi << 32) / q);
 		}
 		if (xr)
-			for (size_t k = 0; k < 64; ++k)
+			for (size_t k = 0; k < 128; ++k)
 			{
 				const bool in = k >= 1 && k < G;
-				xr[(pi * 2 + 0) * 64 + k] = in ? mont(W[k], q) : 0;
-				xr[(pi * 2 + 1) * 64 + k] = in ? mont(invmod(W[k], q), q) : 0;
+				xr[(pi * 2 + 0) * 128 + k] = in ? mont(W[k], q) : 0;
+				xr[(pi * 2 + 1) * 128 + k] = in ? mont(invmod(W[k], q), q) : 0;
 			}
 		const uint32_t w1 = W[1];
 		const uint32_t S = mulmod((uint32_t)(((uint64_t)1 << 32) % q), mulmod(2, invmod((uint32_t)(D % q), q), q), q);

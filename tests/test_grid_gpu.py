@@ -16,7 +16,7 @@ def _digits(rng, lanes, D, b):
     return np.array([[rng.randint(-(b[l] - 1), b[l] - 1) for _ in range(D)] for l in range(lanes)], dtype=np.int32)
 
 
-@pytest.mark.parametrize("ln,lanes,csize,primes", [(17, 1, 8, 2), (17, 2, 32, 3), (18, 1, 64, 2), (18, 2, 8, 3)])
+@pytest.mark.parametrize("ln,lanes,csize,primes", [(17, 1, 8, 2), (17, 2, 32, 3), (18, 1, 16, 2), (18, 2, 64, 3)])
 def test_grid_registers_bit_exact(native, ln, lanes, csize, primes):
     from ctwin_gb300 import PrpEngine
     rng = random.Random(ln * 100 + lanes * 10 + primes)
@@ -26,7 +26,8 @@ def test_grid_registers_bit_exact(native, ln, lanes, csize, primes):
     y0 = _digits(rng, lanes, D, b)
     masks = [rng.getrandbits(lanes) for _ in range(3)]
     with PrpEngine(ln, lanes, csize=csize) as eng:
-        assert eng.geometry()["ctas_per_lane"] == 64                      # the grid split
+        # the grid split: 2048 coefficients per CTA where the lanes fit (one lane of 2^18), else 4096
+        assert eng.geometry()["ctas_per_lane"] == (128 if (ln == 18 and lanes == 1) else 64)
         eng.set_b(b)
         eng.set_prime_count(0 if primes == 2 else 3)
         assert eng.prime_count == primes
@@ -44,9 +45,10 @@ def test_grid_registers_bit_exact(native, ln, lanes, csize, primes):
             assert np.array_equal(got[l], x), f"lane {l} differs from the oracle"
 
 
-@pytest.mark.parametrize("ln,lg,csize,primes", [(16, 5, 16, 2), (17, 6, 32, 3)])
+@pytest.mark.parametrize("ln,lg,csize,primes", [(16, 5, 16, 2), (17, 6, 32, 3), (18, 7, 16, 3), (18, 7, 8, 2)])
 def test_grid_2048_registers_bit_exact(native, ln, lg, csize, primes):
-    """The grid kernel with 2048 coefficients per CTA (2^16 on 32 CTAs, 2^17 on 64)."""
+    """The grid kernel with 2048 coefficients per CTA (2^16 on 32 CTAs, 2^17 on
+    64, 2^18 on 128 with 16-column runs)."""
     from ctwin_gb300 import PrpEngine
     rng = random.Random(ln * 11 + lg)
     D = 1 << ln
@@ -83,7 +85,7 @@ def test_grid_matches_cluster_kernel(native, ln):
     out = []
     for lg in (-1, 4):
         with PrpEngine(ln, 1, csize=16, log2_ctas=lg) as eng:
-            assert eng.geometry()["ctas_per_lane"] == (64 if lg < 0 else 16)
+            assert eng.geometry()["ctas_per_lane"] == ((1 << (ln - 11)) if lg < 0 else 16)
             eng.set_b(b)
             eng.write_regs(x0[None], 0)
             for m in (1, 0, 1):
@@ -102,7 +104,7 @@ def test_grid_partial_residue_matches_gmp(native, ln, base):
     L = E.bit_length()
     K = 40
     with PrpEngine(ln, 1, base=base) as eng:
-        assert eng.geometry()["ctas_per_lane"] == 64
+        assert eng.geometry()["ctas_per_lane"] == 1 << (ln - 11)
         eng.set_b([b])
         eng.set(1)
         eng.square_bits(O.int_to_words(E), L - 1, K)
