@@ -197,6 +197,68 @@ int check_handle(ctw_prp *h)
 	return CTW_OK;
 }
 
+// Launch shape of the handle's split: CTAs, coefficients per CTA, shared memory.
+void set_shape(ctw_prp *h)
+{
+	h->lm = h->ln - h->lg;
+	h->G = (size_t)1 << h->lg;
+	h->M = h->D / h->G;
+	if (h->grid)
+	{
+		h->tw_smem = prp_grid_smem_bytes(h->lg, h->lm, 1, 3) <= 227 * 1024 ? 1 : 0;
+		h->smem = prp_grid_smem_bytes(h->lg, h->lm, h->tw_smem, 3);
+		h->threads = 3 * (1 << h->lm) / 16;
+	}
+	else
+	{
+		h->tw_smem = prp_smem_bytes(h->lm, h->lg, 1) <= 227 * 1024 ? 1 : 0;
+		h->smem = prp_smem_bytes(h->lm, h->lg, h->tw_smem);
+		h->threads = prp_threads(h->lm, 3, h->lg);
+	}
+}
+
+// Exchange buffers of a grid split.
+int alloc_grid(ctw_prp *h)
+{
+	if (!h->grid) return CTW_OK;
+	const size_t xw = (size_t)h->lanes * 3 * h->D;        // [lanes][G][3][M] words
+	if (cudaMalloc(&h->d_gx, xw * 4) != cudaSuccess || cudaMalloc(&h->d_gr, xw * 4) != cudaSuccess ||
+	    cudaMalloc(&h->d_gc, (size_t)h->lanes * h->G * h->G * sizeof(long long)) != cudaSuccess ||
+	    cudaMalloc(&h->d_bar, (size_t)h->lanes * 32 * sizeof(unsigned)) != cudaSuccess)
+		return fail(CTW_E_NOMEM, "grid exchange buffers");
+	CTW_CUDA(cudaMemset(h->d_bar, 0, (size_t)h->lanes * 32 * sizeof(unsigned)));
+	return CTW_OK;
+}
+
+int build_tables(ctw_prp *h);
+void choose_primes(ctw_prp *h);
+
+// Change the split of a handle; the registers keep their natural digit order in
+// HBM, so their contents carry over.
+int reshape(ctw_prp *h, int lg, bool grid)
+{
+	CTW_CUDA(cudaStreamSynchronize(h->stream));
+	cudaFree(h->d_tf);
+	cudaFree(h->d_ti);
+	cudaFree(h->d_tfs);
+	cudaFree(h->d_tis);
+	cudaFree(h->d_xr);
+	cudaFree(h->d_gx);
+	cudaFree(h->d_gr);
+	cudaFree(h->d_gc);
+	cudaFree(h->d_bar);
+	h->d_tf = h->d_ti = h->d_tfs = h->d_tis = h->d_xr = h->d_gx = h->d_gr = nullptr;
+	h->d_gc = nullptr;
+	h->d_bar = nullptr;
+	h->grid = grid ? 1 : 0;
+	h->lg = lg;
+	set_shape(h);
+	if (int rc = alloc_grid(h)) return rc;
+	if (int rc = build_tables(h)) return rc;
+	choose_primes(h);
+	return CTW_OK;
+}
+
 // Root tables and launch constants (prp_tables.h), uploaded once per handle.
 int build_tables(ctw_prp *h)
 {
@@ -407,14 +469,15 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
 	if (lanes < 1 || lanes > MAX_INLINE_LANES) return fail(CTW_E_ARG, "lanes %d outside [1, %d]", lanes, MAX_INLINE_LANES);
 	if (ctw_device_count() == 0) return fail(CTW_E_CUDA, "no CUDA device");
-	// Degrees 2^17 and 2^18 default to the grid kernel with 2048 coefficients per
-	// CTA (64 / 128 CTAs per lane) when the lanes fit in one cooperative launch,
-	// else with 4096 per CTA (32 / 64 CTAs), else 16-CTA clusters.
+	// Degrees 2^16..2^18 default to the grid kernel with the most CTAs per lane
+	// that has a kernel (2^16: 64 of 1024 coefficients, 2^17: 64 of 2048, 2^18:
+	// 128 of 2048, else 64 of 4096) when the lanes fit in one cooperative launch,
+	// else to 16-CTA clusters.
 	int lg = log2_ctas < 0 ? prp_lg_for(log2_degree) : log2_ctas;
 	bool grid = false;
-	if (log2_ctas < 0 && log2_degree >= 17)
+	if (log2_ctas < 0 && log2_degree >= 16)
 	{
-		for (int lm = 11; lm <= 12 && !grid; ++lm)
+		for (int lm = 10; lm <= 12 && !grid; ++lm)
 			if (prp_grid_supported(log2_degree - lm, lm) && lanes <= prp_grid_max_lanes(log2_degree - lm, lm, 3))
 			{
 				lg = log2_degree - lm;
@@ -441,20 +504,7 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	h->lm = log2_degree - h->lg;
 	h->D = (size_t)1 << log2_degree;
 	h->Dn = h->D;
-	h->G = (size_t)1 << h->lg;
-	h->M = h->D / h->G;
-	if (h->grid)
-	{
-		h->tw_smem = prp_grid_smem_bytes(h->lg, h->lm, 1, 3) <= 227 * 1024 ? 1 : 0;
-		h->smem = prp_grid_smem_bytes(h->lg, h->lm, h->tw_smem, 3);
-		h->threads = 3 * (1 << h->lm) / 16;
-	}
-	else
-	{
-		h->tw_smem = prp_smem_bytes(h->lm, h->lg, 1) <= 227 * 1024 ? 1 : 0;
-		h->smem = prp_smem_bytes(h->lm, h->lg, h->tw_smem);
-		h->threads = prp_threads(h->lm, 3, h->lg);
-	}
+	set_shape(h);
 	h->b.assign((size_t)lanes, 0);
 	int rc = CTW_OK;
 	auto cleanup = [&](int code) { ctw_prp_destroy(h); return code; };
@@ -467,15 +517,7 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	if (cudaMalloc(&h->d_laneb, (size_t)lanes * 4 * sizeof(uint32_t)) != cudaSuccess)
 		return cleanup(fail(CTW_E_NOMEM, "lane allocation"));
 	if (cudaMalloc(&h->d_status, sizeof(uint32_t)) != cudaSuccess) return cleanup(fail(CTW_E_NOMEM, "status"));
-	if (h->grid)
-	{
-		const size_t xw = (size_t)lanes * 3 * h->D;        // [lanes][G][3][M] words
-		if (cudaMalloc(&h->d_gx, xw * 4) != cudaSuccess || cudaMalloc(&h->d_gr, xw * 4) != cudaSuccess ||
-		    cudaMalloc(&h->d_gc, (size_t)lanes * h->G * h->G * sizeof(long long)) != cudaSuccess ||
-		    cudaMalloc(&h->d_bar, (size_t)lanes * 32 * sizeof(unsigned)) != cudaSuccess)
-			return cleanup(fail(CTW_E_NOMEM, "grid exchange buffers"));
-		cudaMemset(h->d_bar, 0, (size_t)lanes * 32 * sizeof(unsigned));
-	}
+	if ((rc = alloc_grid(h))) return cleanup(rc);
 	cudaMemset(h->d_regs, 0, rbytes);
 	cudaMemset(h->d_status, 0, sizeof(uint32_t));
 	cudaMemset(h->d_laneb, 0, (size_t)lanes * 4 * sizeof(uint32_t));
@@ -513,6 +555,25 @@ int ctw_prp_set_csize(ctw_prp *h, int csize)
 {
 	if (int rc = check_handle(h)) return rc;
 	if (csize != 8 && csize != 16 && csize != 32 && csize != 64) return fail(CTW_E_ARG, "csize %d not in {8,16,32,64}", csize);
+	if (h->grid && (size_t)csize > (h->M >> h->lg))
+	{
+		// a grid shape of this degree with column runs of at least csize, else
+		// the 16-CTA cluster split
+		int to_lg = -1;
+		bool to_grid = false;
+		for (int lm = h->lm + 1; lm <= 12 && to_lg < 0; ++lm)
+		{
+			const int lg = h->ln - lm;
+			if (prp_grid_supported(lg, lm) && h->lanes <= prp_grid_max_lanes(lg, lm, 3) &&
+			    (size_t)csize <= (((size_t)1 << lm) >> lg))
+			{
+				to_lg = lg;
+				to_grid = true;
+			}
+		}
+		if (to_lg < 0) to_lg = prp_lg_for(h->ln);
+		if (int rc = reshape(h, to_lg, to_grid)) return rc;
+	}
 	if ((size_t)csize * 2 > h->M) return fail(CTW_E_ARG, "csize too large for this degree");
 	if (h->lg > 0 && h->lm <= 13 && (size_t)csize > (h->M >> h->lg))
 		return fail(CTW_E_ARG, "csize %d longer than a column run of this split", csize);

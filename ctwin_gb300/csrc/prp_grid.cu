@@ -118,7 +118,7 @@ __device__ __forceinline__ void grid_wait(unsigned *cnt, unsigned target, uint32
 // Swizzle selector of a grid shape: the one-CTA / cluster choice, or 20 (no
 // bit-4 term, so a 16-column run stays in place) when the runs are 16 words.
 template <int LG, int LM> struct GridSwz {
-	static constexpr int v = LM == 12 ? 3 : (((1 << LM) >> LG) >= 32 ? 2 : 20);
+	static constexpr int v = LM == 12 ? 3 : (((1 << LM) >> LG) >= 32 ? (LM == 11 ? 2 : 1) : 20);
 };
 
 template <int LG, int LM, int R, int NP>
@@ -195,13 +195,13 @@ __host__ __device__ __forceinline__ size_t grid_words(int lg, int lm, int tw_sme
 	return 2 * np * M + M / 4 + 2 * G + 2 * np * G + (tw_smem ? 2 * np * M : 0) + (lm == 12 ? 2 * (size_t)np * 512 : 0);
 }
 
-// LM: 12 (4096 coefficients per CTA, the dedicated radix-16 path) or 11 (2048,
-// the generic passes); column runs of 16 words (G = 128) take the swizzle
+// LM: 12 (4096 coefficients per CTA, the dedicated radix-16 path), 11 or 10
+// (2048 / 1024, the generic passes); column runs of 16 words take the swizzle
 // without its bit-4 term (GridSwz).
 template <int LG, int NP, int LM>
 __global__ void __launch_bounds__(NP * (1 << LM) / 16, 1) prp_kernel_grid(const PrpKernelArgs a, const PrpGridArgs ga)
 {
-	static_assert(LG >= 1 && LG <= 7 && (LM == 12 || LM == 11) && ((1 << LM) >> LG) >= (LM == 12 ? 32 : 16),
+	static_assert(LG >= 1 && LG <= 7 && LM >= 10 && LM <= 12 && ((1 << LM) >> LG) >= (LM == 12 ? 32 : 16),
 	              "grid shape");
 	constexpr int G = 1 << LG, M = 1 << LM, MG = M >> LG, D = M * G, sb = GridSwz<LG, LM>::v;
 	extern __shared__ __align__(16) uint32_t sm[];
@@ -418,7 +418,14 @@ __global__ void __launch_bounds__(NP * (1 << LM) / 16, 1) prp_kernel_grid(const 
 	if (err) atomicOr(a.status, err);
 }
 
-size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np) { return grid_words(lg, lm, tw_smem, np) * 4; }
+// Shared memory a grid CTA asks for: at least 116 KB, so that an SM holds one
+// CTA and the grid spreads over 2^lg SMs.
+constexpr size_t GRID_SMEM_MIN = 116 * 1024;
+size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np)
+{
+	const size_t b = grid_words(lg, lm, tw_smem, np) * 4;
+	return b > GRID_SMEM_MIN ? b : GRID_SMEM_MIN;
+}
 
 template <int LG, int NP, int LM>
 static cudaError_t grid_launch_t(const PrpKernelArgs &a, const PrpGridArgs &ga, int lanes, cudaStream_t stream)
@@ -446,7 +453,8 @@ static cudaError_t grid_launch_t(const PrpKernelArgs &a, const PrpGridArgs &ga, 
 typedef cudaError_t (*GridLaunch)(const PrpKernelArgs &, const PrpGridArgs &, int, cudaStream_t);
 typedef void (*GridKernel)(const PrpKernelArgs, const PrpGridArgs);
 
-// Instances: 2^17 / 2^18 on 32 / 64 CTAs of 4096, 2^16 / 2^17 / 2^18 on 32 / 64 / 128 CTAs of 2048.
+// Instances: 2^17 / 2^18 on 32 / 64 CTAs of 4096, 2^16 / 2^17 / 2^18 on 32 / 64 / 128 CTAs of 2048,
+// 2^16 on 64 CTAs of 1024.
 static bool grid_pick(int lg, int lm, int np, GridLaunch *launch, GridKernel *kern)
 {
 	const bool two = np == 2;
@@ -462,6 +470,7 @@ static bool grid_pick(int lg, int lm, int np, GridLaunch *launch, GridKernel *ke
 	CTW_GRID_CASE(5, 11)
 	CTW_GRID_CASE(6, 11)
 	CTW_GRID_CASE(7, 11)
+	CTW_GRID_CASE(6, 10)
 #undef CTW_GRID_CASE
 	return false;
 }

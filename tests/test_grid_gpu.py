@@ -120,3 +120,30 @@ def test_grid_too_many_lanes_falls_back_to_clusters(native):
         assert eng.geometry()["ctas_per_lane"] == 16
     with pytest.raises(CtwError):
         PrpEngine(18, 8, log2_ctas=6)
+
+
+@pytest.mark.parametrize("csize,ctas", [(8, 64), (32, 32), (64, 32)])
+def test_grid_reshapes_for_long_chunks(native, csize, ctas):
+    """One lane of degree 2^16 runs on 64 CTAs of 1024 coefficients (column runs
+    of 16); a longer carry chunk moves the handle to 32 CTAs of 2048 (runs of
+    64) without losing its registers, which stay bit-exact with the oracle."""
+    from ctwin_gb300 import PrpEngine
+    rng = random.Random(csize)
+    ln, D = 16, 1 << 16
+    b = [rng.randrange(1 << 18, 1 << 20)]
+    x0 = _digits(rng, 1, D, b)
+    with PrpEngine(ln, 1) as eng:
+        assert eng.geometry()["ctas_per_lane"] == 64
+        eng.set_b(b)
+        eng.write_regs(x0[None], 0)
+        eng.set_csize(csize)                      # may re-split the handle
+        assert eng.geometry()["ctas_per_lane"] == ctas
+        assert np.array_equal(eng.read_regs(0, 1)[0], x0)
+        for m in (1, 1, 0):
+            eng.square_dup(m)
+        got = eng.read_regs(0, 1)[0]
+    with O.Tables(ln) as t:
+        x = x0[0].copy()
+        for m in (1, 1, 0):
+            t.square_dup(x, b[0], 2 if m else 1, csize)
+    assert np.array_equal(got[0], x)
