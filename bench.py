@@ -77,7 +77,7 @@ def workload(rank: int):
     return b, E, i0, B_GL, words
 
 
-TRAFFIC_PER_LAUNCH = 1.5872e6   # ncu dram read+write bytes of one 651-squaring two-prime launch at 2^16
+TRAFFIC_PER_LAUNCH = 1.52e6     # ncu dram read+write bytes of one 651-squaring launch at 2^16 (64-CTA grid)
 
 
 def hbm_line(traffic: float, seconds: float) -> dict:
@@ -845,20 +845,20 @@ def main():
                    "degree": D, "b": b, "exponent_bits": i0 + 1, "squarings_per_step": B_GL,
                    "step": "one Gerbicz-Li block: B_GL resident squarings + one multiply",
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}",
-                   "cluster_ctas": geo["ctas_per_lane"], "threads_per_cta": geo["threads"],
+                   "ctas_per_candidate": geo["ctas_per_lane"], "threads_per_cta": geo["threads"],
                    "smem_per_cta": geo["smem_bytes"], "ntt_primes": primes},
         "tests_per_s_projected": value / (i0 + 1),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": peak_imad / 1e12, "unit": "T IMAD/s",
                      "frac": achieved / peak_imad if peak_imad else None,
-                     "traffic": TRAFFIC_PER_LAUNCH if LOG2_D == 16 else None,
+                     "traffic": TRAFFIC_PER_LAUNCH if (LOG2_D == 16 and args.log2_ctas < 0) else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 651-squaring launch "
-                                       "(profiles/prp_kernel_d65536_full.md)",
+                                       "of the default split (profiles/prp_kernel_d65536_full.md)",
                      "peak_source": "32-bit IMAD probe kernel run on this GPU in this process",
                      "sms_used": geo["ctas_per_lane"],
                      "frac_of_used_sms": (achieved / peak_imad) * 152 / geo["ctas_per_lane"] if peak_imad else None,
                      "kernel_ms": t_launch * 1000.0,
-                     "hbm": hbm_line(TRAFFIC_PER_LAUNCH, t_launch) if LOG2_D == 16 else None},
+                     "hbm": hbm_line(TRAFFIC_PER_LAUNCH, t_launch) if (LOG2_D == 16 and args.log2_ctas < 0) else None},
         "cpu_baseline": cpu,
         "gpu_launches": int(launches),
         "clocks": clocks,
