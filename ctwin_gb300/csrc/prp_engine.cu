@@ -207,7 +207,7 @@ void set_shape(ctw_prp *h)
 	{
 		h->tw_smem = prp_grid_smem_bytes(h->lg, h->lm, 1, 3) <= 227 * 1024 ? 1 : 0;
 		h->smem = prp_grid_smem_bytes(h->lg, h->lm, h->tw_smem, 3);
-		h->threads = 3 * (1 << h->lm) / 16;
+		h->threads = prp_grid_threads(h->lm, 3);
 	}
 	else
 	{
@@ -909,7 +909,7 @@ int ctw_prp_geometry(ctw_prp *h, int *ctas, int *threads, int *smem)
 	if (h->grid)
 	{
 		const int tw = prp_grid_smem_bytes(h->lg, h->lm, 1, np) <= 227 * 1024 ? 1 : 0;
-		if (threads) *threads = np * (1 << h->lm) / 16;
+		if (threads) *threads = prp_grid_threads(h->lm, np);
 		if (smem) *smem = (int)prp_grid_smem_bytes(h->lg, h->lm, tw, np);
 		return CTW_OK;
 	}

@@ -199,7 +199,7 @@ __host__ __device__ __forceinline__ size_t grid_words(int lg, int lm, int tw_sme
 // (2048 / 1024, the generic passes); column runs of 16 words take the swizzle
 // without its bit-4 term (GridSwz).
 template <int LG, int NP, int LM>
-__global__ void __launch_bounds__(NP * (1 << LM) / 16, 1) prp_kernel_grid(const PrpKernelArgs a, const PrpGridArgs ga)
+__global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(const PrpKernelArgs a, const PrpGridArgs ga)
 {
 	static_assert(LG >= 1 && LG <= 7 && LM >= 10 && LM <= 12 && ((1 << LM) >> LG) >= (LM == 12 ? 32 : 16),
 	              "grid shape");
@@ -439,7 +439,7 @@ static cudaError_t grid_launch_t(const PrpKernelArgs &a, const PrpGridArgs &ga, 
 	if (e != cudaSuccess) return e;
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(lanes << LG);
-	cfg.blockDim = dim3(NP * (1 << LM) / 16);
+	cfg.blockDim = dim3(prp_grid_threads(LM, NP));
 	cfg.dynamicSmemBytes = smem;
 	cfg.stream = stream;
 	cudaLaunchAttribute at[1];
@@ -493,7 +493,8 @@ int prp_grid_max_lanes(int lg, int lm, int np)
 	const size_t smem = prp_grid_smem_bytes(lg, lm, tw, np);
 	if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
 	int per_sm = 0, dev = 0, sms = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, np * (1 << lm) / 16, smem) != cudaSuccess) return 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, prp_grid_threads(lm, np), smem) != cudaSuccess)
+		return 0;
 	if (cudaGetDevice(&dev) != cudaSuccess) return 0;
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 	return (per_sm * sms) >> lg;

@@ -87,6 +87,13 @@ struct PrpGridArgs {
 // Grid splits with a kernel: 2^lg CTAs of 2^lm coefficients for (lg, lm) =
 // (5, 12), (6, 12) (D = 2^17, 2^18) and (5, 11), (6, 11), (7, 11) (D = 2^16..2^18).
 bool prp_grid_supported(int lg, int lm);
+// Threads of a grid CTA: one per (prime, radix-16 group) for 4096 and 2048
+// coefficients, one per (prime, radix-8 group) for 1024 (measured: 2^16 +3 %
+// with twice the threads, 2^17 / 2^18 -1..3 %).
+__host__ __device__ constexpr int prp_grid_threads(int lm, int np)
+{
+	return lm == 12 ? np * 256 : (lm == 10 ? np * (1 << lm) / 8 : np * (1 << lm) / 16);
+}
 size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np);
 cudaError_t prp_grid_launch(const PrpKernelArgs &a, const PrpGridArgs &ga, int lg, int lanes, cudaStream_t stream);
 // Lanes of degree 2^(lm + lg) one cooperative grid launch can hold on this device.
