@@ -234,27 +234,50 @@ int build_tables(ctw_prp *h);
 void choose_primes(ctw_prp *h);
 
 // Change the split of a handle; the registers keep their natural digit order in
-// HBM, so their contents carry over.
+// HBM, so their contents carry over.  The new shape's buffers are made first:
+// on failure the handle keeps its old split.
 int reshape(ctw_prp *h, int lg, bool grid)
 {
 	CTW_CUDA(cudaStreamSynchronize(h->stream));
-	cudaFree(h->d_tf);
-	cudaFree(h->d_ti);
-	cudaFree(h->d_tfs);
-	cudaFree(h->d_tis);
-	cudaFree(h->d_xr);
-	cudaFree(h->d_gx);
-	cudaFree(h->d_gr);
-	cudaFree(h->d_gc);
-	cudaFree(h->d_bar);
+	ctw_prp old = *h;                    // shape, tables and buffers in use
 	h->d_tf = h->d_ti = h->d_tfs = h->d_tis = h->d_xr = h->d_gx = h->d_gr = nullptr;
 	h->d_gc = nullptr;
 	h->d_bar = nullptr;
 	h->grid = grid ? 1 : 0;
 	h->lg = lg;
 	set_shape(h);
-	if (int rc = alloc_grid(h)) return rc;
-	if (int rc = build_tables(h)) return rc;
+	int rc = alloc_grid(h);
+	if (!rc) rc = build_tables(h);
+	auto release = [](ctw_prp &x) {
+		cudaFree(x.d_tf);
+		cudaFree(x.d_ti);
+		cudaFree(x.d_tfs);
+		cudaFree(x.d_tis);
+		cudaFree(x.d_xr);
+		cudaFree(x.d_gx);
+		cudaFree(x.d_gr);
+		cudaFree(x.d_gc);
+		cudaFree(x.d_bar);
+	};
+	if (rc)
+	{
+		release(*h);
+		h->grid = old.grid;
+		h->lg = old.lg;
+		h->proto = old.proto;
+		set_shape(h);
+		h->d_tf = old.d_tf;
+		h->d_ti = old.d_ti;
+		h->d_tfs = old.d_tfs;
+		h->d_tis = old.d_tis;
+		h->d_xr = old.d_xr;
+		h->d_gx = old.d_gx;
+		h->d_gr = old.d_gr;
+		h->d_gc = old.d_gc;
+		h->d_bar = old.d_bar;
+		return rc;
+	}
+	release(old);
 	choose_primes(h);
 	return CTW_OK;
 }
