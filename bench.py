@@ -198,10 +198,9 @@ def run_reference(args, rank, world):
         return 0
     threads = os.cpu_count() or 1
     samples = []
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
+    per_step = args.cpu_seconds if args.cpu_seconds > 0 else max(2.0, 20.0 / max(1, args.steps))
     for _ in range(max(1, args.steps)):
-        v, cb = cpu_squarings_per_s(threads, seconds=max(2.0, 20.0 / max(1, args.steps)))
+        v, cb = cpu_squarings_per_s(threads, seconds=per_step)
         samples.append(v)
     v = statistics.median(samples)
     cb["value"] = v
@@ -696,6 +695,8 @@ def main():
     ap.add_argument("--hbm-budget", type=int, default=64, help="serve: pool budget in GiB")
     ap.add_argument("--log2-degree", type=int, default=16, choices=range(12, 19),
                     help="single: degree of the candidate (2^16 is the headline configuration)")
+    ap.add_argument("--cpu-seconds", type=float, default=0.0,
+                    help="reference arm: seconds of CPU work per step (0: 20 s spread over the steps, 2 s minimum)")
     ap.add_argument("--log2-ctas", type=int, default=-1,
                     help="single: CTAs per candidate as a power of two (-1: the library's default split)")
     args = ap.parse_args()
