@@ -8,8 +8,11 @@ has the reference source; the outputs are committed, the GPU tests only read the
   sieve_files.json  md5 of cand_*.txt / sv_*.dat written by the reference's write(true)
   prp_gmp.json      GMP Fermat residues (RES64, PRP flag) for base 2 and 3, N+ and N-
   pool_gmp.json     GMP Fermat residues of the pool / server cases (degrees 2^9..2^15)
+  prp16_gmp.json    degree 2^16: whole Fermat tests of small b (N+ base 2 and 3, N-),
+                    and r_K = base^(E >> (L - K)) mod N+ for K = 4096 at the single-test
+                    workload's b (sha256 of the residue's little-endian bytes + its low 64 bits)
 
-Usage:  python tests/golden/make_golden.py [--skip-slow] [--only pool]
+Usage:  python tests/golden/make_golden.py [--skip-slow] [--only pool|big]
 """
 from __future__ import annotations
 
@@ -75,6 +78,27 @@ def prp_case(args):
     return {"b": b, "n": ln, "base": base, "form": "-" if minus else "+", "res64": f"{r64:016X}", "prp": bool(prp)}
 
 
+# degree 2^16 whole tests: GMP needs 10-40 minutes each for b < 2^7
+BIG_FULL = [(65, 16, 2, False), (100, 16, 2, False), (127, 16, 2, False), (100, 16, 3, False), (101, 16, 2, True)]
+# b of the single-test workload (b uniform in [2^20, 2^21), seed 1) and the prefix length
+BIG_PARTIAL_B, BIG_PARTIAL_K = 1330358, 4096
+
+
+def partial_case(args):
+    from oracle import oracle as O
+    b, ln, base, K = args
+    N = O.n_plus(b, ln)
+    E = N - 1
+    r = O.powmod(base, E >> (E.bit_length() - K), N)
+    raw = r.to_bytes((N.bit_length() + 7) // 8, "little")
+    return {"b": b, "n": ln, "base": base, "form": "+", "K": K, "sha256": hashlib.sha256(raw).hexdigest(),
+            "low64": f"{r & (2 ** 64 - 1):016X}"}
+
+
+def big_case(job):
+    return partial_case(job[1]) if job[0] == "partial" else prp_case(job[1])
+
+
 def pool_jobs():
     import random
     jobs = []
@@ -102,10 +126,18 @@ def pool_jobs():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-slow", action="store_true")
-    ap.add_argument("--only", choices=["pool"], default=None)
+    ap.add_argument("--only", choices=["pool", "big"], default=None)
     args = ap.parse_args()
     from oracle import oracle as O
     O.build()
+    if args.only == "big":
+        jobs = [("partial", (BIG_PARTIAL_B, 16, base, BIG_PARTIAL_K)) for base in (2, 3)]
+        jobs += [("full", j) for j in BIG_FULL]
+        with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+            res = pool.map(big_case, jobs)
+        json.dump(res, open(os.path.join(HERE, "prp16_gmp.json"), "w"), indent=0)
+        print("done", len(res), "degree-2^16 cases")
+        return
     if args.only == "pool":
         path = os.path.join(HERE, "pool_gmp.json")
         have = {}
