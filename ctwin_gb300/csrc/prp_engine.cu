@@ -224,9 +224,9 @@ int alloc_grid(ctw_prp *h)
 	const size_t xw = (size_t)h->lanes * 3 * h->D;        // [lanes][G][3][M] words
 	if (cudaMalloc(&h->d_gx, xw * 4) != cudaSuccess || cudaMalloc(&h->d_gr, xw * 4) != cudaSuccess ||
 	    cudaMalloc(&h->d_gc, (size_t)h->lanes * h->G * h->G * sizeof(long long)) != cudaSuccess ||
-	    cudaMalloc(&h->d_bar, (size_t)h->lanes * 32 * sizeof(unsigned)) != cudaSuccess)
+	    cudaMalloc(&h->d_bar, (size_t)h->lanes * GRID_BAR_WORDS * sizeof(unsigned)) != cudaSuccess)
 		return fail(CTW_E_NOMEM, "grid exchange buffers");
-	CTW_CUDA(cudaMemset(h->d_bar, 0, (size_t)h->lanes * 32 * sizeof(unsigned)));
+	CTW_CUDA(cudaMemset(h->d_bar, 0, (size_t)h->lanes * GRID_BAR_WORDS * sizeof(unsigned)));
 	return CTW_OK;
 }
 
@@ -343,7 +343,7 @@ int launch(ctw_prp *h, const PrpKernelArgs &a)
 	if (h->grid)
 	{
 		// barrier counters start at zero in every launch
-		e = cudaMemsetAsync(h->d_bar, 0, (size_t)h->lanes * 32 * sizeof(unsigned), h->stream);
+		e = cudaMemsetAsync(h->d_bar, 0, (size_t)h->lanes * GRID_BAR_WORDS * sizeof(unsigned), h->stream);
 		if (e == cudaSuccess)
 		{
 			const PrpGridArgs ga{ h->d_gx, h->d_gr, h->d_gc, h->d_bar, h->d_xr };

@@ -10,7 +10,8 @@
 //   block g (16-byte loads that bypass L1); the 4096-coefficient local
 //   transform, pointwise square and inverse; publish the row; grid barrier B;
 //   gather the columns; inverse cross levels; Garner; carry over the runs;
-//   publish the run-end carries; grid barrier C; chunk carries.
+//   publish the run-end carries; wait for those of the preceding CTA only;
+//   chunk carries.
 // Registers after every squaring equal the cluster kernel's (and the
 // reference's) for the same CSIZE: the same transform, carry and wrap rules.
 //
@@ -81,7 +82,8 @@ __device__ __forceinline__ long long ld_l2_ll(const long long *p)
 
 // Barrier k of the launch over the G CTAs of one lane, in two halves: arrive
 // (after every thread's global writes), then wait until k * G arrivals.  A CTA
-// whose wait ran out (*dead) no longer waits.
+// whose wait ran out (*dead) no longer waits.  The same pair on a per-CTA count
+// (target k) waits for the k-th publication of one other CTA.
 __device__ __forceinline__ void grid_arrive(unsigned *cnt)
 {
 	__syncthreads();
@@ -242,8 +244,9 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 	uint32_t *gx = ga.gx + (size_t)lane * G * 3 * M;             // [G][3][M]: CTA c's column planes at c*3M
 	uint32_t *gr = ga.gr + (size_t)lane * G * 3 * M;             // [G][3][M]: CTA h's row planes at h*3M
 	long long *gc = ga.gc + (size_t)lane * G * G;                // [G][G]: run-end carries of CTA c at c*G
-	unsigned *bar = ga.bar + (size_t)lane * 32;
-	unsigned nbar = 0;
+	unsigned *bar = ga.bar + (size_t)lane * GRID_BAR_WORDS;
+	unsigned *cpub = bar + 32;                                  // [G] carry publications of each CTA
+	unsigned nbar = 0, ncar = 0;
 	auto garrive = [&]() {
 		++nbar;
 		grid_arrive(bar);
@@ -340,8 +343,11 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 		for (int h = tid; h < G; h += nt) gc[(size_t)g * G + h] = xch[h];
 		// normalize2: chunk j of run (h, g) takes the carry of the chunk before it
 		// in natural order; -f of the last chunk goes to coefficient 0, +f to D/2.
-		// Chunks j > 0 need only this CTA's carries and run while the barrier
-		// completes; the first chunk of each run follows it.
+		// Chunks j > 0 need only this CTA's carries; the first chunk of each run
+		// needs the run-end carries of CTA g - 1 (CTA 0: of CTA G - 1), so CTA g
+		// publishes its own and waits for that one CTA's publication only.  The
+		// words of gc are rewritten one squaring later, after two grid barriers
+		// that the reader reaches only after it has read them.
 		auto carry_in = [&](int h, int j, int64_t acc) {
 			// a chunk carry plus digits: 64-bit arithmetic is exact
 			uint32_t *Xh = XC + h * MG;
@@ -363,13 +369,14 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 				Xh[p] = (uint32_t)(int32_t)s;
 			}
 		};
-		garrive();
+		++ncar;
+		grid_arrive(cpub + g);
 		for (int k = tid; k < ncl - G; k += nt)
 		{
 			const int h = k / (runc - 1), j = k - h * (runc - 1) + 1;
 			carry_in(h, j, fch[h * runc + j - 1]);
 		}
-		gwait();
+		grid_wait(cpub + (g + G - 1) % G, ncar, err, &dead);
 		for (int h = tid; h < G; h += nt)
 		{
 			int64_t acc;

@@ -75,13 +75,16 @@ enum PrpStatus : uint32_t {
 	ST_GRID_WAIT = 4,           // a grid barrier wait ran out (the launch's results are void)
 };
 
+constexpr int GRID_BAR_WORDS = 32 + 128;
+
 // Buffers of the grid kernel (prp_grid.cu): one candidate on G = 2^lg CTAs of a
 // cooperative launch, transposes and run-end carries through L2.
 struct PrpGridArgs {
 	uint32_t *gx;               // [lanes][G][3][M] published column planes
 	uint32_t *gr;               // [lanes][G][3][M] published row planes
 	long long *gc;              // [lanes][G][G] run-end carries
-	unsigned *bar;              // [lanes][32] barrier counters (word 0 used), zero at launch
+	unsigned *bar;              // [lanes][GRID_BAR_WORDS], zero at launch: word 0 the grid barrier
+	                            // count, words 32 + g the carry publications of CTA g
 	const uint32_t *xr;         // [3][2][128] cross-level roots (Montgomery): forward, inverse
 };
 // Grid splits with a kernel: 2^lg CTAs of 2^lm coefficients for (lg, lm) =
