@@ -77,7 +77,7 @@ def workload(rank: int):
     return b, E, i0, B_GL, words
 
 
-TRAFFIC_PER_LAUNCH = 1.52e6     # ncu dram read+write bytes of one 651-squaring launch at 2^16 (64-CTA grid)
+TRAFFIC_PER_LAUNCH = 1.50e6     # ncu dram read+write bytes of one 651-squaring launch at 2^16 (64-CTA grid)
 
 
 def hbm_line(traffic: float, seconds: float) -> dict:
