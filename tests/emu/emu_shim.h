@@ -1,0 +1,34 @@
+// Host stand-ins for the CUDA built-ins the grid kernel (prp_grid.cu) uses, so
+// that its source compiles with g++ and runs with one host thread per GPU
+// thread (test infrastructure: tests/test_grid_emu_cpu.py).  Shared memory,
+// __syncthreads and the clock come from the driver (grid_emu.cpp); global
+// atomics and fences map to the host's sequentially consistent atomics.
+#pragma once
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+struct dim3 {
+	unsigned x, y, z;
+	dim3(unsigned a = 1, unsigned b = 1, unsigned c = 1) : x(a), y(b), z(c) {}
+};
+extern thread_local dim3 threadIdx, blockIdx;
+extern dim3 blockDim, gridDim;
+#define __global__
+#define __device__
+#define __host__
+#define __forceinline__ inline
+#define __launch_bounds__(...)
+#define __align__(n) alignas(n)
+#define __shared__
+#define CTW_EMU 1
+using std::max;
+using std::min;
+struct alignas(8) uint2 { uint32_t x, y; };
+struct alignas(16) uint4 { uint32_t x, y, z, w; };
+inline uint32_t __umulhi(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) >> 32); }
+inline unsigned atomicOr(unsigned *p, unsigned v) { return __atomic_fetch_or(p, v, __ATOMIC_SEQ_CST); }
+inline unsigned atomicAdd(unsigned *p, unsigned v) { return __atomic_fetch_add(p, v, __ATOMIC_SEQ_CST); }
+inline void __threadfence() { __atomic_thread_fence(__ATOMIC_SEQ_CST); }
+void __syncthreads();
+uint32_t *emu_smem();
+unsigned long long emu_timer_ns();
