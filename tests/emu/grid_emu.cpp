@@ -3,7 +3,7 @@
 // CTA, the grid barriers and carry publications are the kernel's own counters
 // on host atomics.  It squares a seeded register twice (doubling both times),
 // multiplies it by a second one, and compares the digits with the oracle's C
-// restatement (bit-exact).  Test infrastructure (tests/test_grid_emu_cpu.py).
+// restatement (bit-exact).  Test infrastructure (tests/test_kernels_emu_cpu.py).
 //
 // usage: grid_emu <log2 D> <log2 M> <primes> <csize> <b> <threads per CTA>
 #include "emu_shim.h"
@@ -31,6 +31,10 @@ static std::vector<std::vector<uint32_t>> g_sm;
 static std::vector<std::barrier<> *> g_bar;
 void __syncthreads() { g_bar[t_cta]->arrive_and_wait(); }
 uint32_t *emu_smem() { return g_sm[t_cta].data(); }
+// the grid kernel uses no cluster: these abort the emulation if reached
+int emu_cta_rank() { abort(); }
+void emu_cluster_sync() { abort(); }
+void *emu_map_shared(void *, int) { abort(); }
 // the kernel's wait budget is 50 ms of this clock; host threads are far slower
 // than the GPU, so the clock runs 2000 times slow
 unsigned long long emu_timer_ns()

@@ -1,12 +1,15 @@
-// Stand-in for cooperative_groups: the grid kernel's headers name cluster
-// groups, the grid path never uses them (a call aborts the emulation).
+// Stand-in for cooperative_groups in the host emulation of the kernels: the
+// cluster calls go to the emulation driver (rank of this CTA, cluster barrier,
+// the address of a word in a peer CTA's shared memory).
 #pragma once
-#include <cstdlib>
+int emu_cta_rank();
+void emu_cluster_sync();
+void *emu_map_shared(void *p, int rank);
 namespace cooperative_groups {
 struct cluster_group {
-	unsigned block_rank() const { abort(); }
-	void sync() { abort(); }
-	template <class T> T *map_shared_rank(T *, int) { abort(); }
+	unsigned block_rank() const { return (unsigned)emu_cta_rank(); }
+	void sync() { emu_cluster_sync(); }
+	template <class T> T *map_shared_rank(T *p, int r) { return (T *)emu_map_shared((void *)p, r); }
 };
 inline cluster_group this_cluster() { return {}; }
 }

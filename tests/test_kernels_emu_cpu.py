@@ -1,0 +1,118 @@
+"""The PRP kernels' own source compiled for the host and run with one host
+thread per GPU thread (tests/emu/), under AddressSanitizer and UBSan:
+
+* the grid kernel (ctwin_gb300/csrc/prp_grid.cu): every CTA of a lane at once,
+  the grid barriers and the neighbour carry publications on host atomics;
+* the one-CTA and cluster kernels (prp_kernel_impl.cuh): the CTAs of a
+  cluster at once, cluster barriers and distributed shared memory emulated.
+
+Squarings with doubling and one multiply, digits bit-exact with the oracle's C
+restatement; integer work, tolerance 0.  No GPU involved."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+from oracle import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+EMU = os.path.join(HERE, "emu")
+BUILD = os.path.join(EMU, "_build")
+CSRC = os.path.join(ROOT, "ctwin_gb300", "csrc")
+# (lg, primes, lm) shapes compiled: 2^16 on 64 CTAs of 1024 (the single-test
+# default), 2^16 on 32 CTAs of 2048 with three primes, 2^17 on 32 CTAs of 4096
+SHAPES = [(6, 2, 10), (5, 3, 11), (5, 2, 12)]
+MARK = "size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np)"
+
+
+# AddressSanitizer and UBSan on by default; CTW_EMU_FAST=1 builds without them
+SAN = [] if os.environ.get("CTW_EMU_FAST") else ["-fsanitize=address,undefined", "-fno-omit-frame-pointer"]
+
+
+def _compile(exe, sources, shapes_macro):
+    lib = O.build()
+    cmd = ["g++", "-std=c++20", "-O1", "-g", *SAN, "-I", os.path.join(EMU, "stub"), "-I", EMU, "-I", CSRC,
+           "-include", "emu_shim.h", f"-DCTW_EMU_SHAPES={shapes_macro}", "-o", exe, *sources,
+           lib, f"-Wl,-rpath,{os.path.dirname(lib)}", "-lpthread"]
+    subprocess.run(cmd, check=True, timeout=900)
+    return exe
+
+
+def _run(args):
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
+    r = subprocess.run([str(v) for v in args], capture_output=True, text=True, timeout=900, env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "status 0 mismatches square 0 mul 0" in r.stdout
+
+
+@pytest.fixture(scope="module")
+def grid_emu():
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    os.makedirs(BUILD, exist_ok=True)
+    src = open(os.path.join(CSRC, "prp_grid.cu")).read()
+    cut = src.find(MARK)
+    assert cut > 0, "prp_grid.cu: host launch code not found"
+    body = src[:cut]
+    decl = "extern __shared__ __align__(16) uint32_t sm[];"
+    assert body.count(decl) == 1
+    body = body.replace(decl, "uint32_t *sm = emu_smem();")
+    inst = "".join(f"template void prp_kernel_grid<{lg}, {np}, {lm}>(const PrpKernelArgs, const PrpGridArgs);\n"
+                   for lg, np, lm in SHAPES)
+    kern = os.path.join(BUILD, "grid_kernels.cpp")
+    with open(kern, "w") as f:
+        f.write('#include "emu_shim.h"\n' + body + inst + "}  // namespace ctw\n")
+    shapes = " ".join(f"CTW_EMU_SHAPE({lg}, {np}, {lm})" for lg, np, lm in SHAPES)
+    return _compile(os.path.join(BUILD, "grid_emu"), [kern, os.path.join(EMU, "grid_emu.cpp")], shapes)
+
+
+@pytest.mark.parametrize("ln,lm,primes,csize,b,threads", [
+    (16, 10, 2, 16, 1330358, 64),        # the 2^16 single-test shape, two primes
+    (16, 11, 3, 32, 2000000003, 64),     # three primes, b near 2^31 (128-bit carries)
+    (17, 12, 2, 8, 1330358, 32),         # 4096-coefficient CTAs
+])
+def test_grid_kernel_emulated_bit_exact(grid_emu, ln, lm, primes, csize, b, threads):
+    _run([grid_emu, ln, lm, primes, csize, b, threads])
+
+
+# (cols, lg, m12, primes, dense) instantiations of prp_kernel / prp_kernel_cols
+CLUSTER_SHAPES = [(0, 0, 0, 2, 0), (0, 0, 1, 3, 0), (1, 2, 1, 2, 0), (1, 1, 1, 3, 1), (1, 2, 0, 3, 0)]
+IMPL_MARK = "template <int LG, bool M12, bool COLS, int NP, bool DENSE = false>\nstatic cudaError_t launch_lg"
+
+
+@pytest.fixture(scope="module")
+def cluster_emu():
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    os.makedirs(BUILD, exist_ok=True)
+    src = open(os.path.join(CSRC, "prp_kernel_impl.cuh")).read()
+    cut = src.find(IMPL_MARK)
+    assert cut > 0, "prp_kernel_impl.cuh: launch_lg not found"
+    body = src[:cut]
+    decl = "extern __shared__ __align__(16) uint32_t sm[];"
+    assert body.count(decl) == 2
+    body = body.replace(decl, "uint32_t *sm = emu_smem();")
+    cu = open(os.path.join(CSRC, "prp_kernels.cu")).read()
+    i0, i1 = cu.find("size_t prp_smem_bytes("), cu.find("// Cluster splits with a kernel")
+    assert 0 < i0 < i1, "prp_kernels.cu: shared-memory / thread helpers not found"
+    tf = lambda v: "true" if v else "false"
+    inst = "".join(f"template void {'prp_kernel_cols' if c else 'prp_kernel'}<{lg}, {tf(m)}, {np}, {tf(d)}>"
+                   f"(const PrpKernelArgs);\n" for c, lg, m, np, d in CLUSTER_SHAPES)
+    kern = os.path.join(BUILD, "cluster_kernels.cpp")
+    with open(kern, "w") as f:
+        f.write('#include "emu_shim.h"\n' + body + "\n" + cu[i0:i1] + inst + "}  // namespace ctw\n")
+    shapes = " ".join(f"CTW_EMU_SHAPE({c}, {lg}, {tf(m)}, {np}, {tf(d)})" for c, lg, m, np, d in CLUSTER_SHAPES)
+    return _compile(os.path.join(BUILD, "cluster_emu"), [kern, os.path.join(EMU, "cluster_emu.cpp")], shapes)
+
+
+@pytest.mark.parametrize("ln,lg,primes,dense,csize,b0,b1", [
+    (11, 0, 2, 0, 16, 100003, 299993),       # one CTA of 2048, two primes (the twin-search degree)
+    (12, 0, 3, 0, 8, 2000000003, 65537),     # one CTA of 4096, three primes, b near 2^31
+    (14, 2, 2, 0, 32, 1330358, 70001),       # 4-CTA cluster of 4096, two primes
+    (13, 1, 3, 1, 16, 1330358, 4000037),     # 2-CTA cluster, dense three-prime build (384 threads)
+    (13, 2, 3, 0, 8, 2000000011, 100003),    # 4-CTA cluster of 2048, generic three-prime path
+])
+def test_cluster_kernels_emulated_bit_exact(cluster_emu, ln, lg, primes, dense, csize, b0, b1):
+    _run([cluster_emu, ln, lg, primes, dense, csize, b0, b1])
