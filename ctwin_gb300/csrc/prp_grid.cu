@@ -269,6 +269,38 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 		}
 	};
 
+	// The transposes: block c of prime plane pi comes from CTA c's published
+	// planes (src + c*3M + pi*M + g*MG) to dst + pi*M + c*MG.  Each thread
+	// issues up to GB = 4 16-byte L2 loads before it stores them, so that their
+	// round trips overlap (2^16 on 64 CTAs: 74.8 k -> 77.9 k squarings/s).
+	auto gather = [&](uint32_t *dst, const uint32_t *src) {
+		constexpr int NV = NP * G * MG4, GB = 4;
+		for (int v0 = tid; v0 < NV; v0 += GB * nt)
+		{
+			uint4 t[GB] = {};
+#pragma unroll
+			for (int k = 0; k < GB; ++k)
+			{
+				const int v = v0 + k * nt;
+				if (v < NV)
+				{
+					const int bx = v / MG4, o = (v - bx * MG4) * 4, pi = bx / G, c = bx - pi * G;
+					t[k] = ld_l2(src + (size_t)c * 3 * M + pi * M + g * MG + o);
+				}
+			}
+#pragma unroll
+			for (int k = 0; k < GB; ++k)
+			{
+				const int v = v0 + k * nt;
+				if (v < NV)
+				{
+					const int bx = v / MG4, o = (v - bx * MG4) * 4, pi = bx / G, c = bx - pi * G;
+					*reinterpret_cast<uint4 *>(dst + pi * M + c * MG + o) = t[k];
+				}
+			}
+		}
+	};
+
 	auto transform_and_normalize = [&](int mode, int mult) {
 		__syncthreads();
 		for (int e = tid; e < M; e += nt)
@@ -282,12 +314,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 		for (int v = tid; v < NP * M4; v += nt)
 			st_l2(gx + (size_t)g * 3 * M + 4 * v, *reinterpret_cast<const uint4 *>(XC + 4 * v));
 		gsync();
-		for (int v = tid; v < NP * G * MG4; v += nt)
-		{
-			const int pcx = v / MG4, o = (v - pcx * MG4) * 4;
-			const int pi = pcx / G, c = pcx - pi * G;
-			*reinterpret_cast<uint4 *>(XR + pi * M + c * MG + o) = ld_l2(gx + (size_t)c * 3 * M + pi * M + g * MG + o);
-		}
+		gather(XR, gx);
 		__syncthreads();
 		if constexpr (LM == 12) local_transform12<NP>(XR, TFl, TIl, SF, SI, mode, false, a, scr, scr, tid, nt);
 		else local_transform<NP>(XR, TFl, TIl, M, LM, mode, false, a, scr, scr, tid, nt);
@@ -296,12 +323,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 		for (int v = tid; v < NP * M4; v += nt)
 			st_l2(gr + (size_t)g * 3 * M + 4 * v, *reinterpret_cast<const uint4 *>(XR + 4 * v));
 		gsync();
-		for (int v = tid; v < NP * G * MG4; v += nt)
-		{
-			const int ph = v / MG4, o = (v - ph * MG4) * 4;
-			const int pi = ph / G, h = ph - pi * G;
-			*reinterpret_cast<uint4 *>(XC + pi * M + h * MG + o) = ld_l2(gr + (size_t)h * 3 * M + pi * M + g * MG + o);
-		}
+		gather(XC, gr);
 		__syncthreads();
 		cross_all<LG, LM, NP>(XC, XRT, 1, cb, a, tid, nt);
 		for (int e = tid; e < M; e += nt) garner_at<NP>(XC, M, (e / MG) * MG + (swz(cb + e % MG, sb) - cb), a, narrow);
