@@ -22,8 +22,9 @@ EMU = os.path.join(HERE, "emu")
 BUILD = os.path.join(EMU, "_build")
 CSRC = os.path.join(ROOT, "ctwin_gb300", "csrc")
 # (lg, primes, lm) shapes compiled: 2^16 on 64 CTAs of 1024 (the single-test
-# default), 2^16 on 32 CTAs of 2048 with three primes, 2^17 on 32 CTAs of 4096
-SHAPES = [(6, 2, 10), (5, 3, 11), (5, 2, 12)]
+# default), 2^16 on 32 CTAs of 2048 with three primes, 2^17 on 32 CTAs of 4096,
+# 2^18 on 128 CTAs of 2048 with three primes (the 2^18 default)
+SHAPES = [(6, 2, 10), (5, 3, 11), (5, 2, 12), (7, 3, 11)]
 MARK = "size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np)"
 
 
@@ -72,6 +73,7 @@ def grid_emu():
     (16, 10, 2, 16, 1330358, 64),        # the 2^16 single-test shape, two primes
     (16, 11, 3, 32, 2000000003, 64),     # three primes, b near 2^31 (128-bit carries)
     (17, 12, 2, 8, 1330358, 32),         # 4096-coefficient CTAs
+    (18, 11, 3, 16, 1330358, 32),        # 128 CTAs
 ])
 def test_grid_kernel_emulated_bit_exact(grid_emu, ln, lm, primes, csize, b, threads):
     _run([grid_emu, ln, lm, primes, csize, b, threads])
