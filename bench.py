@@ -709,9 +709,12 @@ def main():
     dist = None
     if world > 1:
         import torch.distributed as dist
-        import torch
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        if args.impl == "ours":
+            import torch
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")      # the reference arm runs on the host cores only
 
     if args.impl == "reference":
         rc = run_reference(args, rank, world)
