@@ -491,6 +491,10 @@ int ctw_prp_create_split(int log2_degree, int lanes, int log2_ctas, ctw_prp **ou
 	*out = nullptr;
 	if (log2_degree < 8 || log2_degree > 18) return fail(CTW_E_ARG, "log2_degree %d outside [8, 18]", log2_degree);
 	if (lanes < 1 || lanes > MAX_INLINE_LANES) return fail(CTW_E_ARG, "lanes %d outside [1, %d]", lanes, MAX_INLINE_LANES);
+	// an explicit split must have a kernel (host-only check, before the device is asked)
+	if (log2_ctas >= 0 && !(log2_ctas > MAX_LG ? prp_grid_supported(log2_ctas, log2_degree - log2_ctas)
+	                                            : prp_split_supported(log2_degree - log2_ctas, log2_ctas)))
+		return fail(CTW_E_ARG, "no kernel for degree 2^%d on 2^%d CTAs", log2_degree, log2_ctas);
 	if (ctw_device_count() == 0) return fail(CTW_E_CUDA, "no CUDA device");
 	// Degrees 2^16..2^18 default to the grid kernel with the most CTAs per lane
 	// that has a kernel (2^16: 64 of 1024 coefficients, 2^17: 64 of 2048, 2^18:

@@ -48,3 +48,22 @@ def test_create_fails_cleanly_without_gpu_or_bad_args():
     if L.ctw_device_count() == 0:
         assert L.ctw_prp_create(11, 1, ctypes.byref(h)) == -2   # CUDA error, not a crash
         assert b"no CUDA device" in L.ctw_last_error()
+
+
+def test_argument_errors_are_reported_before_the_device_is_asked():
+    """Invalid shapes give CTW_E_ARG (-1) with or without a GPU; valid ones
+    without a GPU give CTW_E_CUDA (-2).  Nothing crashes, no handle is returned."""
+    import ctypes
+    from ctwin_gb300._native import lib
+    L = lib()
+    h = ctypes.c_void_p()
+    assert L.ctw_prp_create_split(16, 1, 9, ctypes.byref(h)) == -1     # 2^16 on 512 CTAs: no kernel
+    assert L.ctw_prp_create_split(18, 1, 2, ctypes.byref(h)) == -1     # 2^18 on 4 CTAs of 65536: no kernel
+    assert L.ctw_prp_create_split(8, 1, 3, ctypes.byref(h)) == -1      # runs of 32 coefficients: none
+    assert L.ctw_pool_create(12, 4, 9, 0, 2, 0, ctypes.byref(h)) == -1
+    assert L.ctw_pool_create(12, 0, -1, 0, 2, 0, ctypes.byref(h)) == -1
+    assert not h.value
+    if L.ctw_device_count() == 0:
+        assert L.ctw_prp_create_split(16, 1, 5, ctypes.byref(h)) == -2  # the 32-CTA grid exists
+        assert L.ctw_pool_create(12, 4, -1, 0, 2, 0, ctypes.byref(h)) == -2
+        assert not h.value
