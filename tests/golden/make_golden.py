@@ -11,8 +11,10 @@ has the reference source; the outputs are committed, the GPU tests only read the
   prp16_gmp.json    degree 2^16: whole Fermat tests of small b (N+ base 2 and 3, N-),
                     and r_K = base^(E >> (L - K)) mod N+ for K = 4096 at the single-test
                     workload's b (sha256 of the residue's little-endian bytes + its low 64 bits)
+  prefix_gmp.json   the same 4096-squaring prefix at degrees 2^17 and 2^18 (the grid
+                    kernel on two and three primes), base 2
 
-Usage:  python tests/golden/make_golden.py [--skip-slow] [--only pool|big]
+Usage:  python tests/golden/make_golden.py [--skip-slow] [--only pool|big|prefix]
 """
 from __future__ import annotations
 
@@ -126,10 +128,17 @@ def pool_jobs():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-slow", action="store_true")
-    ap.add_argument("--only", choices=["pool", "big"], default=None)
+    ap.add_argument("--only", choices=["pool", "big", "prefix"], default=None)
     args = ap.parse_args()
     from oracle import oracle as O
     O.build()
+    if args.only == "prefix":
+        jobs = [(BIG_PARTIAL_B, ln, 2, BIG_PARTIAL_K) for ln in (17, 18)]
+        with mp.get_context("spawn").Pool(len(jobs)) as pool:
+            res = pool.map(partial_case, jobs)
+        json.dump(res, open(os.path.join(HERE, "prefix_gmp.json"), "w"), indent=0)
+        print("done", len(res), "prefix cases")
+        return
     if args.only == "big":
         jobs = [("partial", (BIG_PARTIAL_B, 16, base, BIG_PARTIAL_K)) for base in (2, 3)]
         jobs += [("full", j) for j in BIG_FULL]

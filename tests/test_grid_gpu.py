@@ -2,6 +2,9 @@
 launch) on the GPU: registers bit-exact with the oracle and with the cluster
 kernel, on two and three primes, one and two lanes, and partial residues of
 the real exponent against GMP.  Integer work: tolerance 0."""
+import hashlib
+import json
+import os
 import random
 
 import numpy as np
@@ -110,6 +113,30 @@ def test_grid_partial_residue_matches_gmp(native, ln, base):
         eng.square_bits(O.int_to_words(E), L - 1, K)
         dig = eng.get_int(0)[0]
     assert O.digits_to_int(dig, b) == O.powmod(base, E >> (L - K), O.n_plus(b, ln))
+
+
+@pytest.mark.parametrize("ln,primes", [(17, 2), (18, 3)])
+def test_grid_prefix_4096_matches_gmp(native, golden_dir, ln, primes):
+    """The first 4096 squarings of the single-test workload's exponent
+    (b = 1330358) on the default grid split, against GMP through a hash of the
+    whole residue (tests/golden/prefix_gmp.json)."""
+    from ctwin_gb300 import PrpEngine
+    c = next(c for c in json.load(open(os.path.join(golden_dir, "prefix_gmp.json"))) if c["n"] == ln)
+    b, K = c["b"], c["K"]
+    E = O.exponent(b, ln)
+    L = E.bit_length()
+    with PrpEngine(ln, 1) as eng:
+        assert eng.geometry()["ctas_per_lane"] == 1 << (ln - 11)
+        eng.set_b([b])
+        assert eng.prime_count == primes
+        eng.set(1)
+        eng.square_bits(O.int_to_words(E), L - 1, K)
+        dig = eng.get_int(0)[0]
+    assert all(0 <= int(v) < b for v in dig)
+    r = O.digits_to_int(dig, b)
+    raw = r.to_bytes((O.n_plus(b, ln).bit_length() + 7) // 8, "little")
+    assert f"{r & (2 ** 64 - 1):016X}" == c["low64"]
+    assert hashlib.sha256(raw).hexdigest() == c["sha256"]
 
 
 def test_grid_too_many_lanes_falls_back_to_clusters(native):
