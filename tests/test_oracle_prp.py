@@ -74,3 +74,21 @@ def test_gmp_matches_python_pow():
     for b, ln in ((1000, 8), (70001, 8)):
         N = O.n_plus(b, ln)
         assert O.powmod(3, N - 1, N) == pow(3, N - 1, N)
+
+
+@pytest.mark.parametrize("ln,b,base", [(16, 1330358, 2), (16, 1330358, 3), (17, 1048583, 2)])
+def test_square_loop_prefix_matches_gmp(ln, b, base):
+    """The oracle's left-to-right loop at the headline degrees: after K squarings
+    (digits doubled or tripled where E has a one) the register is
+    base^(E >> (L - K)) mod N+, computed by GMP."""
+    import numpy as np
+    from oracle import oracle as O
+    K = 96
+    E = O.exponent(b, ln)
+    L = E.bit_length()
+    x = np.zeros(1 << ln, dtype=np.int32)
+    x[0] = 1
+    with O.Tables(ln) as t:
+        t.square_loop(x, b, base, 16, O.int_to_words(E), L - 1, K)
+    got = O.digits_to_int(O.get_int(x, b), b)
+    assert got == O.powmod(base, E >> (L - K), O.n_plus(b, ln))
