@@ -633,7 +633,7 @@ def run_config1(args):
     t_minus = time.perf_counter() - t0
     bad = sum(1 for r in list(plus.values()) + list(minus.values()) if r["status"] != 0 or not r["gl_ok"])
     twins = [b for b in surv if plus[b]["is_prp"] and minus[b]["is_prp"]]
-    # parity sample: the GMP residues of the first 64 survivors (N+, base 3)
+    # parity sample: the survivors with a GMP residue in tests/golden (N+, base 3; the first 256)
     gold = {}
     try:
         for x in json.load(open(os.path.join(ROOT, "tests", "golden", "prp_gmp.json"))):

@@ -14,7 +14,9 @@ has the reference source; the outputs are committed, the GPU tests only read the
   prefix_gmp.json   the same 4096-squaring prefix at degrees 2^17 and 2^18 (the grid
                     kernel on two and three primes), base 2
 
-Usage:  python tests/golden/make_golden.py [--skip-slow] [--only pool|big|prefix]
+Usage:  python tests/golden/make_golden.py [--skip-slow] [--only pool|big|prefix|cfg1]
+  (--only cfg1 extends prp_gmp.json to the first 256 twin survivors at n = 11:
+   N+ base 2 and 3, N- base 2 and 3)
 """
 from __future__ import annotations
 
@@ -128,10 +130,25 @@ def pool_jobs():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-slow", action="store_true")
-    ap.add_argument("--only", choices=["pool", "big", "prefix"], default=None)
+    ap.add_argument("--only", choices=["pool", "big", "prefix", "cfg1"], default=None)
     args = ap.parse_args()
     from oracle import oracle as O
     O.build()
+    if args.only == "cfg1":
+        path = os.path.join(HERE, "prp_gmp.json")
+        old = json.load(open(path))
+        have = {(d["b"], d["n"], d["base"], d["form"] == "-") for d in old}
+        z = np.load(os.path.join(HERE, "sieve_ref.npz"))
+        meta = json.load(open(os.path.join(HERE, "sieve_files.json")))["cases"]["cfg1_twin"]
+        twin = np.unpackbits(z["cfg1_twin"], bitorder="little")[: meta["size"]]
+        surv = [meta["b_min"] + int(i) for i in np.flatnonzero(twin == 0)[:256]]
+        jobs = [(b, 11, base, minus) for b in surv for base in (2, 3) for minus in (False, True)]
+        todo = [j for j in jobs if j not in have]
+        with mp.get_context("spawn").Pool(min(8, os.cpu_count() or 1)) as pool:
+            new = pool.map(prp_case, todo)
+        json.dump(old + new, open(path, "w"), indent=0)
+        print("added", len(new), "config-1 cases")
+        return
     if args.only == "prefix":
         jobs = [(BIG_PARTIAL_B, ln, 2, BIG_PARTIAL_K) for ln in (17, 18)]
         with mp.get_context("spawn").Pool(len(jobs)) as pool:

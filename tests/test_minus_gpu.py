@@ -33,6 +33,22 @@ def test_minus_run_matches_gmp(native, n, lanes):
         assert (bool(p), int(r)) == (want_prp, want64), b
 
 
+@pytest.mark.parametrize("base", [2, 3])
+def test_minus_config1_survivors_match_gmp(native, base):
+    """N- of the first 256 twin-sieve survivors of b in [100000, 300000) at
+    n = 11, base 2 and 3, in vectors of 64 lanes."""
+    from ctwin_gb300 import PrpEngine
+    cases = minus_cases(11, base)
+    assert len(cases) == 256
+    for i in range(0, len(cases), 64):
+        part = cases[i:i + 64]
+        with PrpEngine(11, 64, base=base, minus=True) as eng:
+            prp, r64, gl = eng.run([c[0] for c in part])
+        for (b, want64, want_prp), p, r, g in zip(part, prp, r64, gl):
+            assert g, b
+            assert (bool(p), int(r)) == (want_prp, want64), b
+
+
 def test_minus_finds_prps(native):
     """Every N- PRP of the golden n = 8 list comes out as residue 1."""
     from ctwin_gb300 import prp_test

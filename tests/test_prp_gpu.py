@@ -98,18 +98,21 @@ def test_run_vs_gmp_n8(native, golden_dir):
 
 
 def test_run_vs_gmp_config1_survivors(native, golden_dir):
-    """The first 64 twin-sieve survivors of b in [100000, 300000) at n = 11."""
+    """The first 256 twin-sieve survivors of b in [100000, 300000) at n = 11,
+    base 2 and 3, in vectors of 64 lanes."""
     from ctwin_gb300 import PrpEngine
     cases = [c for c in json.load(open(os.path.join(golden_dir, "prp_gmp.json")))
              if c["n"] == 11 and c["form"] == "+"]
     for base in (2, 3):
         sel = [c for c in cases if c["base"] == base]
-        assert len(sel) == 64
-        with PrpEngine(11, 64, base=base) as eng:
-            prp, r64, gl = eng.run([c["b"] for c in sel])
-        assert gl.all()
-        assert [f"{int(r):016X}" for r in r64] == [c["res64"] for c in sel]
-        assert list(prp) == [c["prp"] for c in sel]
+        assert len(sel) == 256
+        for i in range(0, len(sel), 64):
+            part = sel[i:i + 64]
+            with PrpEngine(11, 64, base=base) as eng:
+                prp, r64, gl = eng.run([c["b"] for c in part])
+            assert gl.all()
+            assert [f"{int(r):016X}" for r in r64] == [c["res64"] for c in part]
+            assert list(prp) == [c["prp"] for c in part]
 
 
 def test_run_pads_lanes_with_last_b(native):
