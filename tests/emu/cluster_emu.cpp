@@ -4,9 +4,12 @@
 // barrier one over the cluster, and distributed shared memory maps a word to
 // the same offset in the peer CTA's buffer.  Two lanes (b given), one doubling
 // squaring and one multiply, digits compared with the oracle's C restatement
-// (bit-exact).  Test infrastructure (tests/test_kernels_emu_cpu.py).
+// (bit-exact).  With minus = 1 the registers are N- values on the degree-2D
+// transform (upper halves zero) and the digits are printed for a check of
+// x1 = mult x0^2 and out = x1 y mod N- by the caller.  Test infrastructure
+// (tests/test_kernels_emu_cpu.py).
 //
-// usage: cluster_emu <log2 D> <log2 G> <primes> <dense 0|1> <csize> <b0> <b1>
+// usage: cluster_emu <log2 D> <log2 G> <primes> <dense 0|1> <csize> <b0> <b1> [minus mult]
 #include "emu_shim.h"
 #include <barrier>
 #include <cstdio>
@@ -99,6 +102,7 @@ int main(int argc, char **argv)
 	if (argc < 8) { fprintf(stderr, "usage: cluster_emu ln lg primes dense csize b0 b1\n"); return 2; }
 	const int ln = atoi(argv[1]), lg = atoi(argv[2]), np = atoi(argv[3]), dense = atoi(argv[4]), csize = atoi(argv[5]);
 	const uint32_t bs[2] = { (uint32_t)strtoul(argv[6], nullptr, 10), (uint32_t)strtoul(argv[7], nullptr, 10) };
+	const int minus = argc > 8 ? atoi(argv[8]) : 0, mult = argc > 9 ? atoi(argv[9]) : 2;
 	const int lm = ln - lg, G = 1 << lg, lanes = 2;
 	const size_t D = (size_t)1 << ln, M = D / G;
 	Kern k = pick(lg, lm == 12, np, dense != 0);
@@ -119,12 +123,14 @@ int main(int argc, char **argv)
 		laneb[4 * l + 3] = (8.0 * D * (double)b * b < 4.611686018427388e18) ? 1 : 0;
 		for (size_t j = 0; j < D; ++j)
 		{
-			x[l * D + j] = (int32_t)(rng() % b) - (int32_t)(b / 2);
-			y[l * D + j] = (int32_t)(rng() % b) - (int32_t)(b / 2);
+			const bool upper = minus && j >= D / 2;
+			x[l * D + j] = upper ? 0 : (int32_t)(rng() % b) - (int32_t)(b / 2);
+			y[l * D + j] = upper ? 0 : (int32_t)(rng() % b) - (int32_t)(b / 2);
 		}
 	}
 	a.tf = tf.data(); a.ti = ti.data(); a.tfs = tfs.data(); a.tis = tis.data(); a.lane_b = laneb.data();
-	a.status = status.data(); a.lm = lm; a.csize = csize; a.mult = 2; a.scratch = scratch.data(); a.nprime = np;
+	a.status = status.data(); a.lm = lm; a.csize = csize; a.mult = mult; a.scratch = scratch.data(); a.nprime = np;
+	a.minus = minus;
 	// the launch's choices (launch_lg): the dense three-prime build keeps roots and
 	// Shoup tables in global memory and runs 384 threads
 	const bool dense3 = dense && np == 3;
@@ -137,6 +143,18 @@ int main(int argc, char **argv)
 	launch(k, a, lanes, G, threads, smem);
 	a.op = OP_MUL; a.reg_in = x.data(); a.reg_y = y.data(); a.reg_out = out.data(); a.count = 1;
 	launch(k, a, lanes, G, threads, smem);
+	if (minus)
+	{
+		// lanes of four lines each: x0, y, x after the squaring, x * y
+		for (int l = 0; l < lanes; ++l)
+			for (const std::vector<int32_t> *v : { &x0, &y, &x, &out })
+			{
+				for (size_t j = 0; j < D; ++j) printf("%d ", (*v)[l * D + j]);
+				printf("\n");
+			}
+		printf("status %u\n", status[0]);
+		return status[0] ? 1 : 0;
+	}
 	orc_prp_tables *t = orc_prp_tables_create(ln);
 	int bad = 0, bad2 = 0;
 	for (int l = 0; l < lanes; ++l)

@@ -80,7 +80,7 @@ def test_grid_kernel_emulated_bit_exact(grid_emu, ln, lm, primes, csize, b, thre
 
 
 # (cols, lg, m12, primes, dense) instantiations of prp_kernel / prp_kernel_cols
-CLUSTER_SHAPES = [(0, 0, 0, 2, 0), (0, 0, 1, 3, 0), (1, 2, 1, 2, 0), (1, 1, 1, 3, 1), (1, 2, 0, 3, 0)]
+CLUSTER_SHAPES = [(0, 0, 0, 2, 0), (0, 0, 1, 3, 0), (1, 2, 1, 2, 0), (1, 1, 1, 3, 1), (1, 2, 0, 3, 0), (0, 0, 1, 2, 0)]
 IMPL_MARK = "template <int LG, bool M12, bool COLS, int NP, bool DENSE = false>\nstatic cudaError_t launch_lg"
 
 
@@ -118,3 +118,26 @@ def cluster_emu():
 ])
 def test_cluster_kernels_emulated_bit_exact(cluster_emu, ln, lg, primes, dense, csize, b0, b1):
     _run([cluster_emu, ln, lg, primes, dense, csize, b0, b1])
+
+
+@pytest.mark.parametrize("primes,mult", [(2, 2), (2, 3), (3, 3)])
+def test_minus_kernel_emulated(cluster_emu, primes, mult):
+    """N- of degree 2^11 on the 4096-coefficient transform (the fold of the
+    upper half in the kernel): after one squaring with the base multiplier the
+    register is mult x0^2 mod N-, after the multiply x1 y mod N-; the upper
+    halves stay zero."""
+    b0, b1 = 100019, 299993
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
+    r = subprocess.run([str(v) for v in (cluster_emu, 12, 0, primes, 0, 16, b0, b1, 1, mult)],
+                       capture_output=True, text=True, timeout=900, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = r.stdout.strip().split("\n")
+    assert lines[-1] == "status 0"
+    Dn = 1 << 11
+    for lane, b in enumerate((b0, b1)):
+        x0, y, x1, out = ([int(v) for v in lines[4 * lane + k].split()] for k in range(4))
+        N = b ** Dn - b ** (Dn // 2) - 1
+        assert not any(x1[Dn:]) and not any(out[Dn:])
+        want1 = mult * O.digits_to_int(x0, b) ** 2 % N
+        assert O.digits_to_int(x1, b) % N == want1
+        assert O.digits_to_int(out, b) % N == want1 * O.digits_to_int(y, b) % N
