@@ -1,13 +1,14 @@
-// Grid kernel: one candidate of degree D = G * 4096 spread over G = 2^LG CTAs
-// of one cooperative launch (G = 32 for D = 2^17, 64 for D = 2^18), more SMs
-// than a thread-block cluster (at most 16) can give one candidate.
+// Grid kernel: one candidate of degree D = G * M spread over G = 2^LG CTAs of
+// M = 2^LM coefficients in one cooperative launch (the defaults: 64 CTAs of
+// 1024 for D = 2^16, 64 of 2048 for 2^17, 128 of 2048 for 2^18), more SMs than
+// a thread-block cluster (at most 16) can give one candidate.
 //
 // The residue rests in shared memory in the column layout of the cluster
 // kernel: CTA g keeps, for every row block h < G, the run of coefficients
-// [h*4096 + g*MG, h*4096 + (g+1)*MG), MG = 4096/G.  Per squaring:
+// [h*M + g*MG, h*M + (g+1)*MG), MG = M/G.  Per squaring:
 //   digits -> residues; the LG cross levels of every column (radix-8/4 passes
 //   in shared memory); publish the columns to L2; grid barrier A; gather row
-//   block g (16-byte loads that bypass L1); the 4096-coefficient local
+//   block g (16-byte loads that bypass L1); the M-coefficient local
 //   transform, pointwise square and inverse; publish the row; grid barrier B;
 //   gather the columns; inverse cross levels; Garner; carry over the runs;
 //   publish the run-end carries; wait for those of the preceding CTA only;
