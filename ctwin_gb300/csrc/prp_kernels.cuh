@@ -88,7 +88,8 @@ struct PrpGridArgs {
 	const uint32_t *xr;         // [3][2][128] cross-level roots (Montgomery): forward, inverse
 };
 // Grid splits with a kernel: 2^lg CTAs of 2^lm coefficients for (lg, lm) =
-// (5, 12), (6, 12) (D = 2^17, 2^18) and (5, 11), (6, 11), (7, 11) (D = 2^16..2^18).
+// (5, 12), (6, 12) (D = 2^17, 2^18), (5, 11), (6, 11), (7, 11) (D = 2^16..2^18)
+// and (6, 10) (D = 2^16).
 bool prp_grid_supported(int lg, int lm);
 // Threads of a grid CTA: one per (prime, radix-16 group) for 4096 and 2048
 // coefficients, one per (prime, radix-8 group) for 1024 (measured: 2^16 +3 %
