@@ -1,4 +1,4 @@
-"""The grid kernel (degrees 2^17 and 2^18 on 32 / 64 CTAs of one cooperative
+"""The grid kernel (degrees 2^16..2^18 on 32 to 128 CTAs of one cooperative
 launch) on the GPU: registers bit-exact with the oracle and with the cluster
 kernel, on two and three primes, one and two lanes, and partial residues of
 the real exponent against GMP.  Integer work: tolerance 0."""
