@@ -173,7 +173,7 @@ def cpu_squarings_per_s(threads: int, seconds: float = 12.0):
         i = i0
         n = 0
         while time.perf_counter() < stop:
-            tabs.square_loop(x, b, 2, 16, words, i, 4)
+            tabs.square_loop(x, b, 3, 16, words, i, 4)        # Fermat base 3
             i -= 4
             n += 4
         with lock:
@@ -738,7 +738,7 @@ def main():
 
     b, E, i0, B_GL, words = workload(rank)
     D = 1 << LOG2_D
-    eng = PrpEngine(LOG2_D, 1, log2_ctas=args.log2_ctas)
+    eng = PrpEngine(LOG2_D, 1, base=3, log2_ctas=args.log2_ctas)          # Fermat base 3
     eng.set_b([b])
     eng.set(1)
     eng.copy(1, 0)
@@ -845,8 +845,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": f"single large PRP, degree 2^{LOG2_D} (N = b^{1 << LOG2_D} - b^{1 << (LOG2_D - 1)} + 1), "
-                               "b uniform in [2^20, 2^21) seed 1, one candidate per launch sequence",
-                   "degree": D, "b": b, "exponent_bits": i0 + 1, "squarings_per_step": B_GL,
+                               "b uniform in [2^20, 2^21) seed 1, Fermat base 3, one candidate per launch sequence",
+                   "degree": D, "b": b, "base": 3, "exponent_bits": i0 + 1, "squarings_per_step": B_GL,
                    "step": "one Gerbicz-Li block: B_GL resident squarings + one multiply",
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}",
                    "ctas_per_candidate": geo["ctas_per_lane"], "threads_per_cta": geo["threads"],
