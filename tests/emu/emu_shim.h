@@ -1,8 +1,9 @@
-// Host stand-ins for the CUDA built-ins the grid kernel (prp_grid.cu) uses, so
-// that its source compiles with g++ and runs with one host thread per GPU
-// thread (test infrastructure: tests/test_kernels_emu_cpu.py).  Shared memory,
-// __syncthreads and the clock come from the driver (grid_emu.cpp); global
-// atomics and fences map to the host's sequentially consistent atomics.
+// Host stand-ins for the CUDA built-ins the PRP kernels use, so that their
+// source compiles with g++ and runs with one host thread per GPU thread (test
+// infrastructure: tests/test_kernels_emu_cpu.py).  Shared memory, __syncthreads
+// and the clock come from the emulation programs (grid_emu.cpp,
+// cluster_emu.cpp); global atomics and fences map to the host's sequentially
+// consistent atomics.
 #pragma once
 #include <algorithm>
 #include <cstdint>

@@ -1,5 +1,5 @@
 // Stand-in for cooperative_groups in the host emulation of the kernels: the
-// cluster calls go to the emulation driver (rank of this CTA, cluster barrier,
+// cluster calls go to the emulation program (rank of this CTA, cluster barrier,
 // the address of a word in a peer CTA's shared memory).
 #pragma once
 int emu_cta_rank();
