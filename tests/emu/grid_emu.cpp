@@ -5,7 +5,7 @@
 // multiplies it by a second one, and compares the digits with the oracle's C
 // restatement (bit-exact).  Test infrastructure (tests/test_kernels_emu_cpu.py).
 //
-// usage: grid_emu <log2 D> <log2 M> <primes> <csize> <b> <threads per CTA>
+// usage: grid_emu <log2 D> <log2 M> <primes> <csize> <b> <threads per CTA> [base multiplier, 2]
 #include "emu_shim.h"
 #include <barrier>
 #include <chrono>
@@ -111,6 +111,7 @@ int main(int argc, char **argv)
 	const int ln = atoi(argv[1]), lm = atoi(argv[2]), np = atoi(argv[3]), csize = atoi(argv[4]);
 	const uint32_t bs = (uint32_t)strtoul(argv[5], nullptr, 10);
 	const int nth = atoi(argv[6]);
+	const int mult = argc > 7 ? atoi(argv[7]) : 2;
 	const int lg = ln - lm, G = 1 << lg;
 	const size_t D = (size_t)1 << ln, M = (size_t)1 << lm;
 	Kern k = pick(lg, lm, np);
@@ -133,7 +134,7 @@ int main(int argc, char **argv)
 		y[j] = (int32_t)(rng() % bs) - (int32_t)(bs / 2);
 	}
 	a.tf = tf.data(); a.ti = ti.data(); a.tfs = tfs.data(); a.tis = tis.data(); a.lane_b = laneb.data();
-	a.status = status.data(); a.lm = lm; a.csize = csize; a.mult = 2; a.scratch = scratch.data(); a.nprime = np;
+	a.status = status.data(); a.lm = lm; a.csize = csize; a.mult = mult; a.scratch = scratch.data(); a.nprime = np;
 	a.tw_smem = grid_words(lg, lm, 1, np) * 4 <= 227 * 1024 ? 1 : 0;
 	if (lm <= 11 && ((1 << lm) >> lg) < 32) a.swz_b = 20;   // the launch's swizzle for 16-word runs
 	PrpGridArgs ga{ gx.data(), gr.data(), gc.data(), bar.data(), xr.data() };
@@ -146,8 +147,8 @@ int main(int argc, char **argv)
 	launch(k, a, ga, G, nth, words);
 	orc_prp_tables *t = orc_prp_tables_create(ln);
 	std::vector<int32_t> r = x0;
-	orc_square_dup(t, r.data(), bs, 2, csize);
-	orc_square_dup(t, r.data(), bs, 2, csize);
+	orc_square_dup(t, r.data(), bs, mult, csize);
+	orc_square_dup(t, r.data(), bs, mult, csize);
 	int bad = 0, bad2 = 0;
 	for (size_t j = 0; j < D; ++j) bad += r[j] != x[j];
 	orc_mul(t, r.data(), y.data(), bs, csize);

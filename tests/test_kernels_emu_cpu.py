@@ -69,14 +69,15 @@ def grid_emu():
     return _compile(os.path.join(BUILD, "grid_emu"), [kern, os.path.join(EMU, "grid_emu.cpp")], shapes)
 
 
-@pytest.mark.parametrize("ln,lm,primes,csize,b,threads", [
-    (16, 10, 2, 16, 1330358, 64),        # the 2^16 single-test shape, two primes
-    (16, 11, 3, 32, 2000000003, 64),     # three primes, b near 2^31 (128-bit carries)
-    (17, 12, 2, 8, 1330358, 32),         # 4096-coefficient CTAs
-    (18, 11, 3, 16, 1330358, 32),        # 128 CTAs
+@pytest.mark.parametrize("ln,lm,primes,csize,b,threads,mult", [
+    (16, 10, 2, 16, 1330358, 64, 3),     # the 2^16 single-test shape, two primes, Fermat base 3
+    (16, 10, 2, 8, 1330358, 64, 2),
+    (16, 11, 3, 32, 2000000003, 64, 2),  # three primes, b near 2^31 (128-bit carries)
+    (17, 12, 2, 8, 1330358, 32, 2),      # 4096-coefficient CTAs
+    (18, 11, 3, 16, 1330358, 32, 3),     # 128 CTAs
 ])
-def test_grid_kernel_emulated_bit_exact(grid_emu, ln, lm, primes, csize, b, threads):
-    _run([grid_emu, ln, lm, primes, csize, b, threads])
+def test_grid_kernel_emulated_bit_exact(grid_emu, ln, lm, primes, csize, b, threads, mult):
+    _run([grid_emu, ln, lm, primes, csize, b, threads, mult])
 
 
 # (cols, lg, m12, primes, dense) instantiations of prp_kernel / prp_kernel_cols
