@@ -1,0 +1,70 @@
+// Host emulation of the sieve path (ctwin_gb300/csrc/sieve.cu, compiled with
+// sieve_shim.h): runs ctw_sieve_run on the CPU and prints the struck bitmap
+// and the last p, for a comparison with the oracle's sieve by the caller.
+// Test infrastructure (tests/test_kernels_emu_cpu.py).
+//
+// usage: sieve_emu <n> <b_min> <b_max> <p_min> <p_max> <mode +1|-1>
+#include "sieve_shim.h"
+#include "../../include/ctwin_gb300.h"
+
+thread_local dim3 threadIdx, blockIdx;
+dim3 blockDim, gridDim;
+static std::barrier<> *g_bar = nullptr;
+static std::vector<uint32_t> g_dyn;
+void __syncthreads() { g_bar->arrive_and_wait(); }
+uint32_t *emu_dyn_smem() { return g_dyn.data(); }
+int emu_sms() { return 2; }
+
+// CTAs one after another (their static shared variables are plain statics),
+// the threads of a CTA at once
+void emu_run_blocks(const EmuCfg &c, void (*body)(void *), void *ctx)
+{
+	gridDim = c.grid;
+	blockDim = c.block;
+	const unsigned nt = c.block.x * c.block.y * c.block.z;
+	for (unsigned bz = 0; bz < c.grid.z; ++bz)
+		for (unsigned by = 0; by < c.grid.y; ++by)
+			for (unsigned bx = 0; bx < c.grid.x; ++bx)
+			{
+				g_dyn.assign(c.smem / 4 + 1, 0xdeadbeefu);
+				std::barrier<> bar(nt);
+				g_bar = &bar;
+				std::vector<std::thread> th;
+				th.reserve(nt);
+				for (unsigned t = 0; t < nt; ++t)
+					th.emplace_back([=] {
+						threadIdx = dim3(t % c.block.x, (t / c.block.x) % c.block.y, t / (c.block.x * c.block.y));
+						blockIdx = dim3(bx, by, bz);
+						body(ctx);
+					});
+				for (auto &x : th) x.join();
+			}
+}
+
+namespace ctw {
+int fail(int code, const char *fmt, ...)
+{
+	va_list ap;
+	va_start(ap, fmt);
+	vfprintf(stderr, fmt, ap);
+	va_end(ap);
+	fprintf(stderr, "\n");
+	return code;
+}
+}
+extern "C" int ctw_device_count(void) { return 1; }
+
+int main(int argc, char **argv)
+{
+	if (argc < 7) { fprintf(stderr, "usage: sieve_emu n b_min b_max p_min p_max mode\n"); return 2; }
+	const int n = atoi(argv[1]), mode = atoi(argv[6]);
+	const uint64_t b_min = strtoull(argv[2], nullptr, 10), b_max = strtoull(argv[3], nullptr, 10);
+	const uint64_t p_min = strtoull(argv[4], nullptr, 10), p_max = strtoull(argv[5], nullptr, 10);
+	std::vector<uint32_t> words((b_max - b_min + 1 + 31) / 32, 0);
+	uint64_t p_last = 0;
+	const int rc = ctw_sieve_run(n, b_min, b_max, p_min, p_max, mode, words.data(), &p_last);
+	printf("rc %d p_last %llu\n", rc, (unsigned long long)p_last);
+	for (uint32_t w : words) printf("%u ", w);
+	printf("\n");
+	return rc ? 1 : 0;
+}

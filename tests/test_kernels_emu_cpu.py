@@ -4,11 +4,15 @@ thread per GPU thread (tests/emu/), under AddressSanitizer and UBSan:
 * the grid kernel (ctwin_gb300/csrc/prp_grid.cu): every CTA of a lane at once,
   the grid barriers and the neighbour carry publications on host atomics;
 * the one-CTA and cluster kernels (prp_kernel_impl.cuh): the CTAs of a
-  cluster at once, cluster barriers and distributed shared memory emulated.
+  cluster at once, cluster barriers and distributed shared memory emulated;
+* the whole sieve path (sieve.cu: host driver and kernels, ctw_sieve_run) on
+  a stand-in CUDA runtime, CTAs one after another.
 
 Squarings with doubling and one multiply, digits bit-exact with the oracle's C
-restatement; integer work, tolerance 0.  No GPU involved."""
+restatement; struck bitmaps and last p equal to the oracle's sieve; integer
+work, tolerance 0.  No GPU involved."""
 import os
+import re
 import shutil
 import subprocess
 
@@ -142,3 +146,49 @@ def test_minus_kernel_emulated(cluster_emu, primes, mult):
         want1 = mult * O.digits_to_int(x0, b) ** 2 % N
         assert O.digits_to_int(x1, b) % N == want1
         assert O.digits_to_int(out, b) % N == want1 * O.digits_to_int(y, b) % N
+
+
+SIEVE_LAUNCH = re.compile(r"([A-Za-z_]\w*(?:<[^<>;()]*>)?)<<<(.*?)>>>\(")
+
+
+@pytest.fixture(scope="module")
+def sieve_emu():
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    os.makedirs(BUILD, exist_ok=True)
+    src = open(os.path.join(CSRC, "sieve.cu")).read()
+    decl = "extern __shared__ uint32_t sbits[];"
+    assert src.count(decl) == 2
+    src = src.replace(decl, "uint32_t *sbits = emu_dyn_smem();")
+    src, k = SIEVE_LAUNCH.subn(lambda m: f"emu_launch({m.group(1)}, EmuCfg{{{m.group(2)}}})(", src)
+    assert k > 0 and "<<<" not in src
+    gen = os.path.join(BUILD, "sieve_src.cpp")
+    with open(gen, "w") as f:
+        f.write(src)
+    exe = os.path.join(BUILD, "sieve_emu")
+    cmd = ["g++", "-std=c++20", "-O1", "-g", *SAN, "-I", os.path.join(EMU, "sieve_stub"), "-I", EMU, "-I", CSRC,
+           "-o", exe, gen, os.path.join(EMU, "sieve_emu.cpp"), "-lpthread"]
+    subprocess.run(cmd, check=True, timeout=900)
+    return exe
+
+
+@pytest.mark.parametrize("n,b_min,b_max,p_min,p_max,mode", [
+    (8, 2, 2000, 769, 10 ** 6, 1),
+    (8, 2, 2, 11, 10 ** 5, -1),                                  # a single b
+    (12, 5, 20000, 11, 10 ** 6, -1),                             # 32-bit Montgomery path
+    (11, 2, 10 ** 6, 2 ** 32 - 10 ** 7, 2 ** 32 + 10 ** 7, 1),   # p across 2^32
+    (12, 5, 20000, 2 ** 32 - 10 ** 6, 2 ** 32 + 10 ** 6, -1),    # 64-bit path of the - form
+])
+def test_sieve_emulated_matches_oracle(sieve_emu, n, b_min, b_max, p_min, p_max, mode):
+    import numpy as np
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
+    r = subprocess.run([str(v) for v in (sieve_emu, n, b_min, b_max, p_min, p_max, mode)],
+                       capture_output=True, text=True, timeout=900, env=env)
+    assert r.returncode == 0, r.stdout[:500] + r.stderr[-2000:]
+    head, words = r.stdout.strip().split("\n")[:2]
+    p_last = int(head.split()[3])
+    w = np.array([int(v) for v in words.split()], dtype=np.uint32)
+    got = np.unpackbits(w.view(np.uint8), bitorder="little")[: b_max - b_min + 1]
+    want, want_last = O.sieve(n, b_min, b_max, p_min, p_max, mode, threads=8)
+    assert np.array_equal(got, want)
+    assert p_last == want_last
