@@ -4,6 +4,10 @@
 // Test infrastructure (tests/test_kernels_emu_cpu.py).
 //
 // usage: sieve_emu <n> <b_min> <b_max> <p_min> <p_max> <mode +1|-1>
+//        sieve_emu case <n> <b_min> <b_max> <p_max_pos> <p_max_neg> <mode 1|0|-1> <dir>
+// The second form runs a reference sieve case as the reference's Sieve class
+// does (+ from 3*2^n + 1, - from 11, each pass raising its last p) and writes
+// sv_*.dat / cand_*.txt into dir with ctw_sieve_write_files.
 #include "sieve_shim.h"
 #include "../../include/ctwin_gb300.h"
 
@@ -54,8 +58,24 @@ int fail(int code, const char *fmt, ...)
 }
 extern "C" int ctw_device_count(void) { return 1; }
 
+static int run_case(char **argv)
+{
+	const int n = atoi(argv[2]), mode = atoi(argv[7]);
+	const uint64_t b_min = strtoull(argv[3], nullptr, 10), b_max = strtoull(argv[4], nullptr, 10);
+	const uint64_t pmax_pos = strtoull(argv[5], nullptr, 10), pmax_neg = strtoull(argv[6], nullptr, 10);
+	std::vector<uint32_t> words((b_max - b_min + 1 + 31) / 32, 0);
+	uint64_t p_pos = 3 * (1ull << n) + 1, p_neg = 11;
+	int rc = 0;
+	if (mode >= 0) rc = ctw_sieve_run(n, b_min, b_max, p_pos, pmax_pos, 1, words.data(), &p_pos);
+	if (!rc && mode <= 0) rc = ctw_sieve_run(n, b_min, b_max, p_neg, pmax_neg, -1, words.data(), &p_neg);
+	if (!rc) rc = ctw_sieve_write_files(n, b_min, b_max, words.data(), p_pos, p_neg, argv[8]);
+	printf("rc %d p_last %llu %llu\n", rc, (unsigned long long)p_pos, (unsigned long long)p_neg);
+	return rc ? 1 : 0;
+}
+
 int main(int argc, char **argv)
 {
+	if (argc >= 9 && strcmp(argv[1], "case") == 0) return run_case(argv);
 	if (argc < 7) { fprintf(stderr, "usage: sieve_emu n b_min b_max p_min p_max mode\n"); return 2; }
 	const int n = atoi(argv[1]), mode = atoi(argv[6]);
 	const uint64_t b_min = strtoull(argv[2], nullptr, 10), b_max = strtoull(argv[3], nullptr, 10);

@@ -192,3 +192,28 @@ def test_sieve_emulated_matches_oracle(sieve_emu, n, b_min, b_max, p_min, p_max,
     want, want_last = O.sieve(n, b_min, b_max, p_min, p_max, mode, threads=8)
     assert np.array_equal(got, want)
     assert p_last == want_last
+
+
+@pytest.mark.parametrize("name", ["n8_small", "n9_small"])
+def test_sieve_emulated_matches_reference_files(sieve_emu, golden_dir, name, tmp_path):
+    """A reference sieve case run through the emulated product path: the last p
+    of each form and the md5 of the sv_*.dat / cand_*.txt files equal the
+    reference CPU sieve's own (tests/golden/sieve_files.json)."""
+    import hashlib
+    import json
+    meta = json.load(open(os.path.join(golden_dir, "sieve_files.json")))
+    m = meta["cases"][name]
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
+    r = subprocess.run([str(v) for v in (sieve_emu, "case", m["n"], m["b_min"], m["b_max"], m["p_max_pos"],
+                                         m["p_max_neg"], m["mode"], tmp_path)],
+                       capture_output=True, text=True, timeout=900, env=env)
+    assert r.returncode == 0, r.stdout[:500] + r.stderr[-2000:]
+    _, _, _, p_pos, p_neg = r.stdout.split()[:5]
+    if m["mode"] >= 0:
+        assert int(p_pos) == m["p_last_pos"]
+    if m["mode"] <= 0:
+        assert int(p_neg) == m["p_last_neg"]
+    files = meta["files"][name]
+    assert files
+    for fname, md5 in files.items():
+        assert hashlib.md5((tmp_path / fname).read_bytes()).hexdigest() == md5, fname
