@@ -5,6 +5,7 @@
 //
 // usage: sieve_emu <n> <b_min> <b_max> <p_min> <p_max> <mode +1|-1>
 //        sieve_emu case <n> <b_min> <b_max> <p_max_pos> <p_max_neg> <mode 1|0|-1> <dir>
+//        sieve_emu factors <n> <k_begin> <k_end> <mode +1|-1> <b_max>
 // The second form runs a reference sieve case as the reference's Sieve class
 // does (+ from 3*2^n + 1, - from 11, each pass raising its last p) and writes
 // sv_*.dat / cand_*.txt into dir with ctw_sieve_write_files.
@@ -73,9 +74,25 @@ static int run_case(char **argv)
 	return rc ? 1 : 0;
 }
 
+// ctw_sieve_factors: prints the pair count, then "p b" per line
+static int run_factors(char **argv)
+{
+	const int n = atoi(argv[2]), mode = atoi(argv[5]);
+	const uint64_t k_b = strtoull(argv[3], nullptr, 10), k_e = strtoull(argv[4], nullptr, 10);
+	const uint64_t b_max = strtoull(argv[6], nullptr, 10), cap = 1 << 20;
+	std::vector<uint64_t> pairs(2 * cap);
+	uint64_t count = 0;
+	const int rc = ctw_sieve_factors(n, k_b, k_e, mode, b_max, pairs.data(), cap, &count);
+	printf("rc %d count %llu\n", rc, (unsigned long long)count);
+	for (uint64_t i = 0; i < count && !rc; ++i)
+		printf("%llu %llu\n", (unsigned long long)pairs[2 * i], (unsigned long long)pairs[2 * i + 1]);
+	return rc ? 1 : 0;
+}
+
 int main(int argc, char **argv)
 {
 	if (argc >= 9 && strcmp(argv[1], "case") == 0) return run_case(argv);
+	if (argc >= 7 && strcmp(argv[1], "factors") == 0) return run_factors(argv);
 	if (argc < 7) { fprintf(stderr, "usage: sieve_emu n b_min b_max p_min p_max mode\n"); return 2; }
 	const int n = atoi(argv[1]), mode = atoi(argv[6]);
 	const uint64_t b_min = strtoull(argv[2], nullptr, 10), b_max = strtoull(argv[3], nullptr, 10);

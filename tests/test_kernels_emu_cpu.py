@@ -217,3 +217,32 @@ def test_sieve_emulated_matches_reference_files(sieve_emu, golden_dir, name, tmp
     assert files
     for fname, md5 in files.items():
         assert hashlib.md5((tmp_path / fname).read_bytes()).hexdigest() == md5, fname
+
+
+@pytest.mark.parametrize("mode", [1, -1])
+def test_sieve_factors_emulated(sieve_emu, mode):
+    """ctw_sieve_factors (the GPU sieve's factor pairs) on the emulated path:
+    every pair divides, pairs are sorted by p, and the set of b is the set the
+    oracle's sieve strikes over the same primes."""
+    import numpy as np
+    from ctwin_gb300.gfsieve import divides
+    n, b_max = 8, 1 << 16
+    if mode > 0:
+        k_b, k_e = 1 << 14, (1 << 14) + (1 << 10)
+        p_min, p_max = 3 * (k_b << n) + 1, 3 * ((k_e - 1) << n) + 1
+    else:
+        k_b, k_e = 1 << 16, (1 << 16) + (1 << 10)
+        p_min, p_max = 10 * k_b, 10 * (k_e - 1)
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
+    r = subprocess.run([str(v) for v in (sieve_emu, "factors", n, k_b, k_e, mode, b_max)],
+                       capture_output=True, text=True, timeout=900, env=env)
+    assert r.returncode == 0, r.stdout[:500] + r.stderr[-2000:]
+    lines = r.stdout.strip().split("\n")
+    count = int(lines[0].split()[3])
+    pairs = [tuple(map(int, l.split())) for l in lines[1:1 + count]]
+    assert count > 0 and len(pairs) == count
+    assert all(p > b_max for p, _ in pairs)
+    assert all(divides(p, b, n, mode) for p, b in pairs)
+    assert all(pairs[i][0] <= pairs[i + 1][0] for i in range(count - 1))
+    bits, _ = O.sieve(n, 2, b_max, p_min, p_max, mode, threads=8)
+    assert {b for _, b in pairs} == {int(b) for b in np.flatnonzero(bits) + 2}
