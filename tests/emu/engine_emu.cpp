@@ -1,0 +1,94 @@
+// Host emulation of the PRP engine (prp_engine.cu with the kernels of
+// prp_kernels.cu, prp_kernels_np2.cu and prp_grid.cu on the stand-in runtime
+// of engine_stub/cuda_runtime.h): whole Fermat tests through ctw_prp_run on
+// the CPU; prints, per lane, b, the PRP flag, RES64 and the Gerbicz-Li check.
+// Test infrastructure (tests/test_kernels_emu_cpu.py).
+//
+// usage: engine_emu <log2 D> <base 2|3> <minus 0|1> <b> [<b> ...]
+#include "emu_shim.h"
+#include <barrier>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <memory>
+#include <thread>
+#include <vector>
+#include "cuda_runtime.h"
+#include "../../include/ctwin_gb300.h"
+
+thread_local dim3 threadIdx, blockIdx;
+thread_local int t_cta;
+dim3 blockDim, gridDim;
+static std::vector<std::vector<uint32_t>> g_sm;
+static std::vector<std::unique_ptr<std::barrier<>>> g_bar;
+static std::unique_ptr<std::barrier<>> g_cbar;
+void __syncthreads() { g_bar[t_cta]->arrive_and_wait(); }
+uint32_t *emu_smem() { return g_sm[t_cta].data(); }
+int emu_cta_rank() { return t_cta; }
+void emu_cluster_sync() { g_cbar->arrive_and_wait(); }
+void *emu_map_shared(void *p, int r)
+{
+	const char *base = (const char *)g_sm[t_cta].data();
+	const ptrdiff_t off = (const char *)p - base;
+	if (off < 0 || (size_t)off >= g_sm[t_cta].size() * 4 || r < 0 || (size_t)r >= g_sm.size())
+	{
+		fprintf(stderr, "map_shared_rank: pointer outside shared memory or rank out of range\n");
+		abort();
+	}
+	return (char *)g_sm[r].data() + off;
+}
+unsigned long long emu_timer_ns()
+{
+	using namespace std::chrono;
+	return (unsigned long long)duration_cast<nanoseconds>(steady_clock::now().time_since_epoch()).count() / 2000;
+}
+
+// CTAs in groups (a cluster, or the whole cooperative grid) that run at once;
+// groups one after another
+void emu_run_ctas(dim3 grid, dim3 block, size_t smem, int group, void (*body)(void *), void *ctx)
+{
+	gridDim = grid;
+	blockDim = block;
+	const unsigned nt = block.x * block.y * block.z, nb = grid.x * grid.y * grid.z;
+	if (group < 1) group = 1;
+	for (unsigned g0 = 0; g0 < nb; g0 += (unsigned)group)
+	{
+		const unsigned ng = std::min<unsigned>((unsigned)group, nb - g0);
+		g_sm.assign(ng, std::vector<uint32_t>(smem / 4 + 4, 0xdeadbeefu));
+		g_bar.clear();
+		for (unsigned c = 0; c < ng; ++c) g_bar.emplace_back(new std::barrier<>(nt));
+		g_cbar.reset(new std::barrier<>(ng * nt));
+		std::vector<std::thread> th;
+		th.reserve((size_t)ng * nt);
+		for (unsigned c = 0; c < ng; ++c)
+			for (unsigned t = 0; t < nt; ++t)
+				th.emplace_back([=] {
+					t_cta = (int)c;
+					const unsigned b = g0 + c;
+					threadIdx = dim3(t % block.x, (t / block.x) % block.y, t / (block.x * block.y));
+					blockIdx = dim3(b % grid.x, (b / grid.x) % grid.y, b / (grid.x * grid.y));
+					body(ctx);
+				});
+		for (auto &x : th) x.join();
+	}
+}
+
+int main(int argc, char **argv)
+{
+	if (argc < 5) { fprintf(stderr, "usage: engine_emu ln base minus b...\n"); return 2; }
+	const int ln = atoi(argv[1]), base = atoi(argv[2]), minus = atoi(argv[3]);
+	std::vector<uint32_t> bs;
+	for (int i = 4; i < argc; ++i) bs.push_back((uint32_t)strtoul(argv[i], nullptr, 10));
+	const int lanes = (int)bs.size();
+	ctw_prp *h = nullptr;
+	int rc = minus ? ctw_prp_create_minus(ln, lanes, &h) : ctw_prp_create(ln, lanes, &h);
+	if (!rc) rc = ctw_prp_set_base(h, (uint32_t)base);
+	std::vector<uint8_t> prp(lanes), gl(lanes);
+	std::vector<uint64_t> r64(lanes);
+	if (!rc) rc = ctw_prp_run(h, bs.data(), lanes, prp.data(), r64.data(), gl.data());
+	if (rc) fprintf(stderr, "error %d: %s\n", rc, ctw_last_error());
+	for (int l = 0; l < lanes && !rc; ++l)
+		printf("%u %d %016llX %d\n", bs[(size_t)l], prp[(size_t)l], (unsigned long long)r64[(size_t)l], gl[(size_t)l]);
+	if (h) ctw_prp_destroy(h);
+	return rc ? 1 : 0;
+}

@@ -6,7 +6,10 @@ thread per GPU thread (tests/emu/), under AddressSanitizer and UBSan:
 * the one-CTA and cluster kernels (prp_kernel_impl.cuh): the CTAs of a
   cluster at once, cluster barriers and distributed shared memory emulated;
 * the whole sieve path (sieve.cu: host driver and kernels, ctw_sieve_run) on
-  a stand-in CUDA runtime, CTAs one after another.
+  a stand-in CUDA runtime, CTAs one after another;
+* the PRP engine's whole test (prp_engine.cu and its kernels, ctw_prp_run:
+  exponent, bit loop, Gerbicz-Li check, canonical digits, RES64) on a
+  stand-in runtime that runs clusters and cooperative grids on host threads.
 
 Squarings with doubling and one multiply, digits bit-exact with the oracle's C
 restatement; struck bitmaps and last p equal to the oracle's sieve; integer
@@ -75,7 +78,6 @@ def grid_emu():
 
 @pytest.mark.parametrize("ln,lm,primes,csize,b,threads,mult", [
     (16, 10, 2, 16, 1330358, 64, 3),     # the 2^16 single-test shape, two primes, Fermat base 3
-    (16, 10, 2, 8, 1330358, 64, 2),
     (16, 11, 3, 32, 2000000003, 64, 2),  # three primes, b near 2^31 (128-bit carries)
     (17, 12, 2, 8, 1330358, 32, 2),      # 4096-coefficient CTAs
     (18, 11, 3, 16, 1330358, 32, 3),     # 128 CTAs
@@ -246,3 +248,51 @@ def test_sieve_factors_emulated(sieve_emu, mode):
     assert all(pairs[i][0] <= pairs[i + 1][0] for i in range(count - 1))
     bits, _ = O.sieve(n, 2, b_max, p_min, p_max, mode, threads=8)
     assert {b for _, b in pairs} == {int(b) for b in np.flatnonzero(bits) + 2}
+
+
+ENGINE_SOURCES = ("prp_engine.cu", "prp_kernels.cu", "prp_kernels_np2.cu", "prp_grid.cu")
+
+
+@pytest.fixture(scope="module")
+def engine_emu():
+    """The engine's sources with their launches rewritten as calls, compiled
+    without sanitizers (a whole test is thousands of launches)."""
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    b = os.path.join(BUILD, "engine")
+    os.makedirs(b, exist_ok=True)
+    decl = "extern __shared__ __align__(16) uint32_t sm[];"
+    for f in ENGINE_SOURCES + ("prp_kernel_impl.cuh",):
+        src = open(os.path.join(CSRC, f)).read().replace(decl, "uint32_t *sm = emu_smem();")
+        src = SIEVE_LAUNCH.sub(lambda m: f"emu_launch({m.group(1)}, EmuCfg{{{m.group(2)}}})(", src)
+        assert "<<<" not in src
+        with open(os.path.join(b, f[:-3] + ".cpp" if f.endswith(".cu") else f), "w") as fh:
+            fh.write(src)
+    flags = ["-std=c++20", "-O1", "-I", os.path.join(EMU, "engine_stub"), "-I", os.path.join(EMU, "stub"), "-I", EMU,
+             "-I", CSRC, "-include", "emu_shim.h"]
+    objs = []
+    procs = []
+    for f in ENGINE_SOURCES:
+        o = os.path.join(b, f[:-3] + ".o")
+        objs.append(o)
+        procs.append(subprocess.Popen(["g++", *flags, "-c", "-o", o, os.path.join(b, f[:-3] + ".cpp")]))
+    assert all(p.wait(timeout=900) == 0 for p in procs)
+    exe = os.path.join(b, "engine_emu")
+    subprocess.run(["g++", *flags, "-o", exe, os.path.join(EMU, "engine_emu.cpp"), *objs, "-lpthread"], check=True,
+                   timeout=900)
+    return exe
+
+
+@pytest.mark.parametrize("b,base,form", [(68, 3, "+"), (68, 2, "-"), (298, 2, "+")])
+def test_engine_whole_test_emulated_matches_gmp(engine_emu, golden_dir, b, base, form):
+    """ctw_prp_run of one candidate of degree 2^8 (N- on the 2^9 transform) on
+    the emulated engine: PRP flag and RES64 equal GMP's, Gerbicz-Li check passes."""
+    import json
+    want = next(x for x in json.load(open(os.path.join(golden_dir, "prp_gmp.json")))
+                if x["n"] == 8 and x["b"] == b and x["base"] == base and x["form"] == form)
+    r = subprocess.run([engine_emu, "8", str(base), "1" if form == "-" else "0", str(b)],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got_b, prp, res64, gl = r.stdout.split()[:4]
+    assert int(got_b) == b and gl == "1"
+    assert (prp == "1", res64) == (want["prp"], want["res64"])
