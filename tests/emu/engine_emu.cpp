@@ -5,17 +5,23 @@
 // Test infrastructure (tests/test_kernels_emu_cpu.py).
 //
 // usage: engine_emu <log2 D> <base 2|3> <minus 0|1> <b> [<b> ...]
+//        engine_emu pool <log2 D> <slots> <base 2|3> <b> [<b> ...]
+// The second form runs the tests as a pool (continuous batching, ticks
+// replayed from recorded graphs) and prints the same line per test.
 #include "emu_shim.h"
 #include <barrier>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
+#include <functional>
 #include <memory>
 #include <thread>
 #include <vector>
 #include "cuda_runtime.h"
 #include "../../include/ctwin_gb300.h"
 
+std::vector<std::function<void()>> *emu_capture = nullptr;
 thread_local dim3 threadIdx, blockIdx;
 thread_local int t_cta;
 dim3 blockDim, gridDim;
@@ -73,8 +79,36 @@ void emu_run_ctas(dim3 grid, dim3 block, size_t smem, int group, void (*body)(vo
 	}
 }
 
+static int run_pool(int argc, char **argv)
+{
+	const int ln = atoi(argv[2]), slots = atoi(argv[3]), base = atoi(argv[4]);
+	std::vector<uint32_t> bs;
+	for (int i = 5; i < argc; ++i) bs.push_back((uint32_t)strtoul(argv[i], nullptr, 10));
+	ctw_pool *p = nullptr;
+	int rc = ctw_pool_create(ln, slots, -1, 0, (uint32_t)base, 0, &p);
+	size_t next = 0, done = 0;
+	std::vector<ctw_result> res(64);
+	while (!rc && done < bs.size())
+	{
+		// admit while slots are free, one tick at a time
+		while (next < bs.size() && ctw_pool_admit(p, bs[next], next) >= 0) ++next;
+		if ((rc = ctw_pool_run(p, 1)) < 0) break;
+		const int n = ctw_pool_collect(p, 1);
+		if (n < 0) { rc = n; break; }
+		rc = 0;
+		for (int got; (got = ctw_pool_results(p, res.data(), (int)res.size())) > 0;)
+			for (int i = 0; i < got; ++i, ++done)
+				printf("%u %d %016llX %d %d\n", res[(size_t)i].b, res[(size_t)i].is_prp,
+				       (unsigned long long)res[(size_t)i].res64, res[(size_t)i].gl_ok, res[(size_t)i].status);
+	}
+	if (rc) fprintf(stderr, "error %d: %s\n", rc, ctw_last_error());
+	if (p) ctw_pool_destroy(p);
+	return rc ? 1 : 0;
+}
+
 int main(int argc, char **argv)
 {
+	if (argc >= 6 && strcmp(argv[1], "pool") == 0) return run_pool(argc, argv);
 	if (argc < 5) { fprintf(stderr, "usage: engine_emu ln base minus b...\n"); return 2; }
 	const int ln = atoi(argv[1]), base = atoi(argv[2]), minus = atoi(argv[3]);
 	std::vector<uint32_t> bs;

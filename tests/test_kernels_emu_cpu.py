@@ -9,7 +9,9 @@ thread per GPU thread (tests/emu/), under AddressSanitizer and UBSan:
   a stand-in CUDA runtime, CTAs one after another;
 * the PRP engine's whole test (prp_engine.cu and its kernels, ctw_prp_run:
   exponent, bit loop, Gerbicz-Li check, canonical digits, RES64) on a
-  stand-in runtime that runs clusters and cooperative grids on host threads.
+  stand-in runtime that runs clusters and cooperative grids on host threads,
+  and a pool (prp_pool.cu: ticks recorded as graphs and replayed, a slot
+  reused by the next test).
 
 Squarings with doubling and one multiply, digits bit-exact with the oracle's C
 restatement; struck bitmaps and last p equal to the oracle's sieve; integer
@@ -250,7 +252,7 @@ def test_sieve_factors_emulated(sieve_emu, mode):
     assert {b for _, b in pairs} == {int(b) for b in np.flatnonzero(bits) + 2}
 
 
-ENGINE_SOURCES = ("prp_engine.cu", "prp_kernels.cu", "prp_kernels_np2.cu", "prp_grid.cu")
+ENGINE_SOURCES = ("prp_engine.cu", "prp_kernels.cu", "prp_kernels_np2.cu", "prp_grid.cu", "prp_pool.cu")
 
 
 @pytest.fixture(scope="module")
@@ -283,7 +285,7 @@ def engine_emu():
     return exe
 
 
-@pytest.mark.parametrize("b,base,form", [(68, 3, "+"), (68, 2, "-"), (298, 2, "+")])
+@pytest.mark.parametrize("b,base,form", [(68, 3, "+"), (68, 2, "-")])
 def test_engine_whole_test_emulated_matches_gmp(engine_emu, golden_dir, b, base, form):
     """ctw_prp_run of one candidate of degree 2^8 (N- on the 2^9 transform) on
     the emulated engine: PRP flag and RES64 equal GMP's, Gerbicz-Li check passes."""
@@ -296,3 +298,23 @@ def test_engine_whole_test_emulated_matches_gmp(engine_emu, golden_dir, b, base,
     got_b, prp, res64, gl = r.stdout.split()[:4]
     assert int(got_b) == b and gl == "1"
     assert (prp == "1", res64) == (want["prp"], want["res64"])
+
+
+def test_pool_emulated_matches_gmp(engine_emu, golden_dir):
+    """Two base-3 tests of degree 2^8 through a one-slot pool (the second is
+    admitted when the first retires; tick graphs recorded and replayed): PRP
+    flags, RES64 and Gerbicz-Li checks equal GMP's, one of them a PRP."""
+    import json
+    gold = {x["b"]: x for x in json.load(open(os.path.join(golden_dir, "prp_gmp.json")))
+            if x["n"] == 8 and x["base"] == 3 and x["form"] == "+"}
+    bs = [68, 298]
+    r = subprocess.run([engine_emu, "pool", "8", "1", "3", *map(str, bs)], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = {}
+    for line in r.stdout.strip().splitlines():
+        b, prp, res64, gl, status = line.split()
+        got[int(b)] = (prp == "1", res64, gl, status)
+    assert sorted(got) == bs
+    for b in bs:
+        assert got[b] == (gold[b]["prp"], gold[b]["res64"], "1", "0"), b
+    assert any(gold[b]["prp"] for b in bs)
