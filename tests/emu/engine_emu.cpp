@@ -6,6 +6,7 @@
 //
 // usage: engine_emu <log2 D> <base 2|3> <minus 0|1> <b> [<b> ...]
 //        engine_emu pool <log2 D> <slots> <base 2|3> <b> [<b> ...]
+//        engine_emu server <log2 D> <max slots> <base 2|3> <b> [<b> ...]
 // The second form runs the tests as a pool (continuous batching, ticks
 // replayed from recorded graphs) and prints the same line per test.
 #include "emu_shim.h"
@@ -106,9 +107,36 @@ static int run_pool(int argc, char **argv)
 	return rc ? 1 : 0;
 }
 
+// the request loop: submit every b, poll until each has a result
+static int run_server(int argc, char **argv)
+{
+	const int ln = atoi(argv[2]), max_slots = atoi(argv[3]), base = atoi(argv[4]);
+	std::vector<uint32_t> bs;
+	for (int i = 5; i < argc; ++i) bs.push_back((uint32_t)strtoul(argv[i], nullptr, 10));
+	ctw_server *s = nullptr;
+	int rc = ctw_server_create((size_t)1 << 30, max_slots, (uint32_t)base, 1, 0, &s);
+	for (size_t i = 0; i < bs.size() && !rc; ++i) rc = ctw_server_submit(s, ln, bs[i], i);
+	size_t done = 0;
+	std::vector<ctw_result> res(16);
+	const auto t0 = std::chrono::steady_clock::now();
+	while (!rc && done < bs.size())
+	{
+		const int got = ctw_server_poll(s, res.data(), (int)res.size(), 1000);
+		if (got < 0) { rc = got; break; }
+		for (int i = 0; i < got; ++i, ++done)
+			printf("%u %d %016llX %d %d\n", res[(size_t)i].b, res[(size_t)i].is_prp,
+			       (unsigned long long)res[(size_t)i].res64, res[(size_t)i].gl_ok, res[(size_t)i].status);
+		if (std::chrono::steady_clock::now() - t0 > std::chrono::minutes(10)) { rc = -100; break; }
+	}
+	if (rc) fprintf(stderr, "error %d: %s\n", rc, ctw_last_error());
+	if (s) ctw_server_destroy(s);
+	return rc ? 1 : 0;
+}
+
 int main(int argc, char **argv)
 {
 	if (argc >= 6 && strcmp(argv[1], "pool") == 0) return run_pool(argc, argv);
+	if (argc >= 6 && strcmp(argv[1], "server") == 0) return run_server(argc, argv);
 	if (argc < 5) { fprintf(stderr, "usage: engine_emu ln base minus b...\n"); return 2; }
 	const int ln = atoi(argv[1]), base = atoi(argv[2]), minus = atoi(argv[3]);
 	std::vector<uint32_t> bs;

@@ -58,6 +58,13 @@ inline const char *cudaGetErrorString(cudaError_t) { return "emulated CUDA error
 inline cudaError_t cudaGetLastError() { return cudaSuccess; }
 inline cudaError_t cudaDeviceSynchronize() { return cudaSuccess; }
 inline cudaError_t cudaGetDevice(int *d) { *d = 0; return cudaSuccess; }
+inline cudaError_t cudaSetDevice(int) { return cudaSuccess; }
+inline cudaError_t cudaMemGetInfo(size_t *fr, size_t *tot)
+{
+	*fr = (size_t)1 << 32;
+	*tot = (size_t)1 << 33;
+	return cudaSuccess;
+}
 inline cudaError_t cudaGetDeviceCount(int *n) { *n = 1; return cudaSuccess; }
 inline cudaError_t cudaDeviceGetAttribute(int *v, cudaDeviceAttr, int) { *v = 152; return cudaSuccess; }
 template <class F> inline cudaError_t cudaFuncSetAttribute(F, cudaFuncAttribute, int) { return cudaSuccess; }

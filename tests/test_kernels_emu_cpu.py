@@ -10,8 +10,8 @@ thread per GPU thread (tests/emu/), under AddressSanitizer and UBSan:
 * the PRP engine's whole test (prp_engine.cu and its kernels, ctw_prp_run:
   exponent, bit loop, Gerbicz-Li check, canonical digits, RES64) on a
   stand-in runtime that runs clusters and cooperative grids on host threads,
-  and a pool (prp_pool.cu: ticks recorded as graphs and replayed, a slot
-  reused by the next test).
+  and the server (prp_server.cu over prp_pool.cu: its threads, tick graphs
+  recorded and replayed, a slot reused by the next request).
 
 Squarings with doubling and one multiply, digits bit-exact with the oracle's C
 restatement; struck bitmaps and last p equal to the oracle's sieve; integer
@@ -252,7 +252,8 @@ def test_sieve_factors_emulated(sieve_emu, mode):
     assert {b for _, b in pairs} == {int(b) for b in np.flatnonzero(bits) + 2}
 
 
-ENGINE_SOURCES = ("prp_engine.cu", "prp_kernels.cu", "prp_kernels_np2.cu", "prp_grid.cu", "prp_pool.cu")
+ENGINE_SOURCES = ("prp_engine.cu", "prp_kernels.cu", "prp_kernels_np2.cu", "prp_grid.cu", "prp_pool.cu",
+                  "prp_server.cu")
 
 
 @pytest.fixture(scope="module")
@@ -300,15 +301,17 @@ def test_engine_whole_test_emulated_matches_gmp(engine_emu, golden_dir, b, base,
     assert (prp == "1", res64) == (want["prp"], want["res64"])
 
 
-def test_pool_emulated_matches_gmp(engine_emu, golden_dir):
-    """Two base-3 tests of degree 2^8 through a one-slot pool (the second is
-    admitted when the first retires; tick graphs recorded and replayed): PRP
-    flags, RES64 and Gerbicz-Li checks equal GMP's, one of them a PRP."""
+def test_server_emulated_matches_gmp(engine_emu, golden_dir):
+    """The request loop (prp_server.cu: preparation and worker threads over
+    pools) with one slot: two base-3 requests of degree 2^8, the second
+    admitted when the first retires, tick graphs recorded and replayed.
+    PRP flags, RES64 and Gerbicz-Li checks equal GMP's, one of them a PRP."""
     import json
     gold = {x["b"]: x for x in json.load(open(os.path.join(golden_dir, "prp_gmp.json")))
             if x["n"] == 8 and x["base"] == 3 and x["form"] == "+"}
     bs = [68, 298]
-    r = subprocess.run([engine_emu, "pool", "8", "1", "3", *map(str, bs)], capture_output=True, text=True, timeout=900)
+    r = subprocess.run([engine_emu, "server", "8", "1", "3", *map(str, bs)], capture_output=True, text=True,
+                       timeout=900)
     assert r.returncode == 0, r.stderr[-2000:]
     got = {}
     for line in r.stdout.strip().splitlines():
