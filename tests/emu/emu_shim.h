@@ -19,7 +19,7 @@ extern dim3 blockDim, gridDim;
 #define __host__
 #define __forceinline__ inline
 #define __launch_bounds__(...)
-#define __align__(n) alignas(n)
+#define __align__(n) __attribute__((aligned(n)))
 #define __shared__
 #define CTW_EMU 1
 using std::max;

@@ -7,6 +7,9 @@
 // usage: engine_emu <log2 D> <base 2|3> <minus 0|1> <b> [<b> ...]
 //        engine_emu pool <log2 D> <slots> <base 2|3> <b> [<b> ...]
 //        engine_emu server <log2 D> <max slots> <base 2|3> <b> [<b> ...]
+//        engine_emu mul <log2 D> <csize> <in file> <out file> <b> [<b> ...]
+// mul: ctw_prp_mul_noalloc of the lanes' x and y (int32 digits, x then y, read
+// from the in file) into z (written to the out file).
 // The second form runs the tests as a pool (continuous batching, ticks
 // replayed from recorded graphs) and prints the same line per test.
 #include "emu_shim.h"
@@ -133,8 +136,28 @@ static int run_server(int argc, char **argv)
 	return rc ? 1 : 0;
 }
 
+static int run_mul(int argc, char **argv)
+{
+	const int ln = atoi(argv[2]), csize = atoi(argv[3]);
+	std::vector<uint32_t> bs;
+	for (int i = 6; i < argc; ++i) bs.push_back((uint32_t)strtoul(argv[i], nullptr, 10));
+	const size_t lanes = bs.size(), D = (size_t)1 << ln;
+	std::vector<int32_t> xy(2 * lanes * D), z(lanes * D);
+	FILE *f = fopen(argv[4], "rb");
+	if (!f || fread(xy.data(), 4, xy.size(), f) != xy.size()) { fprintf(stderr, "bad input file\n"); return 2; }
+	fclose(f);
+	const int rc = ctw_prp_mul_noalloc(ln, (int)lanes, bs.data(), xy.data(), xy.data() + lanes * D, z.data(), csize,
+	                                   nullptr);
+	if (rc) { fprintf(stderr, "error %d: %s\n", rc, ctw_last_error()); return 1; }
+	f = fopen(argv[5], "wb");
+	if (!f || fwrite(z.data(), 4, z.size(), f) != z.size()) return 2;
+	fclose(f);
+	return 0;
+}
+
 int main(int argc, char **argv)
 {
+	if (argc >= 7 && strcmp(argv[1], "mul") == 0) return run_mul(argc, argv);
 	if (argc >= 6 && strcmp(argv[1], "pool") == 0) return run_pool(argc, argv);
 	if (argc >= 6 && strcmp(argv[1], "server") == 0) return run_server(argc, argv);
 	if (argc < 5) { fprintf(stderr, "usage: engine_emu ln base minus b...\n"); return 2; }

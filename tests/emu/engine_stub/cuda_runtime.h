@@ -59,6 +59,11 @@ inline cudaError_t cudaGetLastError() { return cudaSuccess; }
 inline cudaError_t cudaDeviceSynchronize() { return cudaSuccess; }
 inline cudaError_t cudaGetDevice(int *d) { *d = 0; return cudaSuccess; }
 inline cudaError_t cudaSetDevice(int) { return cudaSuccess; }
+template <class T> inline cudaError_t cudaGetSymbolAddress(void **p, const T &sym)
+{
+	*p = (void *)&sym;
+	return cudaSuccess;
+}
 inline cudaError_t cudaMemGetInfo(size_t *fr, size_t *tot)
 {
 	*fr = (size_t)1 << 32;

@@ -10,8 +10,9 @@ thread per GPU thread (tests/emu/), under AddressSanitizer and UBSan:
 * the PRP engine's whole test (prp_engine.cu and its kernels, ctw_prp_run:
   exponent, bit loop, Gerbicz-Li check, canonical digits, RES64) on a
   stand-in runtime that runs clusters and cooperative grids on host threads,
-  and the server (prp_server.cu over prp_pool.cu: its threads, tick graphs
-  recorded and replayed, a slot reused by the next request).
+  the server (prp_server.cu over prp_pool.cu: its threads, tick graphs
+  recorded and replayed, a slot reused by the next request), and the
+  allocation-free multiply (prp_noalloc.cu).
 
 Squarings with doubling and one multiply, digits bit-exact with the oracle's C
 restatement; struck bitmaps and last p equal to the oracle's sieve; integer
@@ -253,7 +254,7 @@ def test_sieve_factors_emulated(sieve_emu, mode):
 
 
 ENGINE_SOURCES = ("prp_engine.cu", "prp_kernels.cu", "prp_kernels_np2.cu", "prp_grid.cu", "prp_pool.cu",
-                  "prp_server.cu")
+                  "prp_server.cu", "prp_noalloc.cu")
 
 
 @pytest.fixture(scope="module")
@@ -321,3 +322,25 @@ def test_server_emulated_matches_gmp(engine_emu, golden_dir):
     for b in bs:
         assert got[b] == (gold[b]["prp"], gold[b]["res64"], "1", "0"), b
     assert any(gold[b]["prp"] for b in bs)
+
+
+@pytest.mark.parametrize("ln,bs,csize", [(11, [100003, 299993], 16), (13, [1330358], 8)])
+def test_mul_noalloc_emulated_bit_exact(engine_emu, tmp_path, ln, bs, csize):
+    """ctw_prp_mul_noalloc (fixed device arrays, no allocation) on the emulated
+    runtime: z = x * y digits bit-exact with the oracle's multiply."""
+    import numpy as np
+    rng = np.random.default_rng(ln)
+    D = 1 << ln
+    x = np.stack([rng.integers(-(b // 2), b // 2, D, dtype=np.int64) for b in bs]).astype(np.int32)
+    y = np.stack([rng.integers(-(b // 2), b // 2, D, dtype=np.int64) for b in bs]).astype(np.int32)
+    fin, fout = tmp_path / "xy.bin", tmp_path / "z.bin"
+    np.concatenate([x.ravel(), y.ravel()]).tofile(fin)
+    r = subprocess.run([engine_emu, "mul", str(ln), str(csize), str(fin), str(fout), *map(str, bs)],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    z = np.fromfile(fout, dtype=np.int32).reshape(len(bs), D)
+    with O.Tables(ln) as t:
+        for lane, b in enumerate(bs):
+            w = x[lane].copy()
+            t.mul(w, y[lane].copy(), b, csize)
+            assert np.array_equal(z[lane], w), lane
