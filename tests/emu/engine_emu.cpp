@@ -8,6 +8,9 @@
 //        engine_emu pool <log2 D> <slots> <base 2|3> <b> [<b> ...]
 //        engine_emu server <log2 D> <max slots> <base 2|3> <b> [<b> ...]
 //        engine_emu mul <log2 D> <csize> <in file> <out file> <b> [<b> ...]
+//        engine_emu resume <log2 D> <base 2|3> <context file> <b>
+// resume: the whole test stops at its first Gerbicz-Li checkpoint, saves the
+// reference's context file there, and a fresh engine reads it and finishes.
 // mul: ctw_prp_mul_noalloc of the lanes' x and y (int32 digits, x then y, read
 // from the in file) into z (written to the out file).
 // The second form runs the tests as a pool (continuous batching, ticks
@@ -155,8 +158,44 @@ static int run_mul(int argc, char **argv)
 	return 0;
 }
 
+static ctw_prp *g_stop_h = nullptr;
+static const char *g_stop_path = nullptr;
+static int stop_at_checkpoint(void *, long long i)
+{
+	return ctw_prp_save_context(g_stop_h, g_stop_path, 0, (int)i, 0.0) == CTW_OK ? 1 : -1;
+}
+
+static int run_resume(char **argv)
+{
+	const int ln = atoi(argv[2]), base = atoi(argv[3]);
+	g_stop_path = argv[4];
+	const uint32_t b = (uint32_t)strtoul(argv[5], nullptr, 10);
+	uint8_t prp = 0, gl = 0;
+	uint64_t r64 = 0;
+	ctw_prp *h = nullptr;
+	int rc = ctw_prp_create(ln, 1, &h);
+	if (!rc) rc = ctw_prp_set_base(h, (uint32_t)base);
+	g_stop_h = h;
+	if (!rc) rc = ctw_prp_run_ex(h, &b, 1, -1, stop_at_checkpoint, nullptr, &prp, &r64, &gl);
+	if (h) ctw_prp_destroy(h);
+	if (rc != CTW_STOPPED) { fprintf(stderr, "first run: %d (expected a stop) %s\n", rc, ctw_last_error()); return 1; }
+	h = nullptr;
+	int k = 0, i = 0;
+	double el = 0;
+	rc = ctw_prp_create(ln, 1, &h);
+	if (!rc) rc = ctw_prp_set_base(h, (uint32_t)base);
+	if (!rc) rc = ctw_prp_set_b(h, &b, 1);
+	if (!rc) rc = ctw_prp_read_context(h, g_stop_path, &k, &i, &el);
+	if (!rc) rc = ctw_prp_run_ex(h, &b, 1, i, nullptr, nullptr, &prp, &r64, &gl);
+	if (rc) fprintf(stderr, "resume: %d %s\n", rc, ctw_last_error());
+	else printf("%u %d %016llX %d %d\n", b, prp, (unsigned long long)r64, gl, i);
+	if (h) ctw_prp_destroy(h);
+	return rc ? 1 : 0;
+}
+
 int main(int argc, char **argv)
 {
+	if (argc >= 6 && strcmp(argv[1], "resume") == 0) return run_resume(argv);
 	if (argc >= 7 && strcmp(argv[1], "mul") == 0) return run_mul(argc, argv);
 	if (argc >= 6 && strcmp(argv[1], "pool") == 0) return run_pool(argc, argv);
 	if (argc >= 6 && strcmp(argv[1], "server") == 0) return run_server(argc, argv);

@@ -11,8 +11,10 @@ thread per GPU thread (tests/emu/), under AddressSanitizer and UBSan:
   exponent, bit loop, Gerbicz-Li check, canonical digits, RES64) on a
   stand-in runtime that runs clusters and cooperative grids on host threads,
   the server (prp_server.cu over prp_pool.cu: its threads, tick graphs
-  recorded and replayed, a slot reused by the next request), and the
-  allocation-free multiply (prp_noalloc.cu).
+  recorded and replayed, a slot reused by the next request), the
+  allocation-free multiply (prp_noalloc.cu), and a stop at a Gerbicz-Li
+  checkpoint with the reference's context file and a resume from it
+  (cyclo_files.cu).
 
 Squarings with doubling and one multiply, digits bit-exact with the oracle's C
 restatement; struck bitmaps and last p equal to the oracle's sieve; integer
@@ -254,7 +256,7 @@ def test_sieve_factors_emulated(sieve_emu, mode):
 
 
 ENGINE_SOURCES = ("prp_engine.cu", "prp_kernels.cu", "prp_kernels_np2.cu", "prp_grid.cu", "prp_pool.cu",
-                  "prp_server.cu", "prp_noalloc.cu")
+                  "prp_server.cu", "prp_noalloc.cu", "cyclo_files.cu")
 
 
 @pytest.fixture(scope="module")
@@ -344,3 +346,21 @@ def test_mul_noalloc_emulated_bit_exact(engine_emu, tmp_path, ln, bs, csize):
             w = x[lane].copy()
             t.mul(w, y[lane].copy(), b, csize)
             assert np.array_equal(z[lane], w), lane
+
+
+def test_context_stop_and_resume_emulated(engine_emu, golden_dir, tmp_path):
+    """A whole base-3 test of degree 2^8 stops at its first Gerbicz-Li
+    checkpoint and saves the reference's context file there
+    (ctw_prp_save_context); a fresh engine reads it (ctw_prp_read_context)
+    and resumes (ctw_prp_run_ex from the saved bit): the verdict and RES64
+    equal GMP's (a PRP)."""
+    import json
+    want = next(x for x in json.load(open(os.path.join(golden_dir, "prp_gmp.json")))
+                if x["n"] == 8 and x["b"] == 298 and x["base"] == 3 and x["form"] == "+")
+    ctx = tmp_path / "cyclo.ctx"
+    r = subprocess.run([engine_emu, "resume", "8", "3", str(ctx), "298"], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    b, prp, res64, gl, i_stop = r.stdout.split()
+    assert int(b) == 298 and gl == "1" and int(i_stop) > 0
+    assert (prp == "1", res64) == (want["prp"], want["res64"])
+    assert ctx.exists()
