@@ -78,6 +78,8 @@ def workload(rank: int):
 
 
 TRAFFIC_PER_LAUNCH = 1.50e6     # ncu dram read+write bytes of one 651-squaring launch at 2^16 (64-CTA grid)
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one 651-squaring launch of the "
+                  "default split (profiles/prp_kernel_d65536_full.md)")
 
 
 def hbm_line(traffic: float, seconds: float) -> dict:
@@ -93,8 +95,90 @@ def hbm_line(traffic: float, seconds: float) -> dict:
 
 
 def imad_per_squaring(D: int, primes: int = 3) -> float:
-    """4 IMAD per modular multiply; per NTT prime D log2 D + 3 D multiplies per squaring."""
+    """4 IMAD per modular multiply; per NTT prime D log2 D + 3 D multiplies per squaring
+    (three primes: 4 (3 D log2 D + 9 D), the algorithmic count of one squaring)."""
     return 4.0 * primes * (D * math.log2(D) + 3 * D)
+
+
+def roofline_single(achieved, executed, peak_imad, peak_mont, peak_shoup, t_launch, geo, sms, have_traffic):
+    """Roofline of the resident squaring launch.  achieved: algorithmic IMAD/s
+    (three-prime count); executed: the same count for the primes run.  The
+    denominators are probes run in this process: plain 32-bit IMAD chains, and
+    Montgomery / Shoup modular-product chains (4 IMAD-equivalents each, the
+    count's charge per modular multiply)."""
+    fr = {}
+    for wname, w in (("algorithmic", achieved), ("executed_primes", executed)):
+        fr[wname] = {"vs_imad_probe": w / peak_imad if peak_imad else None,
+                     "vs_montgomery_probe": w / (4 * peak_mont) if peak_mont else None,
+                     "vs_shoup_probe": w / (4 * peak_shoup) if peak_shoup else None}
+    used = geo["ctas_per_lane"]
+    out = {"bound": "imad", "achieved": achieved / 1e12, "peak": peak_imad / 1e12, "unit": "T IMAD/s",
+           "frac": achieved / peak_imad if peak_imad else None,
+           "traffic": TRAFFIC_PER_LAUNCH if have_traffic else None,
+           "traffic_source": TRAFFIC_SOURCE,
+           "peak_source": "32-bit IMAD probe kernel run on this GPU in this process",
+           "fractions": fr,
+           "peaks": {"imad_per_s": peak_imad, "montgomery_products_per_s": peak_mont,
+                     "shoup_products_per_s": peak_shoup},
+           "executed_t_imad_per_s": executed / 1e12,
+           "sms_used": used, "sms": sms,
+           "frac_of_used_sms": (achieved / peak_imad) * sms / used if peak_imad else None,
+           "kernel_ms": t_launch * 1000.0,
+           "hbm": hbm_line(TRAFFIC_PER_LAUNCH, t_launch) if have_traffic else None}
+    return out
+
+
+def secondary():
+    """Other workloads, timed in the same process so that one bench line carries
+    them: batched over plain at degrees 2^12..2^14 (256 candidates per degree,
+    b uniform in [2^16, 2^22) seed 3, one pool tick against the one-candidate
+    launch sequence), one pass of the large sieve (n = 20, b < 2^30, p < 2^40)
+    and the n = 11 sieve of b in [10^5, 3 10^5) to 2^32, both forms."""
+    import torch
+    from ctwin_gb300 import Pool, autotune, sieve_pass
+    out = {"batched_over_plain": {}}
+    rng = random.Random(3)
+    t_start = time.perf_counter()
+    for k in (12, 13, 14):
+        bs = [rng.randrange(1 << 16, 1 << 22) for _ in range(256)]
+        lg, cs, _ = autotune(k, len(bs), 2)
+        with Pool(k, len(bs), log2_ctas=lg, csize=cs) as p:
+            assert p.admit_many(bs) == len(bs)
+            p.run(1)
+            p.collect(wait=True)
+            info = p.info()
+            st = torch.cuda.ExternalStream(p.stream)
+            ts = []
+            for _ in range(3):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                p.run(1)
+                e1.record(st)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1) / 1000.0)
+            p.collect(wait=True)
+            batched = info["slots"] * (info["gl_block"] + 1) / statistics.median(ts)
+        plain = plain_rate(k, bs[0])
+        out["batched_over_plain"][str(k)] = {"candidates": len(bs), "batched_sq_per_s": batched,
+                                             "plain_sq_per_s": plain, "ratio": batched / plain,
+                                             "log2_ctas": lg, "csize": cs}
+    n, b_min, b_max = 20, 2, (1 << 30) - 1
+    sieve_pass(n, b_min, b_max, 3 * (1 << n) + 1, 1 << 40, 1)
+    t0 = time.perf_counter()
+    struck, p_last = sieve_pass(n, b_min, b_max, 3 * (1 << n) + 1, 1 << 40, 1)
+    t4 = time.perf_counter() - t0
+    out["large_sieve"] = {"workload": "n = 20, b in [2, 2^30), p < 2^40, + form, one pass through the C ABI "
+                                      "(bitmap copied in and out)", "seconds": t4,
+                          "sieved_b_per_s": (b_max - b_min + 1) / t4, "p_last": p_last}
+    c1 = {}
+    for name, mode, pmn in (("pos", 1, 3 * 2048 + 1), ("neg", -1, 11)):
+        sieve_pass(11, 100000, 299999, pmn, 1 << 32, mode)
+        t0 = time.perf_counter()
+        sieve_pass(11, 100000, 299999, pmn, 1 << 32, mode)
+        c1[name] = time.perf_counter() - t0
+    out["n11_sieve_s"] = c1
+    out["seconds"] = time.perf_counter() - t_start
+    return out
 
 
 class ClockSampler:
@@ -157,8 +241,19 @@ class ClockSampler:
 # CPU arm: the oracle's restatement of the reference transform
 # ---------------------------------------------------------------------------
 
+def single_config(world: int = 1) -> dict:
+    """The single-test workload's config, the same in both arms."""
+    b, E, i0, B_GL, _ = workload(0)
+    return {"workload": f"single large PRP, degree 2^{LOG2_D} (N = b^{1 << LOG2_D} - b^{1 << (LOG2_D - 1)} + 1), "
+                        "b uniform in [2^20, 2^21) seed 1, Fermat base 3, one candidate per launch sequence",
+            "degree": 1 << LOG2_D, "b": b, "base": 3, "seed": SEED, "exponent_bits": i0 + 1,
+            "squarings_per_step": B_GL, "step": "one Gerbicz-Li block: B_GL resident squarings + one multiply",
+            "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}"}
+
+
 def cpu_squarings_per_s(threads: int, seconds: float = 12.0):
-    """Each host thread squares its own degree-2^16 candidate; bounded sample."""
+    """Every host thread squares its own copy of the workload's candidate (b of
+    seed 1, base 3) from the exponent's top bit; bounded sample."""
     from oracle import oracle as O
     O.build()
     per = [0] * threads
@@ -167,7 +262,7 @@ def cpu_squarings_per_s(threads: int, seconds: float = 12.0):
     lock = threading.Lock()
 
     def work(t):
-        b, E, i0, _, words = workload(100 + t)
+        b, E, i0, _, words = workload(0)
         x = np.zeros(1 << LOG2_D, dtype=np.int32)
         x[0] = 1
         i = i0
@@ -189,7 +284,7 @@ def cpu_squarings_per_s(threads: int, seconds: float = 12.0):
     tabs.close()
     total = sum(per)
     return total / dt, {"value": total / dt, "unit": UNIT, "cores": threads, "kind": "port",
-                        "sample": f"{threads} candidates of degree 2^{LOG2_D} (b in [2^20,2^21)), "
+                        "sample": f"{threads} copies of the degree-2^{LOG2_D} candidate (one per thread), "
                                   f"{total} squarings in {dt:.1f} s with the oracle C restatement"}
 
 
@@ -197,20 +292,15 @@ def run_reference(args, rank, world):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    samples = []
-    per_step = args.cpu_seconds if args.cpu_seconds > 0 else max(2.0, 20.0 / max(1, args.steps))
-    for _ in range(max(1, args.steps)):
-        v, cb = cpu_squarings_per_s(threads, seconds=per_step)
-        samples.append(v)
-    v = statistics.median(samples)
-    cb["value"] = v
+    # one sample over all steps: 12 s at least (thread start-up is noise below that)
+    total = args.cpu_seconds if args.cpu_seconds > 0 else min(120.0, max(12.0, 0.5 * max(1, args.steps)))
+    v, cb = cpu_squarings_per_s(threads, seconds=total)
     b, E, i0, B_GL, _ = workload(0)
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * B_GL / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": f"single large PRP, degree 2^{LOG2_D}, b in [2^20, 2^21), one candidate per core",
-                       "degree": 1 << LOG2_D, "squarings_per_step": B_GL},
+            "config": single_config(world),
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -687,6 +777,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="single: skip the secondary block (batched/plain, sieves) of the bench line")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "serve", "sieve", "config1"])
     ap.add_argument("--candidates", type=int, default=4096, help="batch: candidates")
     ap.add_argument("--requests", type=int, default=0, help="serve: requests (0: rate x --serve-seconds)")
@@ -696,7 +788,7 @@ def main():
     ap.add_argument("--log2-degree", type=int, default=16, choices=range(12, 19),
                     help="single: degree of the candidate (2^16 is the headline configuration)")
     ap.add_argument("--cpu-seconds", type=float, default=0.0,
-                    help="reference arm: seconds of CPU work per step (0: 20 s spread over the steps, 2 s minimum)")
+                    help="reference arm: seconds of CPU work in all (0: 0.5 s per step, 12 s to 120 s)")
     ap.add_argument("--log2-ctas", type=int, default=-1,
                     help="single: CTAs per candidate as a power of two (-1: the library's default split)")
     args = ap.parse_args()
@@ -803,8 +895,13 @@ def main():
         i -= B_GL
     t_launch = statistics.median(sq_times)
     primes = eng.prime_count
-    achieved = imad_per_squaring(D, primes) * B_GL / t_launch
+    # algorithmic work: the three-prime count 4 (3 D log2 D + 9 D) IMAD per squaring;
+    # executed work: the same count for the primes the launch ran
+    achieved = imad_per_squaring(D, 3) * B_GL / t_launch
+    executed = imad_per_squaring(D, primes) * B_GL / t_launch
     geo = eng.geometry()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    peak_mont, peak_shoup = L.ctw_modmul_peak(0), L.ctw_modmul_peak(1)
 
     # e2e through the C ABI with host buffers: exponent slice in, residue out
     reg_host = np.zeros((1, 1, D), dtype=np.int32)
@@ -844,29 +941,19 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"single large PRP, degree 2^{LOG2_D} (N = b^{1 << LOG2_D} - b^{1 << (LOG2_D - 1)} + 1), "
-                               "b uniform in [2^20, 2^21) seed 1, Fermat base 3, one candidate per launch sequence",
-                   "degree": D, "b": b, "base": 3, "exponent_bits": i0 + 1, "squarings_per_step": B_GL,
-                   "step": "one Gerbicz-Li block: B_GL resident squarings + one multiply",
-                   "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}",
-                   "ctas_per_candidate": geo["ctas_per_lane"], "threads_per_cta": geo["threads"],
+        "config": single_config(world),
+        "launch": {"ctas_per_candidate": geo["ctas_per_lane"], "threads_per_cta": geo["threads"],
                    "smem_per_cta": geo["smem_bytes"], "ntt_primes": primes},
         "tests_per_s_projected": value / (i0 + 1),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": peak_imad / 1e12, "unit": "T IMAD/s",
-                     "frac": achieved / peak_imad if peak_imad else None,
-                     "traffic": TRAFFIC_PER_LAUNCH if (LOG2_D == 16 and args.log2_ctas < 0) else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 651-squaring launch "
-                                       "of the default split (profiles/prp_kernel_d65536_full.md)",
-                     "peak_source": "32-bit IMAD probe kernel run on this GPU in this process",
-                     "sms_used": geo["ctas_per_lane"],
-                     "frac_of_used_sms": (achieved / peak_imad) * 152 / geo["ctas_per_lane"] if peak_imad else None,
-                     "kernel_ms": t_launch * 1000.0,
-                     "hbm": hbm_line(TRAFFIC_PER_LAUNCH, t_launch) if (LOG2_D == 16 and args.log2_ctas < 0) else None},
+        "roofline": roofline_single(achieved, executed, peak_imad, peak_mont, peak_shoup, t_launch, geo, sms,
+                                    LOG2_D == 16 and args.log2_ctas < 0),
         "cpu_baseline": cpu,
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if not args.no_secondary and LOG2_D == 16 and world == 1:
+        line["secondary"] = secondary()
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

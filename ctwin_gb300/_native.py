@@ -70,7 +70,9 @@ def lib() -> ctypes.CDLL:
             "ctw_prp_stream": ([H], vp),
             "ctw_prp_geometry": ([H, vp, vp, vp], i32),
             "ctw_prp_launches": ([H], i64),
+            "ctw_prp_test_unreachable_barrier": ([H], i32),
             "ctw_imad_peak": ([], ctypes.c_double),
+            "ctw_modmul_peak": ([i32], ctypes.c_double),
             "ctw_prp_mul_noalloc": ([i32, i32, vp, vp, vp, vp, i32, vp], i32),
             "ctw_sieve_run": ([i32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, i32, vp, vp], i32),
             "ctw_sieve_write_files": ([i32, ctypes.c_uint64, ctypes.c_uint64, vp, ctypes.c_uint64, ctypes.c_uint64,

@@ -182,6 +182,7 @@ struct ctw_prp {
 	uint32_t *d_gx = nullptr, *d_gr = nullptr, *d_xr = nullptr;
 	long long *d_gc = nullptr;
 	unsigned *d_bar = nullptr;
+	int bar_unreachable = 0;          // testing: the next grid launch starts its barrier out of reach
 	std::vector<uint32_t> b;
 	PrpKernelArgs proto{};
 	long long launches = 0;
@@ -344,6 +345,11 @@ int launch(ctw_prp *h, const PrpKernelArgs &a)
 	{
 		// barrier counters start at zero in every launch
 		e = cudaMemsetAsync(h->d_bar, 0, (size_t)h->lanes * GRID_BAR_WORDS * sizeof(unsigned), h->stream);
+		// testing only (ctw_prp_test_unreachable_barrier): word 0 of every lane
+		// starts at 0x80808080, 2^31 arrivals short of any target this launch sets
+		for (int l = 0; e == cudaSuccess && h->bar_unreachable && l < h->lanes; ++l)
+			e = cudaMemsetAsync(h->d_bar + (size_t)l * GRID_BAR_WORDS, 0x80, sizeof(unsigned), h->stream);
+		h->bar_unreachable = 0;
 		if (e == cudaSuccess)
 		{
 			const PrpGridArgs ga{ h->d_gx, h->d_gr, h->d_gc, h->d_bar, h->d_xr };
@@ -948,6 +954,14 @@ int ctw_prp_geometry(ctw_prp *h, int *ctas, int *threads, int *smem)
 
 long long ctw_prp_launches(ctw_prp *h) { return h ? h->launches : 0; }
 
+int ctw_prp_test_unreachable_barrier(ctw_prp *h)
+{
+	if (int rc = check_handle(h)) return rc;
+	if (!h->grid) return fail(CTW_E_ARG, "the handle's split is not the grid kernel");
+	h->bar_unreachable = 1;
+	return CTW_OK;
+}
+
 int ctw_prp_shape(ctw_prp *h, int *log2_degree, int *lanes, int *minus)
 {
 	if (int rc = check_handle(h)) return rc;
@@ -962,6 +976,13 @@ double ctw_imad_peak(void)
 	int dev = 0;
 	if (cudaGetDevice(&dev) != cudaSuccess) return 0.0;
 	return imad_peak(dev);
+}
+
+double ctw_modmul_peak(int kind)
+{
+	int dev = 0;
+	if ((kind != 0 && kind != 1) || cudaGetDevice(&dev) != cudaSuccess) return 0.0;
+	return modmul_peak(dev, kind);
 }
 
 }  // extern "C"

@@ -177,6 +177,70 @@ __global__ void imad_probe_kernel(uint32_t *out, int iters)
 	if (s == 0x2545F491u) out[0] = s;
 }
 
+// Modular-product probes: independent chains of the two products the
+// transforms are built from, on the first NTT prime.  KIND 0: Montgomery
+// (mlazy: one wide product, a low product by q^-1, a high product by q);
+// KIND 1: Shoup with a precomputed quotient (one high, two low products).
+template <int KIND>
+__global__ void modmul_probe_kernel(uint32_t *out, int iters)
+{
+	constexpr int C = 8;
+	uint32_t v[C], w[C], wq[C];
+#pragma unroll
+	for (int j = 0; j < C; ++j)
+	{
+		v[j] = threadIdx.x * 7u + j * 13u + blockIdx.x;
+		w[j] = (0x9E3779B9u * (j + 1) + blockIdx.x) % Q0;
+		wq[j] = (uint32_t)(((uint64_t)w[j] << 32) / Q0);
+	}
+	for (int i = 0; i < iters; ++i)
+	{
+#pragma unroll
+		for (int j = 0; j < C; ++j)
+			v[j] = KIND == 0 ? mlazy(v[j], w[j], Q0, QI0) : shoup(v[j], w[j], wq[j], Q0);
+	}
+	uint32_t s = 0;
+#pragma unroll
+	for (int j = 0; j < C; ++j) s ^= v[j];
+	if (s == 0x2545F491u) out[0] = s;
+}
+
+template <class Launch>
+static double probe_rate(int device, double per_thread_iter, Launch launch)
+{
+	int sms = 0;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+	uint32_t *out = nullptr;
+	if (cudaMalloc(&out, 64) != cudaSuccess) return 0.0;
+	const int grid = sms * 8, block = 256, iters = 16384;
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	launch(grid, block, out, 256);
+	float best = 1e30f;
+	for (int rep = 0; rep < 3; ++rep)
+	{
+		cudaEventRecord(e0);
+		launch(grid, block, out, iters);
+		cudaEventRecord(e1);
+		cudaEventSynchronize(e1);
+		float ms = 0;
+		cudaEventElapsedTime(&ms, e0, e1);
+		if (ms < best) best = ms;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(out);
+	return double(grid) * block * per_thread_iter * iters / (best * 1e-3);
+}
+
+double modmul_peak(int device, int kind)
+{
+	if (kind == 0)
+		return probe_rate(device, 8, [](int g, int b, uint32_t *o, int it) { modmul_probe_kernel<0><<<g, b>>>(o, it); });
+	return probe_rate(device, 8, [](int g, int b, uint32_t *o, int it) { modmul_probe_kernel<1><<<g, b>>>(o, it); });
+}
+
 double imad_peak(int device)
 {
 	int sms = 0;

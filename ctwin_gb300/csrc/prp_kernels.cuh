@@ -135,5 +135,6 @@ cudaError_t prp_aux_launch(const PrpLaneAux *aux, int32_t *regs, long long reg_s
 
 // Integer-multiply throughput probe (roofline denominator): returns IMAD/s.
 double imad_peak(int device);
+double modmul_peak(int device, int kind);
 
 }  // namespace ctw

@@ -69,8 +69,9 @@ size_t na_shoup_offset(int ln)
 }
 
 // One-time set-up of the current device: device addresses of the file-scope
-// arrays (the names are only host-side stand-ins) and the root tables.
-int na_setup(int dev)
+// arrays (the names are only host-side stand-ins) and the root tables, uploaded
+// on the caller's stream (no device-wide synchronisation) and waited for there.
+int na_setup(int dev, cudaStream_t st)
 {
 	NaDevice &d = g_na_dev[dev];
 	if (d.ready) return CTW_OK;
@@ -93,7 +94,9 @@ int na_setup(int dev)
 		}
 		prp_build_tables(ln, prp_lg_for(ln), tf, tf + 3 * (size_t(1) << ln), d.proto[ln], tfs, tis);
 	}
-	if ((e = cudaMemcpy(d.tables, g_na_host_tables, sizeof(g_na_host_tables), cudaMemcpyHostToDevice)) != cudaSuccess)
+	if ((e = cudaMemcpyAsync(d.tables, g_na_host_tables, sizeof(g_na_host_tables), cudaMemcpyHostToDevice, st)) !=
+	        cudaSuccess ||
+	    (e = cudaStreamSynchronize(st)) != cudaSuccess)
 		return fail(CTW_E_CUDA, "no-alloc set-up: table upload: %s", cudaGetErrorString(e));
 	d.ready = true;
 	return CTW_OK;
@@ -130,7 +133,7 @@ extern "C" int ctw_prp_mul_noalloc(int log2_degree, int lanes, const uint32_t *b
 	NaDevice *d;
 	{
 		std::lock_guard<std::mutex> g(g_na_mu);
-		if (int rc = na_setup(dev)) return rc;
+		if (int rc = na_setup(dev, (cudaStream_t)stream)) return rc;
 		d = &g_na_dev[dev];
 	}
 	cudaStream_t st = (cudaStream_t)stream;

@@ -15,6 +15,9 @@ import numpy as np
 from ._native import check, lib, ptr
 
 
+_CHECKPOINT_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong)
+
+
 class PrpEngine:
     """Fermat-test engine for `lanes` candidates of degree D = 2^log2_degree."""
 
@@ -146,6 +149,35 @@ class PrpEngine:
         r64 = np.zeros(n, dtype=np.uint64)
         gl = np.zeros(n, dtype=np.uint8)
         check(lib().ctw_prp_run(self._h, ptr(arr), n, ptr(prp), ptr(r64), ptr(gl)))
+        return prp.astype(bool), r64, gl.astype(bool)
+
+    def run_ex(self, b, checkpoint=None, i_start: int = -1):
+        """run() with checkpoints and resume, as cyclo::check(b, ctx, k, ri)
+        (cyclo/src/cyclo.h:252-377): checkpoint(i) is called on the host after
+        every Gerbicz-Li multiply, i being the next exponent bit, with the device
+        idle (registers 0 = x and 1 = d may be read or written there); a true
+        return stops the run (CtwError with CTW_STOPPED).  i_start >= 0 resumes
+        before bit i_start from registers 0 and 1 as they are."""
+        arr = np.ascontiguousarray(b, dtype=np.uint32)
+        n = arr.size
+        prp = np.zeros(n, dtype=np.uint8)
+        r64 = np.zeros(n, dtype=np.uint64)
+        gl = np.zeros(n, dtype=np.uint8)
+        errors = []
+
+        def trampoline(_user, i):
+            try:
+                return 1 if checkpoint(int(i)) else 0
+            except Exception as e:      # stop the run, re-raise below
+                errors.append(e)
+                return 1
+
+        cb = _CHECKPOINT_FN(trampoline) if checkpoint else None
+        rc = lib().ctw_prp_run_ex(self._h, ptr(arr), n, i_start, ctypes.cast(cb, ctypes.c_void_p) if cb else None,
+                                  None, ptr(prp), ptr(r64), ptr(gl))
+        if errors:
+            raise errors[0]
+        check(rc)
         return prp.astype(bool), r64, gl.astype(bool)
 
     # -- plumbing --

@@ -182,6 +182,12 @@ int ctw_prp_geometry(ctw_prp *h, int *ctas_per_lane, int *threads, int *smem_byt
 long long ctw_prp_launches(ctw_prp *h);
 /* Degree of the tested numbers (log2), lanes, and 1 for an N- engine. */
 int ctw_prp_shape(ctw_prp *h, int *log2_degree, int *lanes, int *minus);
+/* Testing only, no counterpart in the reference: the next launch of a grid
+ * handle starts its grid-barrier counter out of reach, so that every CTA's
+ * bounded wait (50 ms of %globaltimer) runs out.  That launch ends with
+ * CTW_E_COMPUTE (status ST_GRID_WAIT, results void) and the handle stays
+ * usable; later launches are unaffected.  CTW_E_ARG for a non-grid split. */
+int ctw_prp_test_unreachable_barrier(ctw_prp *h);
 
 /* z = x * y for `lanes` candidates of degree D = 2^log2_degree (8..14), with
  * x, y, z caller-owned DEVICE buffers of lanes * D int32 digits (the register
@@ -195,7 +201,12 @@ int ctw_prp_shape(ctw_prp *h, int *log2_degree, int *lanes, int *minus);
  * larger requests fail with CTW_E_ARG).  Calls share those arrays: calls that
  * overlap on the GPU (other streams, other threads) race and must be
  * serialised by the caller.  The first call on each device sets the arrays up
- * (symbol addresses, root tables) and should come before any stream capture.
+ * (symbol addresses, root tables uploaded on `stream`, which it synchronises)
+ * and should come before any stream capture.  The set-up is kept per device
+ * ordinal for the device's primary context (the runtime's own); a caller that
+ * makes another driver context current on that device is not supported.
+ * z may be x or y, or both (x == y squares): each CTA reads the words of x
+ * and y that it later writes in z, and reads them before it writes.
  * Runs on `stream` (a cudaStream_t, NULL = default) and returns after it has
  * synchronised the stream. */
 int ctw_prp_mul_noalloc(int log2_degree, int lanes, const uint32_t *b, const int32_t *x_dev,
@@ -324,6 +335,11 @@ int ctw_server_destroy(ctw_server *s);
 /* Measured 32-bit integer multiply-add throughput of the device (IMAD/s),
  * from an in-library probe kernel; the roofline denominator. */
 double ctw_imad_peak(void);
+/* Measured throughput of 32-bit modular products (products/s) from probe
+ * kernels of independent chains: kind 0 Montgomery (the product the
+ * algorithmic count charges 4 IMAD), kind 1 Shoup with a precomputed quotient.
+ * 0.0 for another kind or without a device.  No counterpart in the reference. */
+double ctw_modmul_peak(int kind);
 
 /* ------------------------------------------------------------------------ */
 /* Sieve: strike b in [b_min, b_max] with p | b^(2^n) - b^(2^(n-1)) +- 1      */

@@ -39,15 +39,15 @@ def build(force: bool = False) -> str:
     return _LIB_PATH
 
 
-def build_ref() -> str | None:
-    """Compile the reference CPU sieve from its own source when it is present."""
+def build_ref(ref_dir: str | None) -> str | None:
+    """Compile the reference CPU sieve from its own source, ``ref_dir`` being the
+    reference checkout (the directory holding ``sieve/``); None or a missing
+    source leaves it unbuilt (a machine without the reference)."""
     if os.path.exists(_REF_PATH):
         return _REF_PATH
-    src = os.path.join(os.environ.get("CTWIN_REFERENCE", "/root/reference"), "sieve", "CPU", "ctsieve.cpp")
-    if not os.path.exists(src):
+    if not ref_dir or not os.path.exists(os.path.join(ref_dir, "sieve", "CPU", "ctsieve.cpp")):
         return None
-    subprocess.run(["make", "-s", "-C", HERE, "ref",
-                    "REF=" + os.path.dirname(os.path.dirname(os.path.dirname(src)))], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + ref_dir], check=True)
     return _REF_PATH if os.path.exists(_REF_PATH) else None
 
 

@@ -13,8 +13,16 @@ has the reference source; the outputs are committed, the GPU tests only read the
                     workload's b (sha256 of the residue's little-endian bytes + its low 64 bits)
   prefix_gmp.json   the same 4096-squaring prefix at degrees 2^17 and 2^18 (the grid
                     kernel on two and three primes), base 2
+  prefix64k_gmp.json  r_K for K = 65536 at degree 2^16 and the single-test workload's b,
+                    base 3 (the Fermat base of that workload)
+  sieve_cfg4.json   the large sieve (n = 20, p = 3k 2^20 + 1 up to 2^40, + form) of the
+                    reference CPU sieve over four seeded sub-ranges [s, s + 2^24) of
+                    [2, 2^30): sha256 of the packed survivor bitmap, survivor count, last p
+                    and md5 of sv_*.dat / cand_*.txt; the p range is cut into k slices run
+                    in parallel (the reference's own resume by _p_min_pos) and OR-ed
 
-Usage:  python tests/golden/make_golden.py [--skip-slow] [--only pool|big|prefix|cfg1]
+Usage:  CTWIN_REFERENCE=<reference checkout> python tests/golden/make_golden.py
+            [--skip-slow] [--only pool|big|prefix|cfg1|cfg4]
   (--only cfg1 extends prp_gmp.json to the first 256 twin survivors at n = 11:
    N+ base 2 and 3, N- base 2 and 3)
 """
@@ -34,11 +42,17 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-REF = os.environ.get("CTWIN_REFERENCE", "/root/reference")
+REF = os.environ.get("CTWIN_REFERENCE", "")
+
+
+def ref_dir() -> str:
+    if not REF or not os.path.isdir(REF):
+        sys.exit("set CTWIN_REFERENCE to the reference checkout (the directory holding cyclo/ and sieve/)")
+    return REF
 
 
 def algo_kat():
-    src = open(os.path.join(REF, "cyclo", "algo", "algo.cpp")).read()
+    src = open(os.path.join(ref_dir(), "cyclo", "algo", "algo.cpp")).read()
     out = {}
     for n, rhs in re.findall(r'check\((\d+),\s*"\s*=\s*([^"]+)"\)', src):
         n = int(n)
@@ -127,13 +141,91 @@ def pool_jobs():
     return jobs
 
 
+# the large sieve: n = 20, b in [2, 2^30), p = 3k 2^20 + 1 < 2^40, + form
+CFG4_N, CFG4_SPAN, CFG4_P_MAX, CFG4_SEED, CFG4_RANGES, CFG4_SLICES = 20, 1 << 24, 1 << 40, 20, 4, 16
+
+
+def cfg4_starts() -> list[int]:
+    import random
+    rng = random.Random(CFG4_SEED)
+    return [rng.randrange(2, (1 << 30) - CFG4_SPAN + 1) for _ in range(CFG4_RANGES)]
+
+
+def cfg4_slices() -> list[tuple[int, int]]:
+    """(p_min, p_max) per k slice.  check_pos runs k from (p_min >> n) / 3 to the
+    first k with 3 k 2^n + 1 >= p_max (ctsieve.cpp:680-681), so slices of whole k
+    with p_min = 3 k0 2^n + 1 and p_max = 3 (k1 - 1) 2^n + 1 are disjoint; the last
+    one keeps p_max = 2^40 and with it the reference's k past the limit."""
+    n = CFG4_N
+    k_lo = 1
+    k_hi = (CFG4_P_MAX >> n) // 3
+    while 3 * (k_hi << n) + 1 < CFG4_P_MAX:
+        k_hi += 1
+    # equal numbers of primes per slice, roughly: cut the k range evenly
+    cuts = [k_lo + (k_hi + 1 - k_lo) * i // CFG4_SLICES for i in range(CFG4_SLICES + 1)]
+    out = []
+    for i in range(CFG4_SLICES):
+        k0, k1 = cuts[i], cuts[i + 1]
+        p_max = CFG4_P_MAX if i == CFG4_SLICES - 1 else 3 * ((k1 - 1) << n) + 1
+        out.append((3 * (k0 << n) + 1, p_max))
+    return out
+
+
+def cfg4_job(job):
+    from oracle import oracle as O
+    s, p_min, p_max = job
+    tmp = tempfile.mkdtemp()
+    cwd = os.getcwd()
+    os.chdir(tmp)               # the reference's periodic write(false) lands here
+    try:
+        bits, lp, _ = O.ref_sieve(CFG4_N, s, s + CFG4_SPAN - 1, p_max, 11, 1, p_min_pos=p_min)
+    finally:
+        os.chdir(cwd)
+    return s, p_min, np.packbits(bits, bitorder="little"), lp
+
+
+def cfg4():
+    from oracle import oracle as O
+    O.build_ref(ref_dir())
+    jobs = [(s, a, b) for s in cfg4_starts() for a, b in cfg4_slices()]
+    with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
+        res = pool.map(cfg4_job, jobs)
+    out = []
+    for s in cfg4_starts():
+        mine = sorted((r for r in res if r[0] == s), key=lambda r: r[1])
+        packed = np.bitwise_or.reduce(np.stack([r[2] for r in mine]), axis=0)
+        p_last = mine[-1][3]
+        bits = np.unpackbits(packed, bitorder="little")[:CFG4_SPAN]
+        surv = np.flatnonzero(bits == 0)
+        b_max = s + CFG4_SPAN - 1
+        sv = O.sv_bytes(bits, p_last, 11)
+        cand = O.cand_text(bits, s).encode()
+        out.append({"n": CFG4_N, "b_min": s, "b_max": b_max, "p_min_pos": 3 * (1 << CFG4_N) + 1,
+                    "p_max_pos": CFG4_P_MAX, "p_last_pos": p_last, "survivors": int(surv.size),
+                    "sha256_bits": hashlib.sha256(packed.tobytes()).hexdigest(),
+                    "first_survivors": [s + int(i) for i in surv[:64]],
+                    "files": {f"sv_{CFG4_N}_{s}_{b_max}.dat": hashlib.md5(sv).hexdigest(),
+                              f"cand_{CFG4_N}_{s}_{b_max}.txt": hashlib.md5(cand).hexdigest()}})
+        print(s, p_last, surv.size, flush=True)
+    json.dump({"seed": CFG4_SEED, "span": CFG4_SPAN, "slices": CFG4_SLICES, "ranges": out},
+              open(os.path.join(HERE, "sieve_cfg4.json"), "w"), indent=1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-slow", action="store_true")
-    ap.add_argument("--only", choices=["pool", "big", "prefix", "cfg1"], default=None)
+    ap.add_argument("--only", choices=["pool", "big", "prefix", "prefix64k", "cfg1", "cfg4"], default=None)
     args = ap.parse_args()
     from oracle import oracle as O
     O.build()
+    if args.only == "cfg4":
+        cfg4()
+        return
+    if args.only == "prefix64k":
+        res = [partial_case((BIG_PARTIAL_B, 16, 3, 65536))]
+        json.dump(res, open(os.path.join(HERE, "prefix64k_gmp.json"), "w"), indent=0)
+        print("done", res)
+        return
     if args.only == "cfg1":
         path = os.path.join(HERE, "prp_gmp.json")
         old = json.load(open(path))
@@ -176,7 +268,7 @@ def main():
         json.dump(res, open(os.path.join(HERE, "pool_gmp.json"), "w"), indent=0)
         print("done", len(res), "pool cases")
         return
-    O.build_ref()
+    O.build_ref(ref_dir())
 
     json.dump(algo_kat(), open(os.path.join(HERE, "algo_kat.json"), "w"), indent=1)
 

@@ -15,29 +15,40 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("ln,lanes,csize", [(11, 3, 16), (13, 2, 8)])
-def test_mul_noalloc_matches_engine(native, ln, lanes, csize):
+# (degree, lanes, CSIZE, b range, NTT primes the b range selects, z aliases x)
+CASES = [
+    (11, 3, 16, (2 ** 17, 2 ** 30), 3, False),
+    (13, 2, 8, (2 ** 17, 2 ** 30), 3, False),
+    (14, 2, 16, (2 ** 24, 2 ** 30), 3, False),   # three primes at the largest degree
+    (14, 3, 8, (2 ** 16, 2 ** 21), 2, False),    # two primes (3 D (b+1)^2 < q0 q1)
+    (11, 4, 16, (64, 2 ** 18), 2, True),         # two primes, z written over x
+]
+
+
+@pytest.mark.parametrize("ln,lanes,csize,brange,primes,alias", CASES)
+def test_mul_noalloc_matches_engine(native, ln, lanes, csize, brange, primes, alias):
     import torch
 
     from ctwin_gb300 import PrpEngine
     from ctwin_gb300._native import check, lib
 
-    rng = random.Random(4242 + ln)
+    rng = random.Random(4242 + ln + 7 * lanes)
     D = 1 << ln
     L = lib()
     stream = torch.cuda.current_stream()
     for call in range(2):
-        b = np.array([rng.randrange(2 ** 17, 2 ** 30) for _ in range(lanes)], dtype=np.uint32)
+        b = np.array([rng.randrange(*brange) for _ in range(lanes)], dtype=np.uint32)
         x = np.array([[rng.randint(-(int(bb) // 2), int(bb) // 2) for _ in range(D)] for bb in b], dtype=np.int32)
         y = np.array([[rng.randint(-(int(bb) // 2), int(bb) // 2) for _ in range(D)] for bb in b], dtype=np.int32)
         with PrpEngine(ln, lanes, csize=csize) as eng:
             eng.set_b(b)
+            assert eng.prime_count == primes
             eng.write_regs(np.stack([x, y]), 0)
             eng.mul_regs(2, 0, 1)
             want = eng.read_regs(2, 1)[0]
         xd = torch.from_numpy(x).cuda()
         yd = torch.from_numpy(y).cuda()
-        zd = torch.zeros_like(xd)
+        zd = xd if alias else torch.zeros_like(xd)
         torch.cuda.synchronize()
         check(L.ctw_prp_mul_noalloc(ln, lanes, ctypes.c_void_p(b.ctypes.data), ctypes.c_void_p(xd.data_ptr()),
                                     ctypes.c_void_p(yd.data_ptr()), ctypes.c_void_p(zd.data_ptr()), csize,
