@@ -109,6 +109,12 @@ def lib() -> ctypes.CDLL:
             "ctw_pool_prime_count": ([H], i32),
             "ctw_pool_stream": ([H], vp),
             "ctw_pool_schedule": ([i32, u32, i32, vp, i32, vp], i32),
+            "ctw_batch_create": ([vp, i32, ctypes.POINTER(H)], i32),
+            "ctw_batch_run": ([H, i32], i32),
+            "ctw_batch_destroy": ([H], i32),
+            "ctw_batch_stream": ([H], vp),
+            "ctw_batch_launches": ([H], i64),
+            "ctw_batch_set_ctas_per_sm": ([H, i32], i32),
             "ctw_server_create": ([ctypes.c_size_t, i32, u32, i32, i32, ctypes.POINTER(H)], i32),
             "ctw_server_submit": ([H, i32, u32, ctypes.c_uint64], i32),
             "ctw_server_prepare": ([H, i32, i32], i32),

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libctwin_gb300.so")
-SOURCES = ["prp_kernels.cu", "prp_kernels_np2.cu", "prp_grid.cu", "prp_engine.cu", "sieve.cu", "prp_noalloc.cu", "prp_pool.cu", "prp_server.cu", "cyclo_files.cu", "gfsieve_files.cu"]
+SOURCES = ["prp_kernels.cu", "prp_kernels_np2.cu", "prp_grid.cu", "prp_engine.cu", "sieve.cu", "prp_noalloc.cu", "prp_pool.cu", "prp_batch.cu", "prp_server.cu", "cyclo_files.cu", "gfsieve_files.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--expt-relaxed-constexpr"]

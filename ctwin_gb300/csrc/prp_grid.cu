@@ -20,6 +20,8 @@
 // launch).  The cooperative launch guarantees that all CTAs are resident; every
 // wait is still bounded by a %globaltimer budget, after which the CTA records
 // ST_GRID_WAIT and stops waiting, so a launch always ends.
+#include <type_traits>
+
 #include "prp_device.cuh"
 
 namespace ctw {
@@ -448,19 +450,526 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 	if (err) atomicOr(a.status, err);
 }
 
+// ---------------------------------------------------------------------------
+// Grid kernel with warp-local sub-transforms (CTAs of M = 1024 or 2048
+// coefficients): the same squaring as prp_kernel_grid (registers equal), with
+// fewer CTA-wide steps per squaring:
+//   X1  digits -> residues fused into the first forward cross pass
+//   X3  the last forward cross pass stores straight to L2 (no shared copy)
+//   A   gather of row block g fused with local levels 0 .. C-1 (radix 2^C,
+//       C = LM - 8) across the CTA
+//   W   local levels C .. LM-1, the pointwise step and their inverse on
+//       sub-blocks of 256 coefficients, one warp each: three register passes
+//       (radix 8, 8, 4) with warp-synchronous exchanges through shared memory
+//   A'  inverse local levels C-1 .. 0 fused with the publication of the row
+//   Y1  gather of the columns fused with the first inverse cross pass
+//   Y2  the last inverse cross pass (with the final scale) fused with Garner,
+//       one item per column group holding every prime
+//   N   normalize1 with the chunk loaded ahead of its carry chain, then the
+//       run-end carries are published by one otherwise idle thread while the
+//       others carry into the chunks that need no remote carry.
+// Shared memory: XC [NP][G][MG] column runs (natural order, Garner words in
+// place), XR [NP][M] row block (sub-block swizzle sbx), XD [M] digits at rest
+// (column-run order), chunk and run-end carries, cross and local roots.
+// ---------------------------------------------------------------------------
+
+// word of position p (0..255) inside a sub-block: 4-word groups XOR-permuted
+// by the 32-word row, so that the three register layouts of a warp (p = lane +
+// 32 k, 32 c + r + 4 k, 8 lane + k) and the pair stores of A are free of bank
+// conflicts, and aligned quads stay aligned
+__device__ __forceinline__ int sbx(int p) { return p ^ (((p >> 5) & 7) << 2); }
+
+__device__ __forceinline__ uint2 ld_l2_u2(const uint32_t *p)
+{
+#if !defined(CTW_EMU)
+	return __ldcg(reinterpret_cast<const uint2 *>(p));
+#else
+	return *reinterpret_cast<const uint2 *>(p);
+#endif
+}
+__device__ __forceinline__ void st_l2_u2(uint32_t *p, uint2 v)
+{
+#if !defined(CTW_EMU)
+	__stcg(reinterpret_cast<uint2 *>(p), v);
+#else
+	*reinterpret_cast<uint2 *>(p) = v;
+#endif
+}
+__device__ __forceinline__ uint32_t ld_l2_u1(const uint32_t *p)
+{
+#if !defined(CTW_EMU)
+	return __ldcg(p);
+#else
+	return *p;
+#endif
+}
+__device__ __forceinline__ void st_l2_u1(uint32_t *p, uint32_t v)
+{
+#if !defined(CTW_EMU)
+	__stcg(p, v);
+#else
+	*p = v;
+#endif
+}
+__device__ __forceinline__ void warp_sync()
+{
+#if defined(CTW_EMU)
+	emu_syncwarp();
+#else
+	__syncwarp();
+#endif
+}
+
+__host__ __device__ __forceinline__ size_t grid2_words(int lg, int lm, int np)
+{
+	const size_t M = (size_t)1 << lm, G = (size_t)1 << lg;
+	// XC, XR, XD, chunk carries (M/8 int64), run-end carries (G int64), cross roots, TF + TI
+	return 2 * np * M + M + M / 4 + 2 * G + 2 * np * G + 2 * np * M;
+}
+
+// Normalize1 of one chunk of CSZ Garner words (64-bit, two primes or narrow
+// three primes): the words are loaded first, then the carry chain runs on
+// registers.  Returns the chunk's carry.
+template <int CSZ>
+__device__ __forceinline__ int64_t norm1_chunk64(const uint32_t *W0, const uint32_t *W1, int32_t *XDo, int mult,
+                                                  uint32_t b, uint32_t b_inv, int b_s, uint32_t &err)
+{
+	int64_t v[CSZ];
+#pragma unroll
+	for (int i = 0; i < CSZ; ++i) v[i] = (int64_t)((uint64_t)W0[i] | ((uint64_t)W1[i] << 32));
+	int64_t acc = 0;
+#pragma unroll
+	for (int i = 0; i < CSZ; ++i)
+	{
+		acc += v[i] * (int64_t)mult;
+		XDo[i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+	}
+	return acc;
+}
+
+template <int LG, int NP, int LM>
+__global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(const PrpKernelArgs a, const PrpGridArgs ga)
+{
+	static_assert(LM == 10 || LM == 11, "CTAs of 1024 or 2048 coefficients");
+	static_assert(LG >= 4 && LG <= 7, "grid shape");
+	constexpr int G = 1 << LG, M = 1 << LM, MG = M >> LG, D = M * G, C = LM - 8, NSB = 1 << C;
+	constexpr int NPASS = XPass<LG, 0>::np, PL = NPASS - 1;
+	static_assert(NPASS >= 2 && NPASS <= 3, "two or three cross passes");
+	extern __shared__ __align__(16) uint32_t sm[];
+	__shared__ int dead;
+	const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane32 = tid & 31, nwarps = nt >> 5;
+	const int lane = blockIdx.x / G, g = blockIdx.x % G;
+	const int csz = a.csize, runc = MG / csz, ncl = G * runc, cb = g * MG;
+
+	uint32_t *XC = sm;                                          // [NP][G][MG]
+	uint32_t *XR = XC + NP * M;                                 // [NP][M] (sub-block swizzle)
+	int32_t *XD = reinterpret_cast<int32_t *>(XR + NP * M);     // [G][MG] digits
+	int64_t *fch = reinterpret_cast<int64_t *>(XD + M);         // [M/8]
+	int64_t *xch = fch + M / 8;                                 // [G]
+	uint32_t *XRT = reinterpret_cast<uint32_t *>(xch + G);      // [NP][2][G]
+	uint32_t *TF = XRT + NP * 2 * G;                            // [NP][M]
+	uint32_t *TI = TF + NP * M;
+	if (tid == 0) dead = 0;
+
+	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
+	const int b_s = (int)a.lane_b[4 * lane + 2];
+	const bool narrow = NP == 2 || (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;
+	uint32_t err = 0;
+
+	{
+		const uint32_t *tfg = a.tf + (size_t)g * 3 * M, *tig = a.ti + (size_t)g * 3 * M;
+		for (int i = tid; i < NP * M; i += nt) { TF[i] = tfg[i]; TI[i] = tig[i]; }
+		for (int i = tid; i < NP * 2 * G; i += nt) XRT[i] = ga.xr[(i / G) * 128 + i % G];
+	}
+
+	uint32_t *gx = ga.gx + (size_t)lane * G * 3 * M;
+	uint32_t *gr = ga.gr + (size_t)lane * G * 3 * M;
+	long long *gc = ga.gc + (size_t)lane * G * G;
+	unsigned *bar = ga.bar + (size_t)lane * GRID_BAR_WORDS;
+	unsigned *cpub = bar + 32;
+	unsigned nbar = 0, ncar = 0;
+	auto gsync = [&]() {
+		++nbar;
+		grid_arrive(bar);
+		grid_wait(bar, nbar * (unsigned)G, err, &dead);
+	};
+	uint32_t *scr = a.scratch ? a.scratch + ((size_t)lane * G + g) * 3 * M : nullptr;
+	const size_t lane_base = (size_t)lane * D;
+
+	auto load_digits = [&](const int32_t *src) {
+		for (int e = tid; e < M; e += nt)
+		{
+			const int h = e / MG, tt = e - h * MG;
+			XD[e] = src[lane_base + (size_t)h * M + cb + tt];
+		}
+	};
+
+	// cross pass P over XC (or from the digits / to L2), direction dir
+	auto xpass = [&](auto PC, int dir, auto load, auto store) {
+		constexpr int P = decltype(PC)::value;
+		constexpr int R = XPass<LG, P>::R, r = Log2<R>::v, l0 = XPass<LG, P>::l0, NGR = G >> r;
+		constexpr int lsh = LG - l0 - r, stride = 1 << lsh;
+		for (int it = tid; it < NP * NGR * MG; it += nt)
+		{
+			const int pi = it / (NGR * MG);
+			const int rem = it - pi * NGR * MG;
+			const int gam = rem / MG, tt = rem - gam * MG;
+			const int jblk = gam >> lsh, i = gam & (stride - 1);
+			const int hbase = (jblk << (LG - l0)) + i;
+			const uint32_t q = qv(pi), qi = qiv(pi);
+			const uint32_t *tw = XRT + (pi * 2 + dir) * G;
+			auto idx = [&](int t, int kk) { return (1 << (l0 + t)) + (jblk << t) + kk; };
+			uint32_t u[R];
+#pragma unroll
+			for (int k = 0; k < R; ++k) u[k] = load(pi, hbase + k * stride, tt, q);
+			if (dir == 0) group_fwd<R>(u, tw, idx, q, qi, l0 == 0, a.omega[pi]);
+			else group_inv<R>(u, tw, idx, q, qi, l0 == 0, a.omega[pi], a.k1[pi], a.sc[pi]);
+#pragma unroll
+			for (int k = 0; k < R; ++k) store(pi, hbase + k * stride, tt, u[k]);
+		}
+	};
+	auto ld_xc = [&](int pi, int h, int tt, uint32_t) { return XC[pi * M + h * MG + tt]; };
+	auto st_xc = [&](int pi, int h, int tt, uint32_t v) { XC[pi * M + h * MG + tt] = v; };
+
+	// W: local levels C .. LM-1 of sub-block (pi, sb), pointwise, inverse
+	auto wphase = [&](int pi, int sb, int mode) {
+		const uint32_t q = qv(pi), qi = qiv(pi);
+		uint32_t *S = XR + pi * M + sb * 256;
+		const uint32_t *tf = TF + pi * M + sb * 256, *ti = TI + pi * M + sb * 256;
+		const int l = lane32, c4 = l >> 2, r4 = l & 3;
+		uint32_t u[8];
+		// W1: p = l + 32 k, levels C .. C+2
+#pragma unroll
+		for (int k = 0; k < 8; ++k) u[k] = S[sbx(l + 32 * k)];
+		group_fwd<8>(u, tf, [&](int t, int kk) { return (1 << t) + kk; }, q, qi, false, 0);
+#pragma unroll
+		for (int k = 0; k < 8; ++k) S[sbx(l + 32 * k)] = u[k];
+		warp_sync();
+		// W2: p = 32 c + r + 4 k, levels C+3 .. C+5
+#pragma unroll
+		for (int k = 0; k < 8; ++k) u[k] = S[sbx(32 * c4 + r4 + 4 * k)];
+		group_fwd<8>(u, tf, [&](int t, int kk) { return (8 << t) + (c4 << t) + kk; }, q, qi, false, 0);
+#pragma unroll
+		for (int k = 0; k < 8; ++k) S[sbx(32 * c4 + r4 + 4 * k)] = u[k];
+		warp_sync();
+		// W3: p = 8 l + k, levels C+6, C+7 as two radix-4 groups, pointwise, inverse
+		{
+			const uint4 lo = *reinterpret_cast<const uint4 *>(S + sbx(8 * l));
+			const uint4 hi = *reinterpret_cast<const uint4 *>(S + sbx(8 * l + 4));
+			u[0] = lo.x; u[1] = lo.y; u[2] = lo.z; u[3] = lo.w;
+			u[4] = hi.x; u[5] = hi.y; u[6] = hi.z; u[7] = hi.w;
+		}
+#pragma unroll
+		for (int e = 0; e < 2; ++e)
+		{
+			uint32_t *v = u + 4 * e;
+			const uint32_t w6 = tf[64 + 32 * e + l];
+			bf_fwd(v[0], v[2], w6, q, qi);
+			bf_fwd(v[1], v[3], w6, q, qi);
+			bf_fwd(v[0], v[1], tf[128 + 32 * (2 * e) + l], q, qi);
+			bf_fwd(v[2], v[3], tf[128 + 32 * (2 * e + 1) + l], q, qi);
+		}
+		uint32_t *Y = scr + pi * M + sb * 256 + 8 * l;          // the transform of y, logical order
+		if (mode == LM_FWD_ONLY)
+		{
+			uint32_t o[8];
+#pragma unroll
+			for (int k = 0; k < 8; ++k) o[k] = red(u[k], 2 * q);
+			*reinterpret_cast<uint4 *>(Y) = make_uint4(o[0], o[1], o[2], o[3]);
+			*reinterpret_cast<uint4 *>(Y + 4) = make_uint4(o[4], o[5], o[6], o[7]);
+			return;
+		}
+		if (mode == LM_SQUARE)
+		{
+#pragma unroll
+			for (int k = 0; k < 8; ++k) { const uint32_t v = red(u[k], 2 * q); u[k] = mlazy(v, v, q, qi); }
+		}
+		else
+		{
+			const uint4 ylo = *reinterpret_cast<const uint4 *>(Y), yhi = *reinterpret_cast<const uint4 *>(Y + 4);
+			const uint32_t y[8] = { ylo.x, ylo.y, ylo.z, ylo.w, yhi.x, yhi.y, yhi.z, yhi.w };
+#pragma unroll
+			for (int k = 0; k < 8; ++k) u[k] = mlazy(red(u[k], 2 * q), y[k], q, qi);
+		}
+#pragma unroll
+		for (int e = 0; e < 2; ++e)
+		{
+			uint32_t *v = u + 4 * e;
+			bf_inv(v[0], v[1], ti[128 + 32 * (2 * e) + l], q, qi);
+			bf_inv(v[2], v[3], ti[128 + 32 * (2 * e + 1) + l], q, qi);
+			const uint32_t w6 = ti[64 + 32 * e + l];
+			bf_inv(v[0], v[2], w6, q, qi);
+			bf_inv(v[1], v[3], w6, q, qi);
+		}
+		*reinterpret_cast<uint4 *>(S + sbx(8 * l)) = make_uint4(u[0], u[1], u[2], u[3]);
+		*reinterpret_cast<uint4 *>(S + sbx(8 * l + 4)) = make_uint4(u[4], u[5], u[6], u[7]);
+		warp_sync();
+#pragma unroll
+		for (int k = 0; k < 8; ++k) u[k] = S[sbx(32 * c4 + r4 + 4 * k)];
+		group_inv<8>(u, ti, [&](int t, int kk) { return (8 << t) + (c4 << t) + kk; }, q, qi, false, 0, 0, 0);
+#pragma unroll
+		for (int k = 0; k < 8; ++k) S[sbx(32 * c4 + r4 + 4 * k)] = u[k];
+		warp_sync();
+#pragma unroll
+		for (int k = 0; k < 8; ++k) u[k] = S[sbx(l + 32 * k)];
+		group_inv<8>(u, ti, [&](int t, int kk) { return (1 << t) + kk; }, q, qi, false, 0, 0, 0);
+#pragma unroll
+		for (int k = 0; k < 8; ++k) S[sbx(l + 32 * k)] = u[k];
+	};
+
+	// a roots index of the local levels L < C, block J: word 256 (2^L + J)
+	auto aidx = [&](int t, int kk) { return ((1 << t) + kk) * 256; };
+
+	auto transform_and_normalize = [&](int mode, int mult) {
+		__syncthreads();
+		// X1: digits -> residues, first forward cross pass
+		xpass(std::integral_constant<int, 0>{}, 0,
+		      [&](int, int h, int tt, uint32_t q) { return modq_i32(XD[h * MG + tt], q); }, st_xc);
+		__syncthreads();
+		if constexpr (NPASS == 3)
+		{
+			xpass(std::integral_constant<int, 1>{}, 0, ld_xc, st_xc);
+			__syncthreads();
+		}
+		// X3: last forward cross pass, columns published to L2
+		xpass(std::integral_constant<int, PL>{}, 0, ld_xc, [&](int pi, int h, int tt, uint32_t v) {
+			st_l2_u1(gx + (size_t)g * 3 * M + pi * M + h * MG + tt, v);
+		});
+		gsync();
+		// A: gather row block g (pairs of coefficients m0, m0 + 1 of every sub-block j),
+		// local levels 0 .. C-1
+		for (int it = tid; it < NP * 128; it += nt)
+		{
+			const int pi = it >> 7, m0 = 2 * (it & 127);
+			const uint32_t q = qv(pi), qi = qiv(pi);
+			uint32_t v0[NSB], v1[NSB];
+#pragma unroll
+			for (int j = 0; j < NSB; ++j)
+			{
+				const int m = j * 256 + m0, c = m / MG, tt = m - c * MG;
+				const uint2 w = ld_l2_u2(gx + (size_t)c * 3 * M + pi * M + g * MG + tt);
+				v0[j] = w.x;
+				v1[j] = w.y;
+			}
+			group_fwd<NSB>(v0, TF + pi * M, aidx, q, qi, false, 0);
+			group_fwd<NSB>(v1, TF + pi * M, aidx, q, qi, false, 0);
+#pragma unroll
+			for (int j = 0; j < NSB; ++j)
+				*reinterpret_cast<uint2 *>(XR + pi * M + j * 256 + sbx(m0)) = make_uint2(v0[j], v1[j]);
+		}
+		__syncthreads();
+		// W: one warp per sub-block
+		for (int wt = warp; wt < NP * NSB; wt += nwarps) wphase(wt / NSB, wt % NSB, mode);
+		if (mode == LM_FWD_ONLY) return;
+		__syncthreads();
+		// A': inverse local levels C-1 .. 0, row published to L2 (natural order)
+		for (int it = tid; it < NP * 128; it += nt)
+		{
+			const int pi = it >> 7, m0 = 2 * (it & 127);
+			const uint32_t q = qv(pi), qi = qiv(pi);
+			uint32_t v0[NSB], v1[NSB];
+#pragma unroll
+			for (int j = 0; j < NSB; ++j)
+			{
+				const uint2 w = *reinterpret_cast<const uint2 *>(XR + pi * M + j * 256 + sbx(m0));
+				v0[j] = w.x;
+				v1[j] = w.y;
+			}
+			group_inv<NSB>(v0, TI + pi * M, aidx, q, qi, false, 0, 0, 0);
+			group_inv<NSB>(v1, TI + pi * M, aidx, q, qi, false, 0, 0, 0);
+#pragma unroll
+			for (int j = 0; j < NSB; ++j)
+				st_l2_u2(gr + (size_t)g * 3 * M + pi * M + j * 256 + m0, make_uint2(v0[j], v1[j]));
+		}
+		gsync();
+		// Y1: gather the columns, first inverse cross pass
+		xpass(std::integral_constant<int, PL>{}, 1, [&](int pi, int h, int tt, uint32_t) {
+			return ld_l2_u1(gr + (size_t)h * 3 * M + pi * M + g * MG + tt);
+		}, st_xc);
+		__syncthreads();
+		if constexpr (NPASS == 3)
+		{
+			xpass(std::integral_constant<int, 1>{}, 1, ld_xc, st_xc);
+			__syncthreads();
+		}
+		// Y2: last inverse cross pass (levels of pass 0, with the final scale) and
+		// Garner, one item per (column, row group) holding every prime
+		{
+			constexpr int R = XPass<LG, 0>::R, r = Log2<R>::v, NGR = G >> r, lsh = LG - r, stride = 1 << lsh;
+			for (int it = tid; it < NGR * MG; it += nt)
+			{
+				const int gam = it / MG, tt = it - gam * MG;
+				const int hbase = gam;                          // pass 0: jblk = 0, i = gam
+				uint32_t u[NP][R];
+#pragma unroll
+				for (int pi = 0; pi < NP; ++pi)
+				{
+					const uint32_t q = qv(pi), qi = qiv(pi);
+#pragma unroll
+					for (int k = 0; k < R; ++k) u[pi][k] = XC[pi * M + (hbase + k * stride) * MG + tt];
+					group_inv<R>(u[pi], XRT + (pi * 2 + 1) * G, [&](int t, int kk) { return (1 << t) + kk; }, q, qi,
+					             true, a.omega[pi], a.k1[pi], a.sc[pi]);
+				}
+#pragma unroll
+				for (int k = 0; k < R; ++k)
+				{
+					const int pos = (hbase + k * stride) * MG + tt;
+					uint32_t w0, w1;
+					if constexpr (NP == 3)
+					{
+						uint32_t w2;
+						garner3(u[0][k], u[1][k], u[2][k], a, narrow, w0, w1, w2);
+						XC[2 * M + pos] = w2;
+					}
+					else garner2(u[0][k], u[1][k], a, w0, w1);
+					XC[pos] = w0;
+					XC[M + pos] = w1;
+				}
+			}
+		}
+		__syncthreads();
+		// N: normalize1 over the runs; the last chunk of run h keeps its carry in xch
+		for (int c = tid; c < ncl; c += nt)
+		{
+			const int h = c / runc, j = c - h * runc;
+			const int base = h * MG + j * csz;
+			int64_t f;
+			if (narrow && csz == 8) f = norm1_chunk64<8>(XC + base, XC + M + base, XD + base, mult, b, b_inv, b_s, err);
+			else if (narrow && csz == 16)
+				f = norm1_chunk64<16>(XC + base, XC + M + base, XD + base, mult, b, b_inv, b_s, err);
+			else if (narrow)
+			{
+				int64_t acc = 0;
+				for (int i = 0; i < csz; ++i)
+				{
+					acc += load64(XC + base, M, i) * (int64_t)mult;
+					XD[base + i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+				}
+				f = acc;
+			}
+			else
+			{
+				i128 acc = 0;
+				if constexpr (NP == 3)
+					for (int i = 0; i < csz; ++i)
+					{
+						acc += load96(XC + base, M, i) * (i128)mult;
+						XD[base + i] = reduce_b<i128>(acc, b, b_inv, b_s, err);
+					}
+				f = (int64_t)acc;
+				if ((i128)f != acc) err |= ST_DIGIT_RANGE;
+			}
+			fch[c] = f;
+			if (j == runc - 1) xch[h] = f;
+		}
+		__syncthreads();
+		// normalize2 (as prp_kernel_grid): the run-end carries are published by the
+		// last thread (fence and count) while threads 0 .. ncl - G - 1 carry into the
+		// chunks j > 0, which need no remote carry
+		for (int h = tid; h < G; h += nt) gc[(size_t)g * G + h] = xch[h];
+		auto carry_in = [&](int h, int j, int64_t acc) {
+			int32_t *Xh = XD + h * MG + j * csz;
+			int i = 0;
+			bool done = false;
+			for (; i < csz - 1; ++i)
+			{
+				acc += Xh[i];
+				Xh[i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+				if (acc == 0) { done = true; break; }
+			}
+			if (!done)
+			{
+				const int64_t s = (int64_t)Xh[csz - 1] + (int64_t)(int32_t)(int64_t)acc;
+				if (s != (int32_t)s) err |= ST_DIGIT_RANGE;
+				Xh[csz - 1] = (int32_t)s;
+			}
+		};
+		++ncar;
+		__syncthreads();
+		if (tid == nt - 1)
+		{
+			__threadfence();
+			atomicAdd(cpub + g, 1u);
+		}
+		const int nin = ncl - G;                                 // chunks j > 0
+		const int nw = nin < nt - 1 ? nin : nt - 1;              // threads that carry (not the publisher)
+		for (int k = tid; k < nin && tid < nw; k += nw)
+		{
+			const int h = k / (runc - 1), j = k - h * (runc - 1) + 1;
+			carry_in(h, j, fch[h * runc + j - 1]);
+		}
+		grid_wait(cpub + (g + G - 1) % G, ncar, err, &dead);
+		for (int h = tid; h < G; h += nt)
+		{
+			int64_t acc;
+			if (g > 0) acc = ld_l2_ll(gc + (size_t)(g - 1) * G + h);
+			else
+			{
+				const int64_t last = ld_l2_ll(gc + (size_t)(G - 1) * G + (G - 1));
+				if (h == 0) acc = -last;
+				else
+				{
+					acc = ld_l2_ll(gc + (size_t)(G - 1) * G + (h - 1));
+					if (h == G / 2) acc += last;
+				}
+			}
+			carry_in(h, 0, acc);
+		}
+	};
+
+	if (a.op == OP_MUL)
+	{
+		load_digits(a.reg_y);
+		transform_and_normalize(LM_FWD_ONLY, 1);
+		gsync();              // every CTA has gathered y's row block before the columns are rewritten
+		load_digits(a.reg_in);
+		transform_and_normalize(LM_MUL, 1);
+	}
+	else
+	{
+		load_digits(a.reg_in);
+		for (int it = 0; it < a.count; ++it)
+		{
+			const long long i = a.i_hi - it;
+			int bit = 0;
+			if (a.use_dupmask) bit = (int)((a.dupmask[lane >> 6] >> (lane & 63)) & 1);
+			else if (i >= 0 && (i >> 5) < a.nwords) bit = (a.bits[(size_t)lane * a.nwords + (i >> 5)] >> (i & 31)) & 1;
+			transform_and_normalize(LM_SQUARE, bit ? a.mult : 1);
+		}
+	}
+	__syncthreads();
+	for (int e = tid; e < M; e += nt)
+	{
+		const int h = e / MG, tt = e - h * MG;
+		a.reg_out[lane_base + (size_t)h * M + cb + tt] = XD[e];
+	}
+	if (err) atomicOr(a.status, err);
+}
+
 // Shared memory a grid CTA asks for: at least 116 KB, so that an SM holds one
 // CTA and the grid spreads over 2^lg SMs.
 constexpr size_t GRID_SMEM_MIN = 116 * 1024;
 size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np)
 {
-	const size_t b = grid_words(lg, lm, tw_smem, np) * 4;
+	const size_t b = (lm == 12 ? grid_words(lg, lm, tw_smem, np) : grid2_words(lg, lm, np)) * 4;
 	return b > GRID_SMEM_MIN ? b : GRID_SMEM_MIN;
 }
+
+// The kernel of a grid shape: the warp-local kernel for CTAs of 1024 and 2048
+// coefficients, the radix-16 kernel for 4096.
+template <int LG, int NP, int LM> struct GridKern {
+	typedef void (*Fn)(const PrpKernelArgs, const PrpGridArgs);
+	static Fn fn()
+	{
+		if constexpr (LM == 12) return prp_kernel_grid<LG, NP, LM>;
+		else return prp_kernel_grid2<LG, NP, LM>;
+	}
+};
 
 template <int LG, int NP, int LM>
 static cudaError_t grid_launch_t(const PrpKernelArgs &a, const PrpGridArgs &ga, int lanes, cudaStream_t stream)
 {
-	void (*kern)(const PrpKernelArgs, const PrpGridArgs) = prp_kernel_grid<LG, NP, LM>;
+	void (*kern)(const PrpKernelArgs, const PrpGridArgs) = GridKern<LG, NP, LM>::fn();
 	PrpKernelArgs a2 = a;
 	a2.tw_smem = prp_grid_smem_bytes(LG, LM, 1, NP) <= 227 * 1024 ? 1 : 0;
 	a2.swz_b = GridSwz<LG, LM>::v;          // the generic local passes read it
@@ -492,7 +1001,7 @@ static bool grid_pick(int lg, int lm, int np, GridLaunch *launch, GridKernel *ke
 	if (lg == LG_ && lm == LM_)                                                                                  \
 	{                                                                                                          \
 		if (launch) *launch = two ? grid_launch_t<LG_, 2, LM_> : grid_launch_t<LG_, 3, LM_>;                     \
-		if (kern) *kern = two ? prp_kernel_grid<LG_, 2, LM_> : prp_kernel_grid<LG_, 3, LM_>;                     \
+		if (kern) *kern = two ? GridKern<LG_, 2, LM_>::fn() : GridKern<LG_, 3, LM_>::fn();                       \
 		return true;                                                                                           \
 	}
 	CTW_GRID_CASE(5, 12)

@@ -29,18 +29,15 @@ template <bool M12, int NP, int LG, bool DENSE> struct PrpBounds {
 // DENSE (M12, three primes): launched with the root tables and the Shoup
 // tables in global memory, so that two CTAs fit an SM; for pools whose lanes
 // fill the GPU.
+// The body of prp_kernel for lane `lane`, CTA g of its cluster (0 for one
+// CTA); shared by the kernel below and the batch kernel (prp_batch.cu).
 template <int LG, bool M12, int NP, bool DENSE = false>
-__global__ void __launch_bounds__(PrpBounds<M12, NP, LG, DENSE>::threads, PrpBounds<M12, NP, LG, DENSE>::blocks)
-    prp_kernel(const PrpKernelArgs a)
+__device__ __forceinline__ void prp_body(const PrpKernelArgs &a, uint32_t *sm, const int lane, const int g)
 {
 	constexpr int G = 1 << LG;
 	static_assert(NP == 3 || LG == 0, "two-prime launches use one CTA or the column layout");
-	extern __shared__ __align__(16) uint32_t sm[];
 	const int lm = M12 ? 12 : a.lm, M = 1 << lm, D = M * G;   // compile-time sizes on the 4096 path
 	const int tid = threadIdx.x, nt = blockDim.x;
-	int g = 0;
-	if constexpr (LG > 0) g = (int)cg::this_cluster().block_rank();
-	const int lane = blockIdx.x / G;
 	const int ncl = M / a.csize, sb = M12 ? 3 : a.swz_b;
 
 	uint32_t *X = sm;                                           // [NP][M] swizzled planes
@@ -235,6 +232,16 @@ __global__ void __launch_bounds__(PrpBounds<M12, NP, LG, DENSE>::threads, PrpBou
 	csync<LG>();
 }
 
+template <int LG, bool M12, int NP, bool DENSE = false>
+__global__ void __launch_bounds__(PrpBounds<M12, NP, LG, DENSE>::threads, PrpBounds<M12, NP, LG, DENSE>::blocks)
+    prp_kernel(const PrpKernelArgs a)
+{
+	extern __shared__ __align__(16) uint32_t sm[];
+	int g = 0;
+	if constexpr (LG > 0) g = (int)cg::this_cluster().block_rank();
+	prp_body<LG, M12, NP, DENSE>(a, sm, (int)blockIdx.x >> LG, g);
+}
+
 // ---------------------------------------------------------------------------
 // Cluster kernel with the residue at rest in column layout (G > 1, M <= 8192).
 // CTA g holds, for every row block h, the run of coefficients
@@ -255,17 +262,19 @@ __host__ __device__ __forceinline__ size_t cols_words(int lm, int lg, int tw_sme
 
 // DENSE: compiled for two CTAs per SM (64 registers) and launched with the
 // root tables in global memory, for pools whose many lanes fill the GPU.
+// The body of prp_kernel_cols for lane `lane` on the CTAs of cluster ranks
+// rbase .. rbase + G - 1, this CTA being the g-th of them; shared by the
+// kernel below (rbase 0) and the batch kernel (prp_batch.cu), whose clusters
+// hold several lanes.  Cluster barriers span the whole cluster: every lane of
+// a cluster runs the same number of squarings.
 template <int LG, bool M12, int NP, bool DENSE = false>
-__global__ void __launch_bounds__(M12 ? ((DENSE && NP == 3) ? 384 : NP * 256) : NT_MAX, DENSE ? 2 : 1)
-    prp_kernel_cols(const PrpKernelArgs a)
+__device__ __forceinline__ void cols_body(const PrpKernelArgs &a, uint32_t *sm, const int lane, const int g,
+                                          const int rbase)
 {
 	constexpr int G = 1 << LG;
-	extern __shared__ __align__(16) uint32_t sm[];
 	const int lm = M12 ? 12 : a.lm, M = 1 << lm, D = M * G, MG = M >> LG;   // compile-time on the 4096 path
 	const int tid = threadIdx.x, nt = blockDim.x;
 	cg::cluster_group cl = cg::this_cluster();
-	const int g = (int)cl.block_rank();
-	const int lane = blockIdx.x / G;
 	const int csz = a.csize, sb = M12 ? 3 : a.swz_b;
 	const int runc = MG / csz;                                  // chunks per run
 	const int ncl = G * runc;                                   // chunks held by this CTA
@@ -383,7 +392,7 @@ __global__ void __launch_bounds__(M12 ? ((DENSE && NP == 3) ? 384 : NP * 256) : 
 			{
 				const int pc_ = v / MG4, o = (v - pc_ * MG4) * 4;
 				const int pi = pc_ / G, c = pc_ - pi * G;
-				const uint4 val = *reinterpret_cast<const uint4 *>(cl.map_shared_rank(XC + pi * M + g * MG + o, c));
+				const uint4 val = *reinterpret_cast<const uint4 *>(cl.map_shared_rank(XC + pi * M + g * MG + o, rbase + c));
 				*reinterpret_cast<uint4 *>(XR + pi * M + c * MG + o) = val;
 			}
 		}
@@ -399,7 +408,7 @@ __global__ void __launch_bounds__(M12 ? ((DENSE && NP == 3) ? 384 : NP * 256) : 
 			{
 				const int ph = v / MG4, o = (v - ph * MG4) * 4;
 				const int pi = ph / G, h = ph - pi * G;
-				const uint4 val = *reinterpret_cast<const uint4 *>(cl.map_shared_rank(XR + pi * M + g * MG + o, h));
+				const uint4 val = *reinterpret_cast<const uint4 *>(cl.map_shared_rank(XR + pi * M + g * MG + o, rbase + h));
 				*reinterpret_cast<uint4 *>(XC + pi * M + h * MG + o) = val;
 			}
 		}
@@ -518,14 +527,14 @@ __global__ void __launch_bounds__(M12 ? ((DENSE && NP == 3) ? 384 : NP * 256) : 
 			// a chunk carry plus digits: |acc| < 2^62, 64-bit arithmetic is exact
 			int64_t acc;
 			if (j > 0) acc = fch[c - 1];
-			else if (g > 0) acc = *cl.map_shared_rank(xch + h, g - 1);
+			else if (g > 0) acc = *cl.map_shared_rank(xch + h, rbase + g - 1);
 			else
 			{
-				const int64_t last = *cl.map_shared_rank(xch + hl, G - 1);
+				const int64_t last = *cl.map_shared_rank(xch + hl, rbase + G - 1);
 				if (h == 0) acc = a.minus ? last : -last;
 				else
 				{
-					acc = *cl.map_shared_rank(xch + (h - 1), G - 1);
+					acc = *cl.map_shared_rank(xch + (h - 1), rbase + G - 1);
 					if (h == hw) acc += last;
 				}
 			}
@@ -580,6 +589,14 @@ __global__ void __launch_bounds__(M12 ? ((DENSE && NP == 3) ? 384 : NP * 256) : 
 	}
 	if (err) atomicOr(a.status, err);
 	cl.sync();                    // peers may still read this CTA's carries
+}
+
+template <int LG, bool M12, int NP, bool DENSE = false>
+__global__ void __launch_bounds__(M12 ? ((DENSE && NP == 3) ? 384 : NP * 256) : NT_MAX, DENSE ? 2 : 1)
+    prp_kernel_cols(const PrpKernelArgs a)
+{
+	extern __shared__ __align__(16) uint32_t sm[];
+	cols_body<LG, M12, NP, DENSE>(a, sm, (int)blockIdx.x >> LG, (int)cg::this_cluster().block_rank(), 0);
 }
 
 template <int LG, bool M12, bool COLS, int NP, bool DENSE = false>

@@ -34,6 +34,7 @@
 #include "../../include/ctwin_gb300.h"
 #include "bignum.h"
 #include "prp_arith.cuh"
+#include "prp_batch.h"
 #include "prp_host.h"
 #include "prp_kernels.cuh"
 #include "prp_pool.h"
@@ -618,43 +619,53 @@ int ctw_pool_admit_many(ctw_pool *p, const uint32_t *b, const uint64_t *tags, in
 	return n;
 }
 
+// The host half of T ticks from buffer k = seq_issued & 1 (after that
+// buffer's previous launch has completed): the register moves and exponent
+// slices of every active slot, and the launch width and prime count.
+static int plan_ticks(ctw_pool *p, int T, int &k, int &lanes, int &np)
+{
+	const size_t S = (size_t)p->slots;
+	k = (int)(p->seq_issued & 1);
+	if (p->ev_pending[k])
+	{
+		POOL_CUDA(cudaEventSynchronize(p->ev[k]));
+		p->ev_pending[k] = false;
+		p->seq_complete = std::max(p->seq_complete, p->ev_seq[k] + 1);
+	}
+	int hi = 0;
+	for (int s = 0; s < p->slots; ++s)
+		if (p->slot[(size_t)s].state != SLOT_FREE) hi = s + 1;
+	// launch over the lowest slots only, in steps of 8 lanes (one graph per step)
+	lanes = std::min(p->slots, std::max(8, (hi + 7) / 8 * 8));
+	np = pool_primes(p, lanes);
+	memset(p->h_aux[k], 0, (size_t)T * 2 * S * sizeof(PrpLaneAux));
+	memset(p->h_stage[k], 0, (size_t)T * S * p->nws * 4);
+	for (int t = 0; t < T; ++t)
+		for (int s = 0; s < hi; ++s)
+		{
+			PoolSlot &sl = p->slot[(size_t)s];
+			if (sl.state != SLOT_ACTIVE) continue;
+			const SlotTick tk = slot_tick(sl, p->B);
+			PrpLaneAux *ax = p->h_aux[k] + (size_t)t * 2 * S;
+			ax[s] = PrpLaneAux{ tk.before, 1u };
+			ax[S + s] = PrpLaneAux{ tk.after, 1u };
+			bit_slice(tk.source ? sl.t.res : sl.t.E, tk.lo, p->B,
+			          p->h_stage[k] + ((size_t)t * S + s) * p->nws, p->nws);
+			p->squarings += p->B + 1;
+			if (tk.last) sl.done_seq = p->seq_issued;
+		}
+	return CTW_OK;
+}
+
 int ctw_pool_run(ctw_pool *p, int ticks)
 {
 	if (!p) return fail(CTW_E_ARG, "null pool");
 	if (ticks < 0) return fail(CTW_E_ARG, "negative tick count");
-	const size_t S = (size_t)p->slots;
 	while (ticks > 0)
 	{
 		const int T = std::min(ticks, POOL_TMAX);
-		const int k = (int)(p->seq_issued & 1);
-		if (p->ev_pending[k])
-		{
-			POOL_CUDA(cudaEventSynchronize(p->ev[k]));
-			p->ev_pending[k] = false;
-			p->seq_complete = std::max(p->seq_complete, p->ev_seq[k] + 1);
-		}
-		int hi = 0;
-		for (int s = 0; s < p->slots; ++s)
-			if (p->slot[(size_t)s].state != SLOT_FREE) hi = s + 1;
-		// launch over the lowest slots only, in steps of 8 lanes (one graph per step)
-		const int lanes = std::min(p->slots, std::max(8, (hi + 7) / 8 * 8));
-		const int np = pool_primes(p, lanes);
-		memset(p->h_aux[k], 0, (size_t)T * 2 * S * sizeof(PrpLaneAux));
-		memset(p->h_stage[k], 0, (size_t)T * S * p->nws * 4);
-		for (int t = 0; t < T; ++t)
-			for (int s = 0; s < hi; ++s)
-			{
-				PoolSlot &sl = p->slot[(size_t)s];
-				if (sl.state != SLOT_ACTIVE) continue;
-				const SlotTick tk = slot_tick(sl, p->B);
-				PrpLaneAux *ax = p->h_aux[k] + (size_t)t * 2 * S;
-				ax[s] = PrpLaneAux{ tk.before, 1u };
-				ax[S + s] = PrpLaneAux{ tk.after, 1u };
-				bit_slice(tk.source ? sl.t.res : sl.t.E, tk.lo, p->B,
-				          p->h_stage[k] + ((size_t)t * S + s) * p->nws, p->nws);
-				p->squarings += p->B + 1;
-				if (tk.last) sl.done_seq = p->seq_issued;
-			}
+		int k = 0, lanes = 0, np = 3;
+		if (int rc = plan_ticks(p, T, k, lanes, np)) return rc;
 		if (p->direct)
 		{
 			const char *what = nullptr;
@@ -851,5 +862,267 @@ int ctw_prp_autotune_primes(int log2_degree, int lanes, int primes, int *log2_ct
 	if (us_per_squaring) *us_per_squaring = std::get<2>(it->second);
 	return CTW_OK;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: the ticks of several pools (degrees 2^12..2^15, 4096 coefficients
+// per CTA) with every pool's squarings in one persistent launch (and every
+// pool's Gerbicz-Li multiply in a second), per prime count, from one graph.
+// ---------------------------------------------------------------------------
+
+struct ctw_batch {
+	std::vector<ctw_pool *> pools;             // largest degree first
+	cudaStream_t stream = nullptr, cap_stream = nullptr;
+	PrpBatchClass *d_cls[2] = { nullptr, nullptr }, *h_cls[2] = { nullptr, nullptr };
+	unsigned *d_heads[2] = { nullptr, nullptr };
+	size_t cap = 0;                            // entries per buffer: POOL_TMAX * 2 ops * pools
+	cudaEvent_t ev[2] = { nullptr, nullptr };
+	bool ev_pending[2] = { false, false };
+	long long seq = 0;
+	std::map<std::vector<int>, cudaGraphExec_t> graphs;
+	long long launches = 0;
+	int occ = 2;                               // CTAs per SM of the batch kernel build
+};
+
+namespace {
+
+// Entries of a buffer's class array: per (tick t, op, prime count) the pools of
+// that prime count in order (one persistent launch each).
+struct BatchPlan {
+	int T = 0;
+	std::vector<int> k, lanes, np;
+	struct Launch { int np, first, ncls, items; };
+	std::vector<Launch> launches;              // [t][op][prime count index]
+};
+
+void batch_fill(ctw_batch *bt, int kb, BatchPlan &pl)
+{
+	const int P = (int)bt->pools.size();
+	PrpBatchClass *h = bt->h_cls[kb];
+	pl.launches.clear();
+	int e = 0;
+	for (int t = 0; t < pl.T; ++t)
+		for (int op = 0; op < 2; ++op)
+			for (int npi = 0; npi < 2; ++npi)
+			{
+				const int npv = npi == 0 ? 2 : 3;
+				BatchPlan::Launch L{ npv, e, 0, 0 };
+				for (int q = 0; q < P; ++q)
+				{
+					if (pl.np[(size_t)q] != npv) continue;
+					ctw_pool *p = bt->pools[(size_t)q];
+					const int k = pl.k[(size_t)q];
+					PrpBatchClass &c = h[e++];
+					memset(&c, 0, sizeof(c));
+					PrpKernelArgs a = p->proto;
+					a.nprime = npv;
+					a.tw_smem = 0;                       // root tables through L1/L2
+					if (op == 0)
+					{
+						a.op = OP_SQUARE;
+						a.reg_in = reg_plane(p, 0);
+						a.reg_out = reg_plane(p, 0);
+						a.bits = p->d_stage[k] + (size_t)t * p->slots * p->nws;
+						a.nwords = p->nws;
+						a.i_hi = p->B - 1;
+						a.count = p->B;
+					}
+					else
+					{
+						a.op = OP_MUL;
+						a.reg_in = reg_plane(p, 0);
+						a.reg_y = reg_plane(p, 1);
+						a.reg_out = reg_plane(p, 1);
+						a.count = 1;
+						a.i_hi = 0;
+						a.bits = nullptr;
+					}
+					c.a = a;
+					c.lg = p->lg;
+					c.items = pl.lanes[(size_t)q] / (8 >> p->lg);
+					++L.ncls;
+					L.items += c.items;
+				}
+				pl.launches.push_back(L);
+			}
+}
+
+cudaError_t batch_issue(ctw_batch *bt, int kb, const BatchPlan &pl, cudaStream_t cs)
+{
+	const int P = (int)bt->pools.size();
+	cudaError_t e = cudaMemsetAsync(bt->d_heads[kb], 0, bt->cap * sizeof(unsigned), cs);
+	for (int q = 0; q < P && e == cudaSuccess; ++q) e = upload(bt->pools[(size_t)q], pl.k[(size_t)q], pl.T, cs);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(bt->d_cls[kb], bt->h_cls[kb], bt->cap * sizeof(PrpBatchClass), cudaMemcpyHostToDevice, cs);
+	for (int t = 0; t < pl.T && e == cudaSuccess; ++t)
+	{
+		for (int q = 0; q < P && e == cudaSuccess; ++q)
+		{
+			ctw_pool *p = bt->pools[(size_t)q];
+			const PrpLaneAux *aux = p->d_aux[pl.k[(size_t)q]] + (size_t)t * 2 * p->slots;
+			e = prp_aux_launch(aux, p->d_regs, (long long)p->slots * (long long)p->D, p->ln, pl.lanes[(size_t)q], cs);
+		}
+		for (int op = 0; op < 2 && e == cudaSuccess; ++op)
+			for (int npi = 0; npi < 2 && e == cudaSuccess; ++npi)
+			{
+				const BatchPlan::Launch &L = pl.launches[(size_t)((t * 2 + op) * 2 + npi)];
+				e = prp_batch_launch(L.np, bt->occ, bt->d_cls[kb] + L.first, L.ncls, L.items, bt->d_heads[kb] + L.first,
+				                     cs);
+			}
+		for (int q = 0; q < P && e == cudaSuccess; ++q)
+		{
+			ctw_pool *p = bt->pools[(size_t)q];
+			const PrpLaneAux *aux = p->d_aux[pl.k[(size_t)q]] + (size_t)t * 2 * p->slots + p->slots;
+			e = prp_aux_launch(aux, p->d_regs, (long long)p->slots * (long long)p->D, p->ln, pl.lanes[(size_t)q], cs);
+		}
+	}
+	return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ctw_batch_create(ctw_pool *const *pools, int count, ctw_batch **out)
+{
+	if (!out) return fail(CTW_E_ARG, "null output pointer");
+	*out = nullptr;
+	if (!pools || count < 1 || count > 64) return fail(CTW_E_ARG, "count %d outside [1, 64]", count);
+	std::vector<ctw_pool *> v(pools, pools + count);
+	for (ctw_pool *p : v)
+	{
+		if (!p) return fail(CTW_E_ARG, "null pool");
+		if (p->minus || p->lm != 12 || p->lg > 3)
+			return fail(CTW_E_ARG, "batch pools need degrees 2^12..2^15 on CTAs of 4096 coefficients (N+)");
+		if (p->slots % (8 >> p->lg) != 0)
+			return fail(CTW_E_ARG, "a pool of degree 2^%d in a batch needs a multiple of %d slots", p->ln, 8 >> p->lg);
+	}
+	for (size_t i = 0; i < v.size(); ++i)
+		for (size_t j = i + 1; j < v.size(); ++j)
+			if (v[i] == v[j]) return fail(CTW_E_ARG, "a pool appears twice in the batch");
+	std::stable_sort(v.begin(), v.end(), [](const ctw_pool *a, const ctw_pool *b) { return a->lg > b->lg; });
+	ctw_batch *bt = new ctw_batch();
+	bt->pools = v;
+	bt->cap = (size_t)POOL_TMAX * 2 * v.size();
+	bool ok = cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking) == cudaSuccess &&
+	          cudaStreamCreateWithFlags(&bt->cap_stream, cudaStreamNonBlocking) == cudaSuccess &&
+	          cudaEventCreateWithFlags(&bt->ev[0], cudaEventDisableTiming) == cudaSuccess &&
+	          cudaEventCreateWithFlags(&bt->ev[1], cudaEventDisableTiming) == cudaSuccess;
+	for (int k = 0; k < 2 && ok; ++k)
+		ok = cudaMalloc(&bt->d_cls[k], bt->cap * sizeof(PrpBatchClass)) == cudaSuccess &&
+		     cudaMallocHost(&bt->h_cls[k], bt->cap * sizeof(PrpBatchClass)) == cudaSuccess &&
+		     cudaMalloc(&bt->d_heads[k], bt->cap * sizeof(unsigned)) == cudaSuccess;
+	if (!ok)
+	{
+		ctw_batch_destroy(bt);
+		return fail(CTW_E_NOMEM, "batch buffers");
+	}
+	*out = bt;
+	return CTW_OK;
+}
+
+int ctw_batch_destroy(ctw_batch *bt)
+{
+	if (!bt) return CTW_OK;
+	if (bt->stream) cudaStreamSynchronize(bt->stream);
+	for (auto &kv : bt->graphs) cudaGraphExecDestroy(kv.second);
+	for (int k = 0; k < 2; ++k)
+	{
+		cudaFree(bt->d_cls[k]);
+		cudaFreeHost(bt->h_cls[k]);
+		cudaFree(bt->d_heads[k]);
+		if (bt->ev[k]) cudaEventDestroy(bt->ev[k]);
+	}
+	if (bt->stream) cudaStreamDestroy(bt->stream);
+	if (bt->cap_stream) cudaStreamDestroy(bt->cap_stream);
+	delete bt;
+	return CTW_OK;
+}
+
+int ctw_batch_run(ctw_batch *bt, int ticks)
+{
+	if (!bt) return fail(CTW_E_ARG, "null batch");
+	if (ticks < 0) return fail(CTW_E_ARG, "negative tick count");
+	const int P = (int)bt->pools.size();
+	while (ticks > 0)
+	{
+		BatchPlan pl;
+		pl.T = std::min(ticks, POOL_TMAX);
+		const int kb = (int)(bt->seq & 1);
+		if (bt->ev_pending[kb])
+		{
+			POOL_CUDA(cudaEventSynchronize(bt->ev[kb]));
+			bt->ev_pending[kb] = false;
+		}
+		pl.k.resize((size_t)P);
+		pl.lanes.resize((size_t)P);
+		pl.np.resize((size_t)P);
+		for (int q = 0; q < P; ++q)
+		{
+			int k = 0, lanes = 0, np = 3;
+			if (int rc = plan_ticks(bt->pools[(size_t)q], pl.T, k, lanes, np)) return rc;
+			pl.k[(size_t)q] = k;
+			pl.lanes[(size_t)q] = lanes;
+			pl.np[(size_t)q] = np;
+		}
+		batch_fill(bt, kb, pl);
+		std::vector<int> key{ kb, pl.T, bt->occ };
+		for (int q = 0; q < P; ++q)
+		{
+			key.push_back(pl.k[(size_t)q]);
+			key.push_back(pl.lanes[(size_t)q]);
+			key.push_back(pl.np[(size_t)q]);
+		}
+		cudaGraphExec_t exec = nullptr;
+		auto it = bt->graphs.find(key);
+		if (it != bt->graphs.end()) exec = it->second;
+		else
+		{
+			POOL_CUDA(cudaStreamBeginCapture(bt->cap_stream, cudaStreamCaptureModeRelaxed));
+			cudaError_t e = batch_issue(bt, kb, pl, bt->cap_stream);
+			cudaGraph_t graph = nullptr;
+			const cudaError_t e2 = cudaStreamEndCapture(bt->cap_stream, &graph);
+			if (e != cudaSuccess || e2 != cudaSuccess)
+			{
+				if (graph) cudaGraphDestroy(graph);
+				return fail(CTW_E_CUDA, "batch tick capture: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+			}
+			e = cudaGraphInstantiate(&exec, graph, 0);
+			cudaGraphDestroy(graph);
+			if (e != cudaSuccess) return fail(CTW_E_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
+			bt->graphs[key] = exec;
+		}
+		POOL_CUDA(cudaGraphLaunch(exec, bt->stream));
+		for (const BatchPlan::Launch &L : pl.launches) bt->launches += L.items > 0 ? 1 : 0;
+		POOL_CUDA(cudaEventRecord(bt->ev[kb], bt->stream));
+		bt->ev_pending[kb] = true;
+		++bt->seq;
+		for (int q = 0; q < P; ++q)
+		{
+			ctw_pool *p = bt->pools[(size_t)q];
+			const int k = pl.k[(size_t)q];
+			POOL_CUDA(cudaEventRecord(p->ev[k], bt->stream));
+			p->ev_pending[k] = true;
+			p->ev_seq[k] = p->seq_issued;
+			++p->seq_issued;
+		}
+		ticks -= pl.T;
+	}
+	return CTW_OK;
+}
+
+void *ctw_batch_stream(ctw_batch *bt) { return bt ? (void *)bt->stream : nullptr; }
+
+int ctw_batch_set_ctas_per_sm(ctw_batch *bt, int ctas)
+{
+	if (!bt) return fail(CTW_E_ARG, "null batch");
+	if (ctas != 1 && ctas != 2) return fail(CTW_E_ARG, "CTAs per SM must be 1 or 2");
+	if (prp_batch_max_clusters(2, ctas) < 1) return fail(CTW_E_CUDA, "the batch kernel does not fit the device");
+	bt->occ = ctas;
+	return CTW_OK;
+}
+
+long long ctw_batch_launches(ctw_batch *bt) { return bt ? bt->launches : 0; }
 
 }  // extern "C"

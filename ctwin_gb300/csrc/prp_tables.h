@@ -149,4 +149,56 @@ inline void prp_build_tables(int ln, int lg, uint32_t *tf, uint32_t *ti, PrpKern
 	proto.scols = prp_stage_cols(lm, lg);
 }
 
+// Root tables of the grid kernel with warp-local sub-transforms
+// (prp_kernel_grid2: 2^lg CTAs of M = 2^lm coefficients, lm = 10 or 11): the
+// first C = lm - 8 local levels run across the CTA (radix 2^C), the last 8 on
+// sub-blocks of 256 coefficients, one warp each.  Per CTA g and prime, M words
+// (Montgomery form), forward in tf and inverse in ti: for sub-block sb, words
+// [256 sb, 256 sb + 256) hold its roots of local level C + l at index 2^l + jj
+// (jj the block within the sub-block; for l = 6 and 7, jj = 2 u + e and
+// 4 u + e are stored at 2^l + 32 e + u, the order a warp reads them in); word
+// 256 j (j = 1 .. 2^C - 1, unused by the sub-blocks) holds the root of local
+// level L < C, block J with 2^L + J = j.  The root of local level L, block J
+// of CTA g is that of global block (G + g) 2^L + J, as in prp_build_tables.
+inline void prp_build_grid2_tables(int ln, int lg, uint32_t *tf, uint32_t *ti)
+{
+	using namespace tables_detail;
+	static const uint32_t kQ[3] = { Q0, Q1, Q2 };
+	static const uint32_t kG[3] = { QGEN0, QGEN1, QGEN2 };
+	const int lm = ln - lg, C = lm - 8;
+	const size_t D = size_t(1) << ln, G = size_t(1) << lg, M = D / G;
+	memset(tf, 0, G * 3 * M * sizeof(uint32_t));
+	memset(ti, 0, G * 3 * M * sizeof(uint32_t));
+	for (int pi = 0; pi < 3; ++pi)
+	{
+		const uint32_t q = kQ[pi];
+		std::vector<uint32_t> W(D, 0);
+		for (size_t s = 1; s < D; s *= 2)
+		{
+			const uint32_t rs = powmod(kG[pi], (q - 1) / (6 * (uint64_t)s), q);
+			for (size_t j = 0; j < s; ++j) W[s + j] = powmod(rs, 3 * bitrev(j, s) + 1 + (2 * j) / s, q);
+		}
+		for (size_t g = 0; g < G; ++g)
+		{
+			uint32_t *f = tf + (g * 3 + pi) * M, *iv = ti + (g * 3 + pi) * M;
+			auto put = [&](size_t idx, int L, size_t J) {
+				const uint32_t w = W[((G + g) << L) + J];
+				f[idx] = mont(w, q);
+				iv[idx] = mont(invmod(w, q), q);
+			};
+			for (int L = 0; L < C; ++L)
+				for (size_t J = 0; J < ((size_t)1 << L); ++J) put((((size_t)1 << L) + J) * 256, L, J);
+			for (size_t sb = 0; sb < ((size_t)1 << C); ++sb)
+				for (int l = 0; l < 8; ++l)
+					for (size_t jj = 0; jj < ((size_t)1 << l); ++jj)
+					{
+						size_t pos = jj;
+						if (l == 6) pos = (jj & 1) * 32 + (jj >> 1);
+						if (l == 7) pos = (jj & 3) * 32 + (jj >> 2);
+						put(sb * 256 + ((size_t)1 << l) + pos, C + l, (sb << l) + jj);
+					}
+		}
+	}
+}
+
 }  // namespace ctw

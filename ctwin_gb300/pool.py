@@ -167,6 +167,67 @@ class Pool:
             res += self.results()
 
 
+class Batch:
+    """Pools of degrees 2^12..2^15 (CTAs of 4096 coefficients) driven together:
+    per tick, every pool's squarings in one persistent launch with per-degree
+    work queues (and every pool's Gerbicz-Li multiply in a second), replayed
+    from CUDA graphs.  Results stay the pools' own (Pool.collect / results)."""
+
+    def __init__(self, pools, ctas_per_sm: int = 2):
+        self.pools = list(pools)
+        arr = (ctypes.c_void_p * len(self.pools))(*[p._h.value for p in self.pools])
+        h = ctypes.c_void_p()
+        check(lib().ctw_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(self.pools), ctypes.byref(h)))
+        self._h = h
+        self.set_ctas_per_sm(ctas_per_sm)
+
+    def set_ctas_per_sm(self, ctas: int):
+        check(lib().ctw_batch_set_ctas_per_sm(self._h, ctas))
+        self.ctas_per_sm = ctas
+
+    def close(self):
+        if self._h:
+            lib().ctw_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, ticks: int = 1):
+        check(lib().ctw_batch_run(self._h, ticks))
+
+    @property
+    def stream(self) -> int:
+        return lib().ctw_batch_stream(self._h) or 0
+
+    @property
+    def launches(self) -> int:
+        return int(lib().ctw_batch_launches(self._h))
+
+    def run_to_completion(self, ticks_per_call: int = 8) -> list[dict]:
+        """Run until every admitted test of every pool has finished."""
+        res = []
+        while True:
+            for p in self.pools:
+                p.collect(wait=False)
+                res += p.results()
+            if all(p.info()["active"] == 0 for p in self.pools):
+                return res
+            self.run(ticks_per_call)
+            for p in self.pools:
+                p.collect(wait=True)
+                res += p.results()
+
+
 class Server:
     """Request loop over pools of every degree (continuous batching by size class)."""
 

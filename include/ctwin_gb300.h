@@ -301,6 +301,30 @@ void *ctw_pool_stream(ctw_pool *p);
  * max_ticks is too small). */
 int ctw_pool_schedule(int log2_degree, uint32_t b, int gl_block, int32_t *ticks_out, int max_ticks, int *block);
 
+/* Batches of pools of uneven degrees, no counterpart in the reference (its
+ * batching is 64 lanes of one degree per vector, cyclo/src/engine.h:19,
+ * cyclo/src/cyclo.h:216-241).  A batch drives pools of degrees 2^12..2^15
+ * whose split has 4096 coefficients per CTA (log2_ctas = log2_degree - 12;
+ * N+ only; slots a multiple of 2^(15 - log2_degree)) tick by tick: per tick
+ * every pool's register moves, then ONE persistent launch (per NTT prime
+ * count) in which clusters of 8 CTAs take work items from per-degree queues,
+ * largest degree first - an item is 2^(15 - k) lanes of a degree-2^k pool,
+ * each on 2^(k - 12) CTAs, for the pool's B squarings - then one such launch
+ * for every pool's Gerbicz-Li multiply, then the moves after; ticks are
+ * replayed from CUDA graphs.  Registers, results and their collection are the
+ * pools' own (ctw_pool_collect / ctw_pool_results); a pool in a batch is run
+ * only through it.  The caller keeps ownership of the pools. */
+typedef struct ctw_batch ctw_batch;
+int ctw_batch_create(ctw_pool *const *pools, int count, ctw_batch **out);
+int ctw_batch_run(ctw_batch *b, int ticks);
+int ctw_batch_destroy(ctw_batch *b);
+void *ctw_batch_stream(ctw_batch *b);
+/* Persistent launches issued by the batch since creation. */
+long long ctw_batch_launches(ctw_batch *b);
+/* CTAs per SM of the batch kernel build (1: up to 128 registers a thread;
+ * 2, the default: 64 / 80 registers), an autotuning choice. */
+int ctw_batch_set_ctas_per_sm(ctw_batch *b, int ctas);
+
 /* ------------------------------------------------------------------------ */
 /* Server: a request loop over pools of every degree.  No counterpart in the */
 /* reference.                                                                */

@@ -31,5 +31,8 @@ inline unsigned atomicOr(unsigned *p, unsigned v) { return __atomic_fetch_or(p, 
 inline unsigned atomicAdd(unsigned *p, unsigned v) { return __atomic_fetch_add(p, v, __ATOMIC_SEQ_CST); }
 inline void __threadfence() { __atomic_thread_fence(__ATOMIC_SEQ_CST); }
 void __syncthreads();
+void emu_syncwarp();
+inline uint2 make_uint2(uint32_t x, uint32_t y) { return uint2{ x, y }; }
+inline uint4 make_uint4(uint32_t x, uint32_t y, uint32_t z, uint32_t w) { return uint4{ x, y, z, w }; }
 uint32_t *emu_smem();
 unsigned long long emu_timer_ns();

@@ -9,8 +9,13 @@
 //        engine_emu server <log2 D> <max slots> <base 2|3> <b> [<b> ...]
 //        engine_emu mul <log2 D> <csize> <in file> <out file> <b> [<b> ...]
 //        engine_emu resume <log2 D> <base 2|3> <context file> <b>
+//        engine_emu batch <ticks>
 // resume: the whole test stops at its first Gerbicz-Li checkpoint, saves the
 // reference's context file there, and a fresh engine reads it and finishes.
+// batch: pools of degrees 2^12 (two and three primes), 2^13 and 2^14 run
+// <ticks> ticks through one batch (ctw_batch_run: the persistent kernel with
+// per-degree queues) and, as a second set of the same pools, through
+// ctw_pool_run; prints the number of register words that differ.
 // mul: ctw_prp_mul_noalloc of the lanes' x and y (int32 digits, x then y, read
 // from the in file) into z (written to the out file).
 // The second form runs the tests as a pool (continuous batching, ticks
@@ -35,7 +40,10 @@ dim3 blockDim, gridDim;
 static std::vector<std::vector<uint32_t>> g_sm;
 static std::vector<std::unique_ptr<std::barrier<>>> g_bar;
 static std::unique_ptr<std::barrier<>> g_cbar;
+static std::vector<std::unique_ptr<std::barrier<>>> g_wbar;   // [CTA][warp] of 32 threads
+static unsigned g_nwarps = 1;
 void __syncthreads() { g_bar[t_cta]->arrive_and_wait(); }
+void emu_syncwarp() { g_wbar[(size_t)t_cta * g_nwarps + threadIdx.x / 32]->arrive_and_wait(); }
 uint32_t *emu_smem() { return g_sm[t_cta].data(); }
 int emu_cta_rank() { return t_cta; }
 void emu_cluster_sync() { g_cbar->arrive_and_wait(); }
@@ -71,6 +79,9 @@ void emu_run_ctas(dim3 grid, dim3 block, size_t smem, int group, void (*body)(vo
 		g_bar.clear();
 		for (unsigned c = 0; c < ng; ++c) g_bar.emplace_back(new std::barrier<>(nt));
 		g_cbar.reset(new std::barrier<>(ng * nt));
+		g_nwarps = nt / 32 ? nt / 32 : 1;
+		g_wbar.clear();
+		for (unsigned w = 0; w < ng * g_nwarps; ++w) g_wbar.emplace_back(new std::barrier<>(nt < 32 ? nt : 32));
 		std::vector<std::thread> th;
 		th.reserve((size_t)ng * nt);
 		for (unsigned c = 0; c < ng; ++c)
@@ -84,6 +95,52 @@ void emu_run_ctas(dim3 grid, dim3 block, size_t smem, int group, void (*body)(vo
 				});
 		for (auto &x : th) x.join();
 	}
+}
+
+static int run_batch(int argc, char **argv)
+{
+	const int ticks = atoi(argv[2]);
+	struct Spec { int ln, slots; std::vector<uint32_t> b; };
+	const std::vector<Spec> specs = {
+		{ 14, 2, { 100003, 65537 } },
+		{ 13, 4, { 70001, 1000003, 64 } },
+		{ 12, 8, { 65537, 100, 9000001, 123457, 2000003 } },
+		{ 12, 8, { 9999991, 16777213 } },                 // above the two-prime bound: three primes
+	};
+	std::vector<ctw_pool *> batched, alone;
+	int rc = 0;
+	for (int set = 0; set < 2 && !rc; ++set)
+		for (const Spec &sp : specs)
+		{
+			ctw_pool *p = nullptr;
+			if ((rc = ctw_pool_create(sp.ln, sp.slots, sp.ln - 12, 8, 3, 0, &p))) break;
+			(set ? alone : batched).push_back(p);
+			for (size_t i = 0; i < sp.b.size() && !rc; ++i) rc = ctw_pool_admit(p, sp.b[i], i) < 0;
+		}
+	ctw_batch *bt = nullptr;
+	if (!rc) rc = ctw_batch_create(batched.data(), (int)batched.size(), &bt);
+	if (!rc) rc = ctw_batch_run(bt, ticks);
+	for (size_t i = 0; i < alone.size() && !rc; ++i) rc = ctw_pool_run(alone[i], ticks);
+	long long bad = 0, words = 0;
+	for (size_t i = 0; i < alone.size() && !rc; ++i)
+	{
+		rc = ctw_pool_collect(batched[i], 1) < 0 || ctw_pool_collect(alone[i], 1) < 0;
+		const size_t D = (size_t)1 << specs[i].ln;
+		std::vector<int32_t> x(D), y(D);
+		for (int s = 0; s < specs[i].slots && !rc; ++s)
+			for (int r = 0; r < 6 && !rc; ++r)
+			{
+				rc = ctw_pool_read_slot(batched[i], s, r, x.data()) || ctw_pool_read_slot(alone[i], s, r, y.data());
+				for (size_t j = 0; j < D; ++j) bad += x[j] != y[j];
+				words += (long long)D;
+			}
+	}
+	if (rc) fprintf(stderr, "batch: %s\n", ctw_last_error());
+	ctw_batch_destroy(bt);
+	for (ctw_pool *p : batched) ctw_pool_destroy(p);
+	for (ctw_pool *p : alone) ctw_pool_destroy(p);
+	printf("batch registers compared %lld differ %lld\n", words, bad);
+	return (rc || bad || !words) ? 1 : 0;
 }
 
 static int run_pool(int argc, char **argv)
@@ -198,6 +255,7 @@ int main(int argc, char **argv)
 	if (argc >= 6 && strcmp(argv[1], "resume") == 0) return run_resume(argv);
 	if (argc >= 7 && strcmp(argv[1], "mul") == 0) return run_mul(argc, argv);
 	if (argc >= 6 && strcmp(argv[1], "pool") == 0) return run_pool(argc, argv);
+	if (argc >= 3 && strcmp(argv[1], "batch") == 0) return run_batch(argc, argv);
 	if (argc >= 6 && strcmp(argv[1], "server") == 0) return run_server(argc, argv);
 	if (argc < 5) { fprintf(stderr, "usage: engine_emu ln base minus b...\n"); return 2; }
 	const int ln = atoi(argv[1]), base = atoi(argv[2]), minus = atoi(argv[3]);

@@ -78,6 +78,11 @@ template <class F> inline cudaError_t cudaOccupancyMaxActiveBlocksPerMultiproces
 	*n = 1;
 	return cudaSuccess;
 }
+template <class F, class C> inline cudaError_t cudaOccupancyMaxActiveClusters(int *n, F, const C *)
+{
+	*n = 2;
+	return cudaSuccess;
+}
 template <class T> inline cudaError_t cudaMalloc(T **p, size_t n)
 {
 	*p = (T *)malloc(n ? n : 1);

@@ -29,7 +29,10 @@ thread_local int t_cta;
 dim3 blockDim, gridDim;
 static std::vector<std::vector<uint32_t>> g_sm;
 static std::vector<std::barrier<> *> g_bar;
+static std::vector<std::barrier<> *> g_wbar;      // [CTA][warp]: 32 threads each
+static int g_warps = 1;
 void __syncthreads() { g_bar[t_cta]->arrive_and_wait(); }
+void emu_syncwarp() { g_wbar[(size_t)t_cta * g_warps + threadIdx.x / 32]->arrive_and_wait(); }
 uint32_t *emu_smem() { return g_sm[t_cta].data(); }
 // the grid kernel uses no cluster: these abort the emulation if reached
 int emu_cta_rank() { abort(); }
@@ -45,22 +48,25 @@ unsigned long long emu_timer_ns()
 
 namespace ctw {
 template <int LG, int NP, int LM> void prp_kernel_grid(const PrpKernelArgs a, const PrpGridArgs ga);
+template <int LG, int NP, int LM> void prp_kernel_grid2(const PrpKernelArgs a, const PrpGridArgs ga);
 }
 using namespace ctw;
 typedef void (*Kern)(const PrpKernelArgs, const PrpGridArgs);
 
 static Kern pick(int lg, int lm, int np)
 {
-#define CTW_EMU_SHAPE(LG, NP, LM) if (lg == LG && np == NP && lm == LM) return prp_kernel_grid<LG, NP, LM>;
+#define CTW_EMU_SHAPE(LG, NP, LM, K) if (lg == LG && np == NP && lm == LM) return K<LG, NP, LM>;
 	CTW_EMU_SHAPES
 #undef CTW_EMU_SHAPE
 	return nullptr;
 }
 
-// shared-memory words of a grid CTA (the layout at the top of prp_kernel_grid)
+// shared-memory words of a grid CTA (the layouts at the top of prp_kernel_grid
+// for 4096 coefficients and of prp_kernel_grid2 for 1024 and 2048)
 static size_t grid_words(int lg, int lm, int tw, int np)
 {
 	const size_t M = (size_t)1 << lm, G = (size_t)1 << lg;
+	if (lm <= 11) return 2 * np * M + M + M / 4 + 2 * G + 2 * np * G + 2 * np * M;
 	return 2 * np * M + M / 4 + 2 * G + 2 * np * G + (tw ? 2 * np * M : 0) + (lm == 12 ? 2 * (size_t)np * 512 : 0);
 }
 
@@ -82,6 +88,9 @@ static int launch(Kern k, const PrpKernelArgs &a, const PrpGridArgs &ga, int G, 
 	g_sm.assign(G, std::vector<uint32_t>(smem_words, 0xdeadbeefu));
 	g_bar.clear();
 	for (int g = 0; g < G; ++g) g_bar.push_back(new std::barrier<>(threads));
+	g_warps = threads / 32;
+	g_wbar.clear();
+	for (int w = 0; w < G * g_warps; ++w) g_wbar.push_back(new std::barrier<>(32));
 	memset(ga.bar, 0, GRID_BAR_WORDS * sizeof(unsigned));
 	std::vector<Job> jobs((size_t)G * threads);
 	std::vector<pthread_t> th((size_t)G * threads);
@@ -102,6 +111,8 @@ static int launch(Kern k, const PrpKernelArgs &a, const PrpGridArgs &ga, int G, 
 	for (size_t i = 0; i < started; ++i) pthread_join(th[i], nullptr);
 	for (auto *b : g_bar) delete b;
 	g_bar.clear();
+	for (auto *b : g_wbar) delete b;
+	g_wbar.clear();
 	return 0;
 }
 
@@ -119,6 +130,7 @@ int main(int argc, char **argv)
 	PrpKernelArgs a{};
 	std::vector<uint32_t> tf(G * 3 * M), ti(G * 3 * M), tfs(G * 3 * 256 * 2), tis(G * 3 * 256 * 2), xr(768);
 	prp_build_tables(ln, lg, tf.data(), ti.data(), a, tfs.data(), tis.data(), xr.data());
+	if (lm <= 11) prp_build_grid2_tables(ln, lg, tf.data(), ti.data());
 	std::vector<int32_t> x(D), y(D), out(D);
 	std::vector<uint32_t> scratch(3 * D), laneb(4), status(1, 0), gx(3 * D), gr(3 * D), bar(GRID_BAR_WORDS);
 	std::vector<long long> gc((size_t)G * G);

@@ -21,9 +21,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 
-def _flip_run(eng, b, at_checkpoint):
-    seen = []
-
+def _flip_run(eng, b, at_checkpoint, seen):
     def cp(i):
         seen.append(i)
         if len(seen) == at_checkpoint:
@@ -33,20 +31,21 @@ def _flip_run(eng, b, at_checkpoint):
             eng.write_regs(x, 0)
         return False
 
-    prp, r64, gl = eng.run_ex([b], cp)
-    return bool(prp[0]), int(r64[0]), bool(gl[0]), len(seen)
+    return eng.run_ex([b], cp)
 
 
 @pytest.mark.parametrize("ln,b", [(16, 65), (12, 1000003)])
 def test_gerbicz_li_catches_a_flipped_digit(native, ln, b):
-    from ctwin_gb300 import PrpEngine
+    from ctwin_gb300 import CtwError, PrpEngine
     with PrpEngine(ln, 1, base=3) as eng:
         prp, r64, gl = eng.run([b])            # clean run: the check passes
         assert gl[0]
-        prp2, r642, gl2, nck = _flip_run(eng, b, 2)
-        assert nck > 2
-        assert not gl2, "Gerbicz-Li missed a changed digit"
-        assert r642 != int(r64[0])
+        seen = []
+        # the reference treats a failed check as a fatal error (cyclo/src/cyclo.h:376-377): CTW_E_GERBICZ
+        with pytest.raises(CtwError) as ei:
+            _flip_run(eng, b, 2, seen)
+        assert ei.value.code == -5, "Gerbicz-Li missed a changed digit"
+        assert len(seen) > 2
         # the engine is unharmed: a clean run again passes
         prp3, r643, gl3 = eng.run([b])
         assert gl3[0] and int(r643[0]) == int(r64[0])

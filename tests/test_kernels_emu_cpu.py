@@ -70,14 +70,16 @@ def grid_emu():
     assert cut > 0, "prp_grid.cu: host launch code not found"
     body = src[:cut]
     decl = "extern __shared__ __align__(16) uint32_t sm[];"
-    assert body.count(decl) == 1
+    assert body.count(decl) == 2                       # prp_kernel_grid and prp_kernel_grid2
     body = body.replace(decl, "uint32_t *sm = emu_smem();")
-    inst = "".join(f"template void prp_kernel_grid<{lg}, {np}, {lm}>(const PrpKernelArgs, const PrpGridArgs);\n"
+    # 1024- and 2048-coefficient CTAs run the warp-local kernel, 4096 the radix-16 one
+    kname = lambda lm: "prp_kernel_grid2" if lm <= 11 else "prp_kernel_grid"
+    inst = "".join(f"template void {kname(lm)}<{lg}, {np}, {lm}>(const PrpKernelArgs, const PrpGridArgs);\n"
                    for lg, np, lm in SHAPES)
     kern = os.path.join(BUILD, "grid_kernels.cpp")
     with open(kern, "w") as f:
         f.write('#include "emu_shim.h"\n' + body + inst + "}  // namespace ctw\n")
-    shapes = " ".join(f"CTW_EMU_SHAPE({lg}, {np}, {lm})" for lg, np, lm in SHAPES)
+    shapes = " ".join(f"CTW_EMU_SHAPE({lg}, {np}, {lm}, {kname(lm)})" for lg, np, lm in SHAPES)
     return _compile(os.path.join(BUILD, "grid_emu"), [kern, os.path.join(EMU, "grid_emu.cpp")], shapes)
 
 
@@ -256,7 +258,7 @@ def test_sieve_factors_emulated(sieve_emu, mode):
 
 
 ENGINE_SOURCES = ("prp_engine.cu", "prp_kernels.cu", "prp_kernels_np2.cu", "prp_grid.cu", "prp_pool.cu",
-                  "prp_server.cu", "prp_noalloc.cu", "cyclo_files.cu")
+                  "prp_batch.cu", "prp_server.cu", "prp_noalloc.cu", "cyclo_files.cu")
 
 
 @pytest.fixture(scope="module")
@@ -324,6 +326,17 @@ def test_server_emulated_matches_gmp(engine_emu, golden_dir):
     for b in bs:
         assert got[b] == (gold[b]["prp"], gold[b]["res64"], "1", "0"), b
     assert any(gold[b]["prp"] for b in bs)
+
+
+def test_batch_emulated_equals_pools(engine_emu):
+    """A batch of pools of degrees 2^12 (two and three primes), 2^13 and 2^14
+    (prp_pool.cu's batch ticks: every pool's squarings in one persistent launch
+    of clusters of 8 CTAs with per-degree queues, prp_batch.cu) against the
+    same pools ticked on their own: every register of every slot equal after
+    two ticks (base 3)."""
+    r = subprocess.run([engine_emu, "batch", "2"], capture_output=True, text=True, timeout=1200)
+    assert r.returncode == 0, r.stdout + r.stderr[-2000:]
+    assert " differ 0" in r.stdout
 
 
 @pytest.mark.parametrize("ln,bs,csize", [(11, [100003, 299993], 16), (13, [1330358], 8)])

@@ -184,3 +184,41 @@ def test_pool_admit_many(native):
         res += p.run_to_completion()
     assert sorted(r["b"] for r in res) == sorted(bs)
     check_results(res, 11)
+
+
+def test_server_admits_arrivals_while_others_run(native):
+    """Continuous batching: requests that arrive while a test is on the device
+    are admitted before it finishes, and their device work overlaps it (pools
+    of other degrees running beside it).  Every result equals GMP's and the
+    same request served alone (tolerance 0)."""
+    import time
+
+    from ctwin_gb300 import Server
+    first = (12, 9999991)                                   # about 95 k squarings
+    later = [(9, server_cases(9)[0]), (10, server_cases(10)[1]), (11, server_cases(11)[2]), (12, 65537)]
+    with Server(hbm_budget_bytes=1 << 30, max_slots=8, ticks_per_launch=1) as s:
+        for ln in (9, 10, 11, 12):
+            s.prepare(ln, 4)
+        s.submit(*first, tag=0)
+        t0 = time.time()
+        while s.stats()["active"] < 1:                      # the first test is on the device
+            assert time.time() - t0 < 60
+            time.sleep(0.001)
+        for i, (ln, b) in enumerate(later):
+            s.submit(ln, b, tag=i + 1)
+            time.sleep(0.002)
+        res = {r["tag"]: r for r in s.drain(1 + len(later), timeout_s=300)}
+    reqs = [first] + later
+    assert sorted(res) == list(range(len(reqs)))
+    for t, r in res.items():
+        check_results([r], reqs[t][0])
+    a = res[0]
+    for t in range(1, len(reqs)):
+        r = res[t]
+        assert a["t_admit"] < r["t_admit"] < a["t_done"], (a, r)        # admitted while the first ran
+        assert r["t_admit"] < a["t_done"] and a["t_admit"] < r["t_done"]   # intervals overlap
+    with Server(hbm_budget_bytes=1 << 30, max_slots=8) as s:
+        for t, (ln, b) in enumerate(reqs):
+            s.submit(ln, b, tag=t)
+            r = s.drain(1, timeout_s=120)[0]
+            assert (r["is_prp"], r["res64"], r["gl_ok"]) == (res[t]["is_prp"], res[t]["res64"], res[t]["gl_ok"])
