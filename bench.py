@@ -19,19 +19,20 @@ work cyclo::check does between two checkpoints (cyclo/src/cyclo.h:277-308).
 Two more workloads print their own line (not the default):
   --workload batch  4096 candidates of degree 2^k, k uniform in {12..15}, b uniform in
          [2^16, 2^22) seed 3, resident in one pool per degree and prime class (b within
-         the degree's two-prime bound or above it; autotuned split and CSIZE per pool);
-         one step = one tick of every pool (B squarings + the Gerbicz-Li multiply
-         of every candidate), the pools' graphs running side by side on their streams;
-         compared per degree with the plain one-candidate-per-launch-sequence path
+         the degree's two-prime bound or above it), driven by one batch: one step = one
+         tick (B squarings + the Gerbicz-Li multiply of every candidate), the squarings
+         of all degrees in one persistent launch with per-degree work queues; CSIZE
+         and CTAs per SM autotuned; compared per degree with the plain
+         one-candidate-per-launch-sequence path
   --workload sieve  sieved b/s of the GPU sieve on n = 20, b < 2^30, p < 2^40 (and the
          n = 11 both-form sieve of b in [10^5, 3 10^5) to 2^32 beside it)
   --workload config1  the reference's workflow at n = 11: sieve b in [10^5, 3 10^5) to
          2^32 (both forms), then base-3 PRP of every survivor and of its twin partner N-
   --workload serve  a seeded Poisson stream of full PRP tests, degree 2^k with k
-         log-uniform in [12, 15) (k = 12, 13, 14), b uniform in [2^16, 2^24), through the
+         log-uniform in [12, --serve-max-degree], b uniform in [2^16, 2^24), through the
          server (continuous batching by degree, admission by pool bytes); tests/s and
-         p50/p99 latency, beside the plain path's, whose queue is replayed from its
-         measured per-degree service times
+         p50/p99 latency per degree, beside the plain path run for real on the first
+         arrivals (one test at a time)
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload single|batch|serve]
 """
@@ -131,37 +132,27 @@ def roofline_single(achieved, executed, peak_imad, peak_mont, peak_shoup, t_laun
 def secondary():
     """Other workloads, timed in the same process so that one bench line carries
     them: batched over plain at degrees 2^12..2^14 (256 candidates per degree,
-    b uniform in [2^16, 2^22) seed 3, one pool tick against the one-candidate
+    b uniform in [2^16, 2^22) seed 3, one batch tick against the one-candidate
     launch sequence), one pass of the large sieve (n = 20, b < 2^30, p < 2^40)
     and the n = 11 sieve of b in [10^5, 3 10^5) to 2^32, both forms."""
     import torch
-    from ctwin_gb300 import Pool, autotune, sieve_pass
+    from ctwin_gb300 import Batch, sieve_pass
     out = {"batched_over_plain": {}}
     rng = random.Random(3)
     t_start = time.perf_counter()
     for k in (12, 13, 14):
         bs = [rng.randrange(1 << 16, 1 << 22) for _ in range(256)]
-        lg, cs, _ = autotune(k, len(bs), 2)
-        with Pool(k, len(bs), log2_ctas=lg, csize=cs) as p:
-            assert p.admit_many(bs) == len(bs)
-            p.run(1)
-            p.collect(wait=True)
-            info = p.info()
-            st = torch.cuda.ExternalStream(p.stream)
-            ts = []
-            for _ in range(3):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(st)
-                p.run(1)
-                e1.record(st)
-                e1.synchronize()
-                ts.append(e0.elapsed_time(e1) / 1000.0)
-            p.collect(wait=True)
-            batched = info["slots"] * (info["gl_block"] + 1) / statistics.median(ts)
+        pools = batch_pools({(k, 2): bs}, 16)
+        p = pools[(k, 2)]
+        with Batch([p]) as bt:
+            bt.run(1)
+            torch.cuda.synchronize()
+            batched = statistics.median(batch_tick_rate(bt, [p]) for _ in range(3))
+        p.close()
         plain = plain_rate(k, bs[0])
         out["batched_over_plain"][str(k)] = {"candidates": len(bs), "batched_sq_per_s": batched,
                                              "plain_sq_per_s": plain, "ratio": batched / plain,
-                                             "log2_ctas": lg, "csize": cs}
+                                             "path": "batch of one pool (persistent launch), CSIZE 16"}
     n, b_min, b_max = 20, 2, (1 << 30) - 1
     sieve_pass(n, b_min, b_max, 3 * (1 << n) + 1, 1 << 40, 1)
     t0 = time.perf_counter()
@@ -351,9 +342,36 @@ def plain_rate(ln: int, b: int, reps: int = 2):
     return (B + 1) / statistics.median(ts)
 
 
+def batch_pools(groups, csize):
+    """One pool per (degree, prime class) on CTAs of 4096 coefficients, slots
+    rounded up to whole work items, every b admitted."""
+    from ctwin_gb300 import Pool
+    pools = {}
+    for c, bl in groups.items():
+        lg = c[0] - 12
+        unit = 8 >> lg
+        slots = (len(bl) + unit - 1) // unit * unit
+        pools[c] = Pool(c[0], slots, log2_ctas=lg, csize=csize)
+        assert pools[c].admit_many(bl) == len(bl)
+    return pools
+
+
+def batch_tick_rate(bt, pools, ticks: int = 1):
+    """Squarings per second of `ticks` batch ticks, CUDA events on the batch's stream."""
+    import torch
+    st = torch.cuda.ExternalStream(bt.stream)
+    sq = sum(p.info()["active"] * (p.info()["gl_block"] + 1) for p in pools) * ticks
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    bt.run(ticks)
+    e1.record(st)
+    e1.synchronize()
+    return sq / (e0.elapsed_time(e1) / 1000.0)
+
+
 def run_batch(args):
     import torch
-    from ctwin_gb300 import Pool, autotune, two_primes
+    from ctwin_gb300 import Batch, two_primes
     from ctwin_gb300._native import lib
     L = lib()
     rng = random.Random(3)
@@ -368,134 +386,154 @@ def run_batch(args):
         groups.setdefault(c, []).append(b)
     groups = dict(sorted(groups.items()))
     name = {c: f"{c[0]}" + ("" if c[1] == 2 else "w") for c in groups}
-    pools, tune = {}, {}
+    # autotune (CSIZE, CTAs per SM of the batch kernel) on a sample of 64 candidates per class
     t0 = time.perf_counter()
-    for c, bl in groups.items():
-        lg, cs, us = autotune(c[0], len(bl), c[1])
-        tune[c] = {"log2_ctas": lg, "csize": cs, "us_per_squaring_lane": us, "ntt_primes": c[1]}
-        pools[c] = Pool(c[0], len(bl), log2_ctas=lg, csize=cs)
+    sample = {c: bl[:64] for c, bl in groups.items()}
+    tune = []
+    for cs in (8, 16, 32):
+        pools = batch_pools(sample, cs)
+        for occ in (2, 1):
+            with Batch(list(pools.values()), ctas_per_sm=occ) as bt:
+                bt.run(1)
+                torch.cuda.synchronize()
+                tune.append((batch_tick_rate(bt, list(pools.values())), cs, occ))
+        for p in pools.values():
+            p.close()
+    _, csize, occ = max(tune)
     t_tune = time.perf_counter() - t0
     t0 = time.perf_counter()
-    for k, bl in groups.items():
-        assert pools[k].admit_many(bl) == len(bl)
+    pools = batch_pools(groups, csize)
     t_admit = time.perf_counter() - t0
-    info = {k: p.info() for k, p in pools.items()}
-    sq_per_step = {k: info[k]["slots"] * (info[k]["gl_block"] + 1) for k in pools}
-    streams = {k: torch.cuda.ExternalStream(p.stream) for k, p in pools.items()}
-    tl = torch.cuda.Stream()
+    plist = list(pools.values())
+    info = {c: p.info() for c, p in pools.items()}
+    sq_per_step = {c: info[c]["active"] * (info[c]["gl_block"] + 1) for c in pools}
     peak_imad = L.ctw_imad_peak()
-
-    def step():
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(tl)
-        ends = []
-        for k, p in pools.items():
-            streams[k].wait_event(e0)
-            p.run(1)
-            ev = torch.cuda.Event()
-            ev.record(streams[k])
-            ends.append(ev)
-        for ev in ends:
-            tl.wait_event(ev)
-        e1.record(tl)
-        return e0, e1
-
+    bt = Batch(plist, ctas_per_sm=occ)
+    st = torch.cuda.ExternalStream(bt.stream)
     for _ in range(args.warmup):
-        e0, e1 = step()
-        e1.synchronize()
-    for p in pools.values():
-        p.collect(wait=True)
+        bt.run(1)
+    torch.cuda.synchronize()
     times = []
-    launches_per_step = sum(3 + (info[c]["gl_block"] + 63) // 64 for c in pools)   # moves x2, multiply, squarings
+    launches0 = bt.launches
     with ClockSampler(0) as clk:
         torch.cuda.synchronize()
         for _ in range(args.steps):
-            e0, e1 = step()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            bt.run(1)
+            e1.record(st)
             e1.synchronize()
             times.append(e0.elapsed_time(e1) / 1000.0)
         torch.cuda.synchronize()
+    persistent = bt.launches - launches0
     t_dev = sum(times)
     total_sq = sum(sq_per_step.values()) * args.steps
     value = total_sq / t_dev
-    imad = sum(sq_per_step[c] * imad_per_squaring(1 << c[0], c[1]) for c in pools) * args.steps / t_dev
+    imad = sum(sq_per_step[c] * imad_per_squaring(1 << c[0], 3) for c in pools) * args.steps / t_dev
+    imad_exec = sum(sq_per_step[c] * imad_per_squaring(1 << c[0], c[1]) for c in pools) * args.steps / t_dev
 
     # e2e through the public API: host planning + graph launch + collect per step (wall clock)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for p in pools.values():
-            p.run(1)
-        for p in pools.values():
+        bt.run(1)
+        for p in plist:
             p.collect(wait=True)
     t_e2e = time.perf_counter() - t0
-    h2d = sum(3 * info[k]["slots"] * 16 for k in pools)
-
-    # per degree: the pool alone vs the plain path (one candidate per launch sequence)
+    bt.close()
+    h2d = sum(info[c]["slots"] * 2 * 8 + info[c]["slots"] * ((info[c]["gl_block"] + 31) // 32) * 4 for c in pools)
+    # per degree: the pool alone in a batch of its own vs the plain path (one candidate per launch sequence)
     per_degree = {}
     for c, p in pools.items():
-        k = c[0]
-        st = streams[c]
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        p.run(1)
-        e1.record(st)
-        e1.synchronize()
-        alone = sq_per_step[c] / (e0.elapsed_time(e1) / 1000.0)
-        plain = plain_rate(k, groups[c][0])
-        bits = (1 << k) * statistics.mean(math.log2(b) for b in groups[c])
-        per_degree[name[c]] = {"candidates": info[c]["slots"], "gl_block": info[c]["gl_block"], **tune[c],
+        with Batch([p], ctas_per_sm=occ) as b1:
+            alone = batch_tick_rate(b1, [p])
+        plain = plain_rate(c[0], groups[c][0])
+        bits = (1 << c[0]) * statistics.mean(math.log2(b) for b in groups[c])
+        per_degree[name[c]] = {"candidates": len(groups[c]), "gl_block": info[c]["gl_block"], "ntt_primes": c[1],
                                "b_range": [min(groups[c]), max(groups[c])],
                                "batched_alone_sq_per_s": alone, "plain_sq_per_s": plain,
                                "batched_over_plain": alone / plain,
                                "tests_per_s_projected": alone / bits, "plain_tests_per_s_projected": plain / bits}
-    for p in pools.values():
+    for p in plist:
         p.close()
-    clocks = clk.summary()
     line = {
         "metric": "PRP squarings/s (batched, uneven degrees)", "value": value, "unit": "squarings/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": f"{N} candidates, degree 2^k with k uniform in {{12..15}}, b uniform in [2^16, 2^22) "
                                "seed 3, one pool per degree and prime class (b within the two-prime bound, or "
-                               "above it: 'w'), one step = one tick of every pool",
+                               "above it: 'w'), all driven by one batch: per tick one persistent launch of every "
+                               "pool's squarings (per-degree work queues) and one of every multiply",
                    "l2": "inputs larger than L2 (registers of all candidates resident)",
+                   "autotune": {"csize": csize, "ctas_per_sm": occ,
+                                "tried": [{"sq_per_s": r, "csize": c_, "ctas_per_sm": o} for r, c_, o in tune]},
                    "setup_s": {"autotune": t_tune, "admit": t_admit}},
         "per_degree": per_degree,
         "e2e": {"value": total_sq / t_e2e, "unit": "squarings/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": 0},
         "roofline": {"bound": "imad", "achieved": imad / 1e12, "peak": peak_imad / 1e12, "unit": "T IMAD/s",
                      "frac": imad / peak_imad if peak_imad else None, "traffic": None,
+                     "executed_t_imad_per_s": imad_exec / 1e12,
+                     "frac_executed_primes": imad_exec / peak_imad if peak_imad else None,
                      "peak_source": "32-bit IMAD probe kernel run on this GPU in this process"},
-        "cpu_baseline": None, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+        "cpu_baseline": None, "gpu_launches": persistent + 2 * len(plist) * args.steps,
+        "persistent_launches": persistent, "clocks": clk.summary(),
     }
     print(json.dumps(line))
     return 0
 
 
+def plain_replay(reqs, limit_s: float):
+    """The plain path, run for real: the same arrivals (time, degree, b) replayed
+    through one FIFO worker that tests one candidate at a time with
+    PrpEngine.run on the default split.  Stops admitting new requests once the
+    replay has run limit_s; returns per-request latencies of those it served."""
+    from ctwin_gb300 import PrpEngine
+    engines = {}
+    t0 = time.perf_counter()
+    lat = []
+    for ta, k, b in reqs:
+        now = time.perf_counter() - t0
+        if now > limit_s:
+            break
+        if now < ta:
+            time.sleep(ta - now)
+        eng = engines.get(k)
+        if eng is None:
+            eng = engines[k] = PrpEngine(k, 1)
+        eng.run([b])
+        lat.append((k, b, time.perf_counter() - t0 - ta))
+    for e in engines.values():
+        e.close()
+    return lat
+
+
+def pct(v, q):
+    v = sorted(v)
+    return v[min(len(v) - 1, int(q * len(v)))] if v else None
+
+
 def run_serve(args):
     import torch  # noqa: F401  (CUDA context for the library)
-    from ctwin_gb300 import Server, autotune
+    from ctwin_gb300 import Pool, Server, autotune, two_primes
     rng = random.Random(11)
-    degrees = (12, 13, 14)
-    lo, hi = math.log(12), math.log(15)
-    # service demand per degree from the tuned per-lane squaring time
+    kmax = args.serve_max_degree
+    degrees = tuple(range(12, kmax + 1))
+    lo, hi = math.log(12), math.log(kmax + 1)
     # capacity from the pools themselves: device time per lane-squaring of a
-    # 64-slot pool tick (squarings, multiply, register moves, graph launch)
-    from ctwin_gb300 import Pool
-    import torch
-    from ctwin_gb300 import two_primes
+    # pool tick of each degree and prime class (squarings, multiply, register
+    # moves, graph launch); 64 slots up to 2^15, 8 above
     us, frac2 = {}, {}
     for k in degrees:
-        # the server keeps b within the degree's two-prime bound and b above it in
-        # pools of their own: time a 64-slot pool of each class
-        lim = max(b for b in range(1 << 16, 1 << 24, 1 << 12) if two_primes(k, b))
-        frac2[k] = (lim - (1 << 16)) / ((1 << 24) - (1 << 16))
+        slots = 64 if k <= 15 else 8
+        lim = max([b for b in range(1 << 16, 1 << 24, 1 << 12) if two_primes(k, b)] or [(1 << 16) - 1])
+        frac2[k] = max(0.0, (lim - (1 << 16)) / ((1 << 24) - (1 << 16)))
         for primes, (b_lo, b_hi) in ((2, (1 << 16, lim)), (3, (lim + (1 << 12), 1 << 24))):
-            lg, cs, _ = autotune(k, 64, primes)
-            with Pool(k, 64, log2_ctas=lg, csize=cs) as p:
-                p.admit_many([rng.randrange(b_lo, b_hi) for _ in range(64)])
+            if b_hi <= b_lo:
+                continue
+            lg, cs, _ = autotune(k, slots, primes)
+            with Pool(k, slots, log2_ctas=lg, csize=cs) as p:
+                p.admit_many([rng.randrange(b_lo, b_hi) for _ in range(slots)])
                 assert p.prime_count == primes
                 p.run(1)
                 p.collect(wait=True)
@@ -506,11 +544,11 @@ def run_serve(args):
                 p.run(2)
                 e1.record(st)
                 e1.synchronize()
-                us[(k, primes)] = e0.elapsed_time(e1) * 1e3 / (2 * (B + 1) * 64)
+                us[(k, primes)] = e0.elapsed_time(e1) * 1e3 / (2 * (B + 1) * slots)
     mean_bits = {k: (1 << k) * statistics.mean(math.log2(rng.randrange(1 << 16, 1 << 24)) for _ in range(2000))
                  for k in degrees}
     w = {k: (math.log(k + 1) - math.log(k)) / (hi - lo) for k in degrees}
-    demand = sum(w[k] * mean_bits[k] * 1e-6 * (frac2[k] * us[(k, 2)] + (1 - frac2[k]) * us[(k, 3)])
+    demand = sum(w[k] * mean_bits[k] * 1e-6 * (frac2[k] * us.get((k, 2), 0.0) + (1 - frac2[k]) * us[(k, 3)])
                  for k in degrees)
     lam = args.load / demand
     n = args.requests or max(50, int(lam * args.serve_seconds))
@@ -536,51 +574,38 @@ def run_serve(args):
                 res += srv.poll(256, 0)
                 time.sleep(0.0005)
             srv.submit(k, b, tag=i)
-        res += srv.drain(n - len(res), timeout_s=600)
+        res += srv.drain(n - len(res), timeout_s=args.serve_drain)
         t_end = srv.clock()
     srv.close()
-    lat = sorted(r["t_done"] - r["t_submit"] for r in res)
+    lat = [r["t_done"] - r["t_submit"] for r in res]
     bad = sum(1 for r in res if r["status"] != 0 or not r["gl_ok"])
     span = max(r["t_done"] for r in res) - (t0 + reqs[0][0])
     per = {}
     for k in degrees:
-        lk = sorted(r["t_done"] - r["t_submit"] for r in res if r["log2_degree"] == k)
+        lk = [r["t_done"] - r["t_submit"] for r in res if r["log2_degree"] == k]
         if lk:
-            per[str(k)] = {"count": len(lk), "p50_s": lk[len(lk) // 2], "p99_s": lk[min(len(lk) - 1, int(0.99 * len(lk)))]}
-    # plain path: one test at a time through PrpEngine.run; service time per degree
-    # measured on one full test each, then the same arrivals replayed through a FIFO queue
-    from ctwin_gb300 import PrpEngine
-    svc = {}
-    for k in degrees:
-        b = next(bb for (_, kk, bb) in reqs if kk == k) if any(kk == k for _, kk, _ in reqs) else 1 << 20
-        with PrpEngine(k, 1) as eng:
-            t1 = time.perf_counter()
-            eng.run([b])
-            svc[k] = (time.perf_counter() - t1) * (mean_bits[k] / ((1 << k) * math.log2(b)))
-    free, plat = 0.0, []
-    for ta, k, b in reqs:
-        start = max(ta, free)
-        free = start + svc[k] * ((1 << k) * math.log2(b)) / mean_bits[k]
-        plat.append(free - ta)
-    plat.sort()
+            per[str(k)] = {"count": len(lk), "p50_s": pct(lk, 0.5), "p99_s": pct(lk, 0.99), "max_s": max(lk)}
+    # the plain path, run: the first arrivals replayed through one test at a time
+    plain = plain_replay(reqs, args.plain_seconds)
+    served_same = [r["t_done"] - r["t_submit"] for r in res if r["tag"] < len(plain)]
+    plat = [x[2] for x in plain]
     line = {
         "metric": "PRP tests/s (served, mixed degrees)", "value": len(res) / span, "unit": "tests/s",
         "n_gpus": 1, "steps": n, "warmup": 0, "ms_per_step": 1000.0 * span / max(1, len(res)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"{n} Poisson arrivals (seed 11, rate {lam:.2f}/s = {args.load:.0%} of the capacity "
-                               "measured on 64-slot pool ticks), degree 2^k, k log-uniform in [12, 15), "
+        "config": {"workload": f"{n} Poisson arrivals (seed 11, rate {lam:.3f}/s = {args.load:.0%} of the capacity "
+                               f"measured on pool ticks), degree 2^k, k log-uniform in [12, {kmax}], "
                                "b uniform in [2^16, 2^24)",
                    "us_per_lane_squaring": {f"{k}" + ("" if c == 2 else "w"): v for (k, c), v in us.items()},
                    "two_prime_fraction": {str(k): v for k, v in frac2.items()},
                    "hbm_budget_gib": args.hbm_budget, "ticks_per_launch": 1},
-        "latency_s": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
-                      "max": lat[-1]},
-        "per_degree": per, "failed": bad,
-        "plain_path": {"tests_per_s": n / free if free > 0 else None, "p50_s": plat[len(plat) // 2],
-                       "p99_s": plat[min(len(plat) - 1, int(0.99 * len(plat)))],
-                       "service_s": {str(k): v for k, v in svc.items()},
-                       "method": "one full test per degree through PrpEngine.run timed, the same arrivals "
-                                 "replayed through a FIFO queue with those service times (scaled by log2 b)"},
+        "latency_s": {"p50": pct(lat, 0.5), "p99": pct(lat, 0.99), "max": max(lat)},
+        "per_degree": per, "failed": bad, "completed": len(res),
+        "plain_path": {"requests": len(plain), "p50_s": pct(plat, 0.5), "p99_s": pct(plat, 0.99),
+                       "served_p50_s_same_requests": pct(served_same, 0.5),
+                       "served_p99_s_same_requests": pct(served_same, 0.99),
+                       "method": f"the first {len(plain)} arrivals replayed at their arrival times through one FIFO "
+                                 "worker (PrpEngine.run, one test at a time, default split), measured"},
         "wall_s": t_end,
         "e2e": {"value": len(res) / span, "unit": "tests/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
         "clocks": clk.summary(),
@@ -785,6 +810,11 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--load", type=float, default=0.8, help="serve: offered load / tuned capacity")
     ap.add_argument("--hbm-budget", type=int, default=64, help="serve: pool budget in GiB")
+    ap.add_argument("--serve-max-degree", type=int, default=14, choices=range(12, 19),
+                    help="serve: degrees 2^12 .. 2^this (log-uniform)")
+    ap.add_argument("--serve-drain", type=float, default=1800.0, help="serve: seconds to wait for the last tests")
+    ap.add_argument("--plain-seconds", type=float, default=120.0,
+                    help="serve: seconds of the plain-path replay (the first arrivals, one test at a time)")
     ap.add_argument("--log2-degree", type=int, default=16, choices=range(12, 19),
                     help="single: degree of the candidate (2^16 is the headline configuration)")
     ap.add_argument("--cpu-seconds", type=float, default=0.0,
