@@ -85,6 +85,7 @@ def grid_emu():
 
 @pytest.mark.parametrize("ln,lm,primes,csize,b,threads,mult", [
     (16, 10, 2, 16, 1330358, 64, 3),     # the 2^16 single-test shape, two primes, Fermat base 3
+    (16, 10, 2, 8, 1330358, 64, 3),      # the same with CSIZE 8 (the unrolled carry chain)
     (16, 11, 3, 32, 2000000003, 64, 2),  # three primes, b near 2^31 (128-bit carries)
     (17, 12, 2, 8, 1330358, 32, 2),      # 4096-coefficient CTAs
     (18, 11, 3, 16, 1330358, 32, 3),     # 128 CTAs
