@@ -12,8 +12,8 @@
 //        engine_emu batch <ticks>
 // resume: the whole test stops at its first Gerbicz-Li checkpoint, saves the
 // reference's context file there, and a fresh engine reads it and finishes.
-// batch: pools of degrees 2^12 (two and three primes), 2^13 and 2^14 run
-// <ticks> ticks through one batch (ctw_batch_run: the persistent kernel with
+// batch: pools of degrees 2^12 (two and three primes), 2^13 and 2^14 (ticks
+// of 8 squarings) run <ticks> ticks through one batch (ctw_batch_run: the persistent kernel with
 // per-degree queues) and, as a second set of the same pools, through
 // ctw_pool_run; prints the number of register words that differ.
 // mul: ctw_prp_mul_noalloc of the lanes' x and y (int32 digits, x then y, read
@@ -113,7 +113,8 @@ static int run_batch(int argc, char **argv)
 		for (const Spec &sp : specs)
 		{
 			ctw_pool *p = nullptr;
-			if ((rc = ctw_pool_create(sp.ln, sp.slots, sp.ln - 12, 8, 3, 0, &p))) break;
+			// Gerbicz-Li blocks of 8 squarings keep the emulated ticks short
+			if ((rc = ctw_pool_create(sp.ln, sp.slots, sp.ln - 12, 8, 3, 8, &p))) break;
 			(set ? alone : batched).push_back(p);
 			for (size_t i = 0; i < sp.b.size() && !rc; ++i) rc = ctw_pool_admit(p, sp.b[i], i) < 0;
 		}

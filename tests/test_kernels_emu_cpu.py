@@ -334,7 +334,7 @@ def test_batch_emulated_equals_pools(engine_emu):
     (prp_pool.cu's batch ticks: every pool's squarings in one persistent launch
     of clusters of 8 CTAs with per-degree queues, prp_batch.cu) against the
     same pools ticked on their own: every register of every slot equal after
-    two ticks (base 3)."""
+    two ticks of 8 squarings and a multiply (base 3)."""
     r = subprocess.run([engine_emu, "batch", "2"], capture_output=True, text=True, timeout=1200)
     assert r.returncode == 0, r.stdout + r.stderr[-2000:]
     assert " differ 0" in r.stdout
