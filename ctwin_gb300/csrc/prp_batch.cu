@@ -25,6 +25,15 @@ __device__ __forceinline__ unsigned ld_volatile_u32(const unsigned *p)
 	return *reinterpret_cast<const volatile unsigned *>(p);
 }
 
+// One item of lanes on 2^LGI CTAs each; not inlined, so that every body gets
+// the build's registers to itself instead of sharing one allocation.
+template <int NP, int LGI>
+__device__ __noinline__ void batch_item(const PrpKernelArgs &a, uint32_t *sm, int lane, int g, int rbase)
+{
+	if constexpr (LGI == 0) prp_body<0, true, NP, true>(a, sm, lane, 0);
+	else cols_body<LGI, true, NP, true>(a, sm, lane, g, rbase);
+}
+
 template <int NP> struct BatchBounds {
 	static constexpr int threads = NP == 2 ? 512 : 384;    // the 4096-coefficient dense builds
 };
@@ -73,10 +82,10 @@ __global__ void __launch_bounds__(BatchBounds<NP>::threads, OCC)
 		const int lane = idx * (BATCH_CLUSTER >> lg) + sub;
 		switch (lg)
 		{
-		case 0: prp_body<0, true, NP, true>(C.a, sm, lane, 0); break;
-		case 1: cols_body<1, true, NP, true>(C.a, sm, lane, g, sub << 1); break;
-		case 2: cols_body<2, true, NP, true>(C.a, sm, lane, g, sub << 2); break;
-		default: cols_body<3, true, NP, true>(C.a, sm, lane, g, 0); break;
+		case 0: batch_item<NP, 0>(C.a, sm, lane, 0, 0); break;
+		case 1: batch_item<NP, 1>(C.a, sm, lane, g, sub << 1); break;
+		case 2: batch_item<NP, 2>(C.a, sm, lane, g, sub << 2); break;
+		default: batch_item<NP, 3>(C.a, sm, lane, g, 0); break;
 		}
 		cl.sync();                                   // every CTA done before the next item is posted
 	}

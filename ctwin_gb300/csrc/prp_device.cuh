@@ -448,33 +448,6 @@ __device__ __forceinline__ int32_t reduce_b<int64_t>(int64_t &f, uint32_t b, uin
 	return s ? -(int32_t)r_l : (int32_t)r_l;
 }
 
-// Floor division of s by b for |s| < 2^50 through a double-precision
-// reciprocal binv = 1/b: the estimate floor(s binv) is off by at most one
-// (relative error below 2^-51), corrected once each way; r in [0, b) after.
-// Sets ST_BARRETT_RANGE if s is out of that range.
-__device__ __forceinline__ int64_t floor_div_small(int64_t s, int64_t b, double binv, int64_t &r, uint32_t &err)
-{
-	if (s >= ((int64_t)1 << 50) || s <= -((int64_t)1 << 50)) err |= ST_BARRETT_RANGE;
-	int64_t f = __double2ll_rd(__ll2double_rn(s) * binv);
-	r = s - f * b;
-	if (r < 0) { f -= 1; r += b; }
-	else if (r >= b) { f += 1; r -= b; }
-	return f;
-}
-
-// Truncated division of s (|s| < 2^50) by b with the remainder's sign that of
-// s: the same quotient and digit as reduce_b<int64_t>, which is an exact
-// truncated division wherever 64-bit carries are used (|s| < 2^62: both of its
-// Barrett steps then estimate the quotient within one).
-__device__ __forceinline__ int32_t trunc_div_small(int64_t &s, int64_t b, double binv, uint32_t &err)
-{
-	int64_t r;
-	int64_t f = floor_div_small(s, b, binv, r, err);
-	if (f < 0 && r != 0) { f += 1; r -= b; }
-	s = f;
-	return (int32_t)r;
-}
-
 constexpr uint64_t Q21 = (uint64_t)Q2 * Q1;
 
 // Balanced CRT value of residues r0, r1, r2 (each in [0, q)) as 96-bit two's

@@ -528,34 +528,21 @@ __host__ __device__ __forceinline__ size_t grid2_words(int lg, int lm, int np)
 }
 
 // Normalize1 of one chunk of CSZ Garner words (64-bit, two primes or narrow
-// three primes), the reference's chain acc <- trunc((acc + mult w_i) / b),
-// digit_i = the remainder, with a short critical path: every mult w_i is first
-// split as Q_i b + R_i (floor, 0 <= R_i < b) by reduce_b, independently of the
-// others; along the chain only the small s = acc + R_i (|s| < 2^42 where
-// 64-bit carries are used) is divided, then acc = Q_i + floor(s / b) with the
-// truncation rule applied to the sum.  Quotients and digits equal reduce_b's.
+// three primes): the words are loaded first, then the carry chain runs on
+// registers.  Returns the chunk's carry.
 template <int CSZ>
 __device__ __forceinline__ int64_t norm1_chunk64(const uint32_t *W0, const uint32_t *W1, int32_t *XDo, int mult,
-                                                  uint32_t b, uint32_t b_inv, int b_s, double binv, uint32_t &err)
+                                                  uint32_t b, uint32_t b_inv, int b_s, uint32_t &err)
 {
-	int64_t Q[CSZ], R[CSZ];
+	int64_t v[CSZ];
 #pragma unroll
-	for (int i = 0; i < CSZ; ++i)
-	{
-		int64_t t = (int64_t)((uint64_t)W0[i] | ((uint64_t)W1[i] << 32)) * (int64_t)mult;
-		const int32_t r = reduce_b<int64_t>(t, b, b_inv, b_s, err);   // t <- trunc quotient
-		Q[i] = r < 0 ? t - 1 : t;
-		R[i] = r < 0 ? (int64_t)r + b : (int64_t)r;
-	}
+	for (int i = 0; i < CSZ; ++i) v[i] = (int64_t)((uint64_t)W0[i] | ((uint64_t)W1[i] << 32));
 	int64_t acc = 0;
 #pragma unroll
 	for (int i = 0; i < CSZ; ++i)
 	{
-		int64_t r;
-		int64_t f = Q[i] + floor_div_small(acc + R[i], (int64_t)b, binv, r, err);
-		if (f < 0 && r != 0) { f += 1; r -= b; }
-		XDo[i] = (int32_t)r;
-		acc = f;
+		acc += v[i] * (int64_t)mult;
+		XDo[i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
 	}
 	return acc;
 }
@@ -587,7 +574,6 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
 	const int b_s = (int)a.lane_b[4 * lane + 2];
 	const bool narrow = NP == 2 || (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;
-	const double binv = 1.0 / (double)b;
 	uint32_t err = 0;
 
 	{
@@ -848,10 +834,9 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 			const int h = c / runc, j = c - h * runc;
 			const int base = h * MG + j * csz;
 			int64_t f;
-			if (narrow && csz == 8)
-				f = norm1_chunk64<8>(XC + base, XC + M + base, XD + base, mult, b, b_inv, b_s, binv, err);
+			if (narrow && csz == 8) f = norm1_chunk64<8>(XC + base, XC + M + base, XD + base, mult, b, b_inv, b_s, err);
 			else if (narrow && csz == 16)
-				f = norm1_chunk64<16>(XC + base, XC + M + base, XD + base, mult, b, b_inv, b_s, binv, err);
+				f = norm1_chunk64<16>(XC + base, XC + M + base, XD + base, mult, b, b_inv, b_s, err);
 			else if (narrow)
 			{
 				int64_t acc = 0;
@@ -882,8 +867,6 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		// last thread (fence and count) while threads 0 .. ncl - G - 1 carry into the
 		// chunks j > 0, which need no remote carry
 		for (int h = tid; h < G; h += nt) gc[(size_t)g * G + h] = xch[h];
-		// a chunk carry plus digits: with 64-bit carries |acc| < 2^42, divided
-		// through the reciprocal; otherwise by reduce_b
 		auto carry_in = [&](int h, int j, int64_t acc) {
 			int32_t *Xh = XD + h * MG + j * csz;
 			int i = 0;
@@ -891,7 +874,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 			for (; i < csz - 1; ++i)
 			{
 				acc += Xh[i];
-				Xh[i] = narrow ? trunc_div_small(acc, (int64_t)b, binv, err) : reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+				Xh[i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
 				if (acc == 0) { done = true; break; }
 			}
 			if (!done)

@@ -635,8 +635,10 @@ static int plan_ticks(ctw_pool *p, int T, int &k, int &lanes, int &np)
 	int hi = 0;
 	for (int s = 0; s < p->slots; ++s)
 		if (p->slot[(size_t)s].state != SLOT_FREE) hi = s + 1;
-	// launch over the lowest slots only, in steps of 8 lanes (one graph per step)
-	lanes = std::min(p->slots, std::max(8, (hi + 7) / 8 * 8));
+	// launch over the lowest slots only, in steps of 8 lanes (one graph per
+	// step); from degree 2^15 up a lane fills SMs by itself: steps of one
+	const int step = p->ln >= 15 ? 1 : 8;
+	lanes = std::min(p->slots, std::max(step, (hi + step - 1) / step * step));
 	np = pool_primes(p, lanes);
 	memset(p->h_aux[k], 0, (size_t)T * 2 * S * sizeof(PrpLaneAux));
 	memset(p->h_stage[k], 0, (size_t)T * S * p->nws * 4);
