@@ -153,6 +153,42 @@ __device__ __forceinline__ void group_inv(uint32_t (&u)[R], const uint32_t *__re
 	}
 }
 
+// The same groups with Shoup pairs (w, floor(w 2^32 / q)) of plain roots.
+template <int R, class Idx>
+__device__ __forceinline__ void group_fwd_s(uint32_t (&u)[R], const uint2 *__restrict__ tw, Idx idx, uint32_t q)
+{
+	constexpr int r = Log2<R>::v;
+#pragma unroll
+	for (int t = 0; t < r; ++t)
+	{
+		const int half = R >> (t + 1);
+#pragma unroll
+		for (int k = 0; k < R; ++k)
+		{
+			if (k & half) continue;
+			const uint2 w = tw[idx(t, k >> (r - t))];
+			bf_fwd_s(u[k], u[k + half], w.x, w.y, q);
+		}
+	}
+}
+template <int R, class Idx>
+__device__ __forceinline__ void group_inv_s(uint32_t (&u)[R], const uint2 *__restrict__ ti, Idx idx, uint32_t q)
+{
+	constexpr int r = Log2<R>::v;
+#pragma unroll
+	for (int t = r - 1; t >= 0; --t)
+	{
+		const int half = R >> (t + 1);
+#pragma unroll
+		for (int k = 0; k < R; ++k)
+		{
+			if (k & half) continue;
+			const uint2 w = ti[idx(t, k >> (r - t))];
+			bf_inv_s(u[k], u[k + half], w.x, w.y, q);
+		}
+	}
+}
+
 // Pointwise step of the last pass: square, multiply by the stored transform
 // of y, or store the transform (values leave in [0, 2q)).
 enum LocalMode { LM_FWD_ONLY = 0, LM_SQUARE = 1, LM_MUL = 2 };

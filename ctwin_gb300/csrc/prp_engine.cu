@@ -289,9 +289,15 @@ int build_tables(ctw_prp *h)
 	const size_t words = h->G * 3 * h->M, swords = h->G * 3 * 256 * 2;
 	std::vector<uint32_t> tf(words), ti(words), tfs(swords), tis(swords), xr(3 * 2 * 128);
 	prp_build_tables(h->ln, h->lg, tf.data(), ti.data(), h->proto, tfs.data(), tis.data(), xr.data());
-	// the grid kernel of 1024- and 2048-coefficient CTAs lays its local roots out per sub-block
-	if (h->grid && h->lm <= 11) prp_build_grid2_tables(h->ln, h->lg, tf.data(), ti.data());
-	const size_t bytes = words * sizeof(uint32_t);
+	// the grid kernel of 1024- and 2048-coefficient CTAs lays its local roots out
+	// per sub-block, as Shoup pairs
+	if (h->grid && h->lm <= 11)
+	{
+		tf.assign(2 * words, 0);
+		ti.assign(2 * words, 0);
+		prp_build_grid2_tables(h->ln, h->lg, tf.data(), ti.data());
+	}
+	const size_t bytes = tf.size() * sizeof(uint32_t);
 	if (h->grid)
 	{
 		CTW_CUDA(cudaMalloc(&h->d_xr, xr.size() * 4));

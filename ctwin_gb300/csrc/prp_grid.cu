@@ -460,7 +460,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 //       C = LM - 8) across the CTA
 //   W   local levels C .. LM-1, the pointwise step and their inverse on
 //       sub-blocks of 256 coefficients, one warp each: three register passes
-//       (radix 8, 8, 4) with warp-synchronous exchanges through shared memory
+//       (radix 8, 8, 4) with warp-synchronous exchanges through shared memory;
+//       local roots as Shoup pairs (one high and two low products each)
 //   A'  inverse local levels C-1 .. 0 fused with the publication of the row
 //   Y1  gather of the columns fused with the first inverse cross pass
 //   Y2  the last inverse cross pass (with the final scale) fused with Garner,
@@ -523,8 +524,8 @@ __device__ __forceinline__ void warp_sync()
 __host__ __device__ __forceinline__ size_t grid2_words(int lg, int lm, int np)
 {
 	const size_t M = (size_t)1 << lm, G = (size_t)1 << lg;
-	// XC, XR, XD, chunk carries (M/8 int64), run-end carries (G int64), cross roots, TF + TI
-	return 2 * np * M + M + M / 4 + 2 * G + 2 * np * G + 2 * np * M;
+	// XC, XR, XD, chunk carries (M/8 int64), run-end carries (G int64), cross roots, TF + TI (pairs)
+	return 2 * np * M + M + M / 4 + 2 * G + 2 * np * G + 4 * np * M;
 }
 
 // Normalize1 of one chunk of CSZ Garner words (64-bit, two primes or narrow
@@ -567,8 +568,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	int64_t *fch = reinterpret_cast<int64_t *>(XD + M);         // [M/8]
 	int64_t *xch = fch + M / 8;                                 // [G]
 	uint32_t *XRT = reinterpret_cast<uint32_t *>(xch + G);      // [NP][2][G]
-	uint32_t *TF = XRT + NP * 2 * G;                            // [NP][M]
-	uint32_t *TI = TF + NP * M;
+	uint32_t *TF = XRT + NP * 2 * G;                            // [NP][M][2] Shoup pairs
+	uint32_t *TI = TF + NP * 2 * M;
 	if (tid == 0) dead = 0;
 
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
@@ -577,8 +578,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	uint32_t err = 0;
 
 	{
-		const uint32_t *tfg = a.tf + (size_t)g * 3 * M, *tig = a.ti + (size_t)g * 3 * M;
-		for (int i = tid; i < NP * M; i += nt) { TF[i] = tfg[i]; TI[i] = tig[i]; }
+		const uint32_t *tfg = a.tf + (size_t)g * 3 * 2 * M, *tig = a.ti + (size_t)g * 3 * 2 * M;
+		for (int i = tid; i < NP * 2 * M; i += nt) { TF[i] = tfg[i]; TI[i] = tig[i]; }
 		for (int i = tid; i < NP * 2 * G; i += nt) XRT[i] = ga.xr[(i / G) * 128 + i % G];
 	}
 
@@ -635,20 +636,21 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	auto wphase = [&](int pi, int sb, int mode) {
 		const uint32_t q = qv(pi), qi = qiv(pi);
 		uint32_t *S = XR + pi * M + sb * 256;
-		const uint32_t *tf = TF + pi * M + sb * 256, *ti = TI + pi * M + sb * 256;
+		const uint2 *tf = reinterpret_cast<const uint2 *>(TF) + pi * M + sb * 256;
+		const uint2 *ti = reinterpret_cast<const uint2 *>(TI) + pi * M + sb * 256;
 		const int l = lane32, c4 = l >> 2, r4 = l & 3;
 		uint32_t u[8];
 		// W1: p = l + 32 k, levels C .. C+2
 #pragma unroll
 		for (int k = 0; k < 8; ++k) u[k] = S[sbx(l + 32 * k)];
-		group_fwd<8>(u, tf, [&](int t, int kk) { return (1 << t) + kk; }, q, qi, false, 0);
+		group_fwd_s<8>(u, tf, [&](int t, int kk) { return (1 << t) + kk; }, q);
 #pragma unroll
 		for (int k = 0; k < 8; ++k) S[sbx(l + 32 * k)] = u[k];
 		warp_sync();
 		// W2: p = 32 c + r + 4 k, levels C+3 .. C+5
 #pragma unroll
 		for (int k = 0; k < 8; ++k) u[k] = S[sbx(32 * c4 + r4 + 4 * k)];
-		group_fwd<8>(u, tf, [&](int t, int kk) { return (8 << t) + (c4 << t) + kk; }, q, qi, false, 0);
+		group_fwd_s<8>(u, tf, [&](int t, int kk) { return (8 << t) + (c4 << t) + kk; }, q);
 #pragma unroll
 		for (int k = 0; k < 8; ++k) S[sbx(32 * c4 + r4 + 4 * k)] = u[k];
 		warp_sync();
@@ -663,11 +665,11 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		for (int e = 0; e < 2; ++e)
 		{
 			uint32_t *v = u + 4 * e;
-			const uint32_t w6 = tf[64 + 32 * e + l];
-			bf_fwd(v[0], v[2], w6, q, qi);
-			bf_fwd(v[1], v[3], w6, q, qi);
-			bf_fwd(v[0], v[1], tf[128 + 32 * (2 * e) + l], q, qi);
-			bf_fwd(v[2], v[3], tf[128 + 32 * (2 * e + 1) + l], q, qi);
+			const uint2 w6 = tf[64 + 32 * e + l], w7a = tf[128 + 32 * (2 * e) + l], w7b = tf[128 + 32 * (2 * e + 1) + l];
+			bf_fwd_s(v[0], v[2], w6.x, w6.y, q);
+			bf_fwd_s(v[1], v[3], w6.x, w6.y, q);
+			bf_fwd_s(v[0], v[1], w7a.x, w7a.y, q);
+			bf_fwd_s(v[2], v[3], w7b.x, w7b.y, q);
 		}
 		uint32_t *Y = scr + pi * M + sb * 256 + 8 * l;          // the transform of y, logical order
 		if (mode == LM_FWD_ONLY)
@@ -695,24 +697,24 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		for (int e = 0; e < 2; ++e)
 		{
 			uint32_t *v = u + 4 * e;
-			bf_inv(v[0], v[1], ti[128 + 32 * (2 * e) + l], q, qi);
-			bf_inv(v[2], v[3], ti[128 + 32 * (2 * e + 1) + l], q, qi);
-			const uint32_t w6 = ti[64 + 32 * e + l];
-			bf_inv(v[0], v[2], w6, q, qi);
-			bf_inv(v[1], v[3], w6, q, qi);
+			const uint2 w6 = ti[64 + 32 * e + l], w7a = ti[128 + 32 * (2 * e) + l], w7b = ti[128 + 32 * (2 * e + 1) + l];
+			bf_inv_s(v[0], v[1], w7a.x, w7a.y, q);
+			bf_inv_s(v[2], v[3], w7b.x, w7b.y, q);
+			bf_inv_s(v[0], v[2], w6.x, w6.y, q);
+			bf_inv_s(v[1], v[3], w6.x, w6.y, q);
 		}
 		*reinterpret_cast<uint4 *>(S + sbx(8 * l)) = make_uint4(u[0], u[1], u[2], u[3]);
 		*reinterpret_cast<uint4 *>(S + sbx(8 * l + 4)) = make_uint4(u[4], u[5], u[6], u[7]);
 		warp_sync();
 #pragma unroll
 		for (int k = 0; k < 8; ++k) u[k] = S[sbx(32 * c4 + r4 + 4 * k)];
-		group_inv<8>(u, ti, [&](int t, int kk) { return (8 << t) + (c4 << t) + kk; }, q, qi, false, 0, 0, 0);
+		group_inv_s<8>(u, ti, [&](int t, int kk) { return (8 << t) + (c4 << t) + kk; }, q);
 #pragma unroll
 		for (int k = 0; k < 8; ++k) S[sbx(32 * c4 + r4 + 4 * k)] = u[k];
 		warp_sync();
 #pragma unroll
 		for (int k = 0; k < 8; ++k) u[k] = S[sbx(l + 32 * k)];
-		group_inv<8>(u, ti, [&](int t, int kk) { return (1 << t) + kk; }, q, qi, false, 0, 0, 0);
+		group_inv_s<8>(u, ti, [&](int t, int kk) { return (1 << t) + kk; }, q);
 #pragma unroll
 		for (int k = 0; k < 8; ++k) S[sbx(l + 32 * k)] = u[k];
 	};
@@ -741,7 +743,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		for (int it = tid; it < NP * 128; it += nt)
 		{
 			const int pi = it >> 7, m0 = 2 * (it & 127);
-			const uint32_t q = qv(pi), qi = qiv(pi);
+			const uint32_t q = qv(pi);
 			uint32_t v0[NSB], v1[NSB];
 #pragma unroll
 			for (int j = 0; j < NSB; ++j)
@@ -751,8 +753,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 				v0[j] = w.x;
 				v1[j] = w.y;
 			}
-			group_fwd<NSB>(v0, TF + pi * M, aidx, q, qi, false, 0);
-			group_fwd<NSB>(v1, TF + pi * M, aidx, q, qi, false, 0);
+			group_fwd_s<NSB>(v0, reinterpret_cast<const uint2 *>(TF) + pi * M, aidx, q);
+			group_fwd_s<NSB>(v1, reinterpret_cast<const uint2 *>(TF) + pi * M, aidx, q);
 #pragma unroll
 			for (int j = 0; j < NSB; ++j)
 				*reinterpret_cast<uint2 *>(XR + pi * M + j * 256 + sbx(m0)) = make_uint2(v0[j], v1[j]);
@@ -766,7 +768,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		for (int it = tid; it < NP * 128; it += nt)
 		{
 			const int pi = it >> 7, m0 = 2 * (it & 127);
-			const uint32_t q = qv(pi), qi = qiv(pi);
+			const uint32_t q = qv(pi);
 			uint32_t v0[NSB], v1[NSB];
 #pragma unroll
 			for (int j = 0; j < NSB; ++j)
@@ -775,8 +777,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 				v0[j] = w.x;
 				v1[j] = w.y;
 			}
-			group_inv<NSB>(v0, TI + pi * M, aidx, q, qi, false, 0, 0, 0);
-			group_inv<NSB>(v1, TI + pi * M, aidx, q, qi, false, 0, 0, 0);
+			group_inv_s<NSB>(v0, reinterpret_cast<const uint2 *>(TI) + pi * M, aidx, q);
+			group_inv_s<NSB>(v1, reinterpret_cast<const uint2 *>(TI) + pi * M, aidx, q);
 #pragma unroll
 			for (int j = 0; j < NSB; ++j)
 				st_l2_u2(gr + (size_t)g * 3 * M + pi * M + j * 256 + m0, make_uint2(v0[j], v1[j]));

@@ -152,14 +152,15 @@ inline void prp_build_tables(int ln, int lg, uint32_t *tf, uint32_t *ti, PrpKern
 // Root tables of the grid kernel with warp-local sub-transforms
 // (prp_kernel_grid2: 2^lg CTAs of M = 2^lm coefficients, lm = 10 or 11): the
 // first C = lm - 8 local levels run across the CTA (radix 2^C), the last 8 on
-// sub-blocks of 256 coefficients, one warp each.  Per CTA g and prime, M words
-// (Montgomery form), forward in tf and inverse in ti: for sub-block sb, words
-// [256 sb, 256 sb + 256) hold its roots of local level C + l at index 2^l + jj
-// (jj the block within the sub-block; for l = 6 and 7, jj = 2 u + e and
-// 4 u + e are stored at 2^l + 32 e + u, the order a warp reads them in); word
-// 256 j (j = 1 .. 2^C - 1, unused by the sub-blocks) holds the root of local
-// level L < C, block J with 2^L + J = j.  The root of local level L, block J
-// of CTA g is that of global block (G + g) 2^L + J, as in prp_build_tables.
+// sub-blocks of 256 coefficients, one warp each.  Per CTA g and prime, M
+// Shoup pairs (w, floor(w 2^32 / q)) of plain roots, 2M words ([G][3][M][2]),
+// forward in tf and inverse in ti: for sub-block sb, pairs [256 sb, 256 sb +
+// 256) hold its roots of local level C + l at index 2^l + jj (jj the block
+// within the sub-block; for l = 6 and 7, jj = 2 u + e and 4 u + e are stored
+// at 2^l + 32 e + u, the order a warp reads them in); pair 256 j (j = 1 ..
+// 2^C - 1, unused by the sub-blocks) holds the root of local level L < C,
+// block J with 2^L + J = j.  The root of local level L, block J of CTA g is
+// that of global block (G + g) 2^L + J, as in prp_build_tables.
 inline void prp_build_grid2_tables(int ln, int lg, uint32_t *tf, uint32_t *ti)
 {
 	using namespace tables_detail;
@@ -167,8 +168,8 @@ inline void prp_build_grid2_tables(int ln, int lg, uint32_t *tf, uint32_t *ti)
 	static const uint32_t kG[3] = { QGEN0, QGEN1, QGEN2 };
 	const int lm = ln - lg, C = lm - 8;
 	const size_t D = size_t(1) << ln, G = size_t(1) << lg, M = D / G;
-	memset(tf, 0, G * 3 * M * sizeof(uint32_t));
-	memset(ti, 0, G * 3 * M * sizeof(uint32_t));
+	memset(tf, 0, G * 3 * 2 * M * sizeof(uint32_t));
+	memset(ti, 0, G * 3 * 2 * M * sizeof(uint32_t));
 	for (int pi = 0; pi < 3; ++pi)
 	{
 		const uint32_t q = kQ[pi];
@@ -180,11 +181,13 @@ inline void prp_build_grid2_tables(int ln, int lg, uint32_t *tf, uint32_t *ti)
 		}
 		for (size_t g = 0; g < G; ++g)
 		{
-			uint32_t *f = tf + (g * 3 + pi) * M, *iv = ti + (g * 3 + pi) * M;
+			uint32_t *f = tf + (g * 3 + pi) * 2 * M, *iv = ti + (g * 3 + pi) * 2 * M;
 			auto put = [&](size_t idx, int L, size_t J) {
-				const uint32_t w = W[((G + g) << L) + J];
-				f[idx] = mont(w, q);
-				iv[idx] = mont(invmod(w, q), q);
+				const uint32_t w = W[((G + g) << L) + J], wi = invmod(w, q);
+				f[2 * idx] = w;
+				f[2 * idx + 1] = (uint32_t)(((uint64_t)w << 32) / q);
+				iv[2 * idx] = wi;
+				iv[2 * idx + 1] = (uint32_t)(((uint64_t)wi << 32) / q);
 			};
 			for (int L = 0; L < C; ++L)
 				for (size_t J = 0; J < ((size_t)1 << L); ++J) put((((size_t)1 << L) + J) * 256, L, J);

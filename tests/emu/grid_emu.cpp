@@ -66,7 +66,7 @@ static Kern pick(int lg, int lm, int np)
 static size_t grid_words(int lg, int lm, int tw, int np)
 {
 	const size_t M = (size_t)1 << lm, G = (size_t)1 << lg;
-	if (lm <= 11) return 2 * np * M + M + M / 4 + 2 * G + 2 * np * G + 2 * np * M;
+	if (lm <= 11) return 2 * np * M + M + M / 4 + 2 * G + 2 * np * G + 4 * np * M;
 	return 2 * np * M + M / 4 + 2 * G + 2 * np * G + (tw ? 2 * np * M : 0) + (lm == 12 ? 2 * (size_t)np * 512 : 0);
 }
 
@@ -130,7 +130,12 @@ int main(int argc, char **argv)
 	PrpKernelArgs a{};
 	std::vector<uint32_t> tf(G * 3 * M), ti(G * 3 * M), tfs(G * 3 * 256 * 2), tis(G * 3 * 256 * 2), xr(768);
 	prp_build_tables(ln, lg, tf.data(), ti.data(), a, tfs.data(), tis.data(), xr.data());
-	if (lm <= 11) prp_build_grid2_tables(ln, lg, tf.data(), ti.data());
+	if (lm <= 11)
+	{
+		tf.assign(2 * tf.size(), 0);
+		ti.assign(2 * ti.size(), 0);
+		prp_build_grid2_tables(ln, lg, tf.data(), ti.data());
+	}
 	std::vector<int32_t> x(D), y(D), out(D);
 	std::vector<uint32_t> scratch(3 * D), laneb(4), status(1, 0), gx(3 * D), gr(3 * D), bar(GRID_BAR_WORDS);
 	std::vector<long long> gc((size_t)G * G);
