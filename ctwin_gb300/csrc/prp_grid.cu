@@ -524,27 +524,37 @@ __device__ __forceinline__ void warp_sync()
 __host__ __device__ __forceinline__ size_t grid2_words(int lg, int lm, int np)
 {
 	const size_t M = (size_t)1 << lm, G = (size_t)1 << lg;
-	// XC, XR, XD, chunk carries (M/8 int64), run-end carries (G int64), cross roots, TF + TI (pairs)
-	return 2 * np * M + M + M / 4 + 2 * G + 2 * np * G + 4 * np * M;
+	// XC (with a 16-word pad every 8 rows), XR, XD, chunk carries (M/8 int64),
+	// run-end carries (G int64), cross roots, TF + TI (pairs)
+	return 2 * np * M + np * (G / 8) * 16 + M + M / 4 + 2 * G + 2 * np * G + 4 * np * M;
 }
 
 // Normalize1 of one chunk of CSZ Garner words (64-bit, two primes or narrow
 // three primes): the words are loaded first, then the carry chain runs on
 // registers.  Returns the chunk's carry.
+// W0, W1 and XDo are 16-byte aligned: the words move in 16-byte pieces.
 template <int CSZ>
 __device__ __forceinline__ int64_t norm1_chunk64(const uint32_t *W0, const uint32_t *W1, int32_t *XDo, int mult,
                                                   uint32_t b, uint32_t b_inv, int b_s, uint32_t &err)
 {
-	int64_t v[CSZ];
+	uint32_t lo[CSZ], hi[CSZ];
 #pragma unroll
-	for (int i = 0; i < CSZ; ++i) v[i] = (int64_t)((uint64_t)W0[i] | ((uint64_t)W1[i] << 32));
+	for (int i = 0; i < CSZ; i += 4)
+	{
+		const uint4 a0 = *reinterpret_cast<const uint4 *>(W0 + i), a1 = *reinterpret_cast<const uint4 *>(W1 + i);
+		lo[i] = a0.x; lo[i + 1] = a0.y; lo[i + 2] = a0.z; lo[i + 3] = a0.w;
+		hi[i] = a1.x; hi[i + 1] = a1.y; hi[i + 2] = a1.z; hi[i + 3] = a1.w;
+	}
+	int32_t d[CSZ];
 	int64_t acc = 0;
 #pragma unroll
 	for (int i = 0; i < CSZ; ++i)
 	{
-		acc += v[i] * (int64_t)mult;
-		XDo[i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+		acc += (int64_t)((uint64_t)lo[i] | ((uint64_t)hi[i] << 32)) * (int64_t)mult;
+		d[i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
 	}
+#pragma unroll
+	for (int i = 0; i < CSZ; i += 4) *reinterpret_cast<int4 *>(XDo + i) = make_int4(d[i], d[i + 1], d[i + 2], d[i + 3]);
 	return acc;
 }
 
@@ -563,7 +573,12 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	const int csz = a.csize, runc = MG / csz, ncl = G * runc, cb = g * MG;
 
 	uint32_t *XC = sm;                                          // [NP][G][MG]
-	uint32_t *XR = XC + NP * M;                                 // [NP][M] (sub-block swizzle)
+	// column planes of MP words: row h at h * MG, plus a 16-word pad after every
+	// 8 rows when a row is 16 words, so that the half-warps of a cross pass whose
+	// rows are 8 apart fall in different banks
+	constexpr int MP = M + (G / 8) * 16;
+	auto xcp = [](int h, int tt) { return h * MG + (MG == 16 ? (h >> 3) * 16 : 0) + tt; };
+	uint32_t *XR = XC + NP * MP;                                // [NP][M] (sub-block swizzle)
 	int32_t *XD = reinterpret_cast<int32_t *>(XR + NP * M);     // [G][MG] digits
 	int64_t *fch = reinterpret_cast<int64_t *>(XD + M);         // [M/8]
 	int64_t *xch = fch + M / 8;                                 // [G]
@@ -629,8 +644,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 			for (int k = 0; k < R; ++k) store(pi, hbase + k * stride, tt, u[k]);
 		}
 	};
-	auto ld_xc = [&](int pi, int h, int tt, uint32_t) { return XC[pi * M + h * MG + tt]; };
-	auto st_xc = [&](int pi, int h, int tt, uint32_t v) { XC[pi * M + h * MG + tt] = v; };
+	auto ld_xc = [&](int pi, int h, int tt, uint32_t) { return XC[pi * MP + xcp(h, tt)]; };
+	auto st_xc = [&](int pi, int h, int tt, uint32_t v) { XC[pi * MP + xcp(h, tt)] = v; };
 
 	// W: local levels C .. LM-1 of sub-block (pi, sb), pointwise, inverse
 	auto wphase = [&](int pi, int sb, int mode) {
@@ -808,24 +823,24 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 				{
 					const uint32_t q = qv(pi), qi = qiv(pi);
 #pragma unroll
-					for (int k = 0; k < R; ++k) u[pi][k] = XC[pi * M + (hbase + k * stride) * MG + tt];
+					for (int k = 0; k < R; ++k) u[pi][k] = XC[pi * MP + xcp(hbase + k * stride, tt)];
 					group_inv<R>(u[pi], XRT + (pi * 2 + 1) * G, [&](int t, int kk) { return (1 << t) + kk; }, q, qi,
 					             true, a.omega[pi], a.k1[pi], a.sc[pi]);
 				}
 #pragma unroll
 				for (int k = 0; k < R; ++k)
 				{
-					const int pos = (hbase + k * stride) * MG + tt;
+					const int pos = xcp(hbase + k * stride, tt);
 					uint32_t w0, w1;
 					if constexpr (NP == 3)
 					{
 						uint32_t w2;
 						garner3(u[0][k], u[1][k], u[2][k], a, narrow, w0, w1, w2);
-						XC[2 * M + pos] = w2;
+						XC[2 * MP + pos] = w2;
 					}
 					else garner2(u[0][k], u[1][k], a, w0, w1);
 					XC[pos] = w0;
-					XC[M + pos] = w1;
+					XC[MP + pos] = w1;
 				}
 			}
 		}
@@ -834,17 +849,17 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		for (int c = tid; c < ncl; c += nt)
 		{
 			const int h = c / runc, j = c - h * runc;
-			const int base = h * MG + j * csz;
+			const int base = h * MG + j * csz, xb = xcp(h, j * csz);
 			int64_t f;
-			if (narrow && csz == 8) f = norm1_chunk64<8>(XC + base, XC + M + base, XD + base, mult, b, b_inv, b_s, err);
+			if (narrow && csz == 8) f = norm1_chunk64<8>(XC + xb, XC + MP + xb, XD + base, mult, b, b_inv, b_s, err);
 			else if (narrow && csz == 16)
-				f = norm1_chunk64<16>(XC + base, XC + M + base, XD + base, mult, b, b_inv, b_s, err);
+				f = norm1_chunk64<16>(XC + xb, XC + MP + xb, XD + base, mult, b, b_inv, b_s, err);
 			else if (narrow)
 			{
 				int64_t acc = 0;
 				for (int i = 0; i < csz; ++i)
 				{
-					acc += load64(XC + base, M, i) * (int64_t)mult;
+					acc += load64(XC + xb, MP, i) * (int64_t)mult;
 					XD[base + i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
 				}
 				f = acc;
@@ -855,7 +870,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 				if constexpr (NP == 3)
 					for (int i = 0; i < csz; ++i)
 					{
-						acc += load96(XC + base, M, i) * (i128)mult;
+						acc += load96(XC + xb, MP, i) * (i128)mult;
 						XD[base + i] = reduce_b<i128>(acc, b, b_inv, b_s, err);
 					}
 				f = (int64_t)acc;

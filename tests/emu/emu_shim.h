@@ -27,6 +27,7 @@ using std::max;
 using std::min;
 struct alignas(8) uint2 { uint32_t x, y; };
 struct alignas(16) uint4 { uint32_t x, y, z, w; };
+struct alignas(16) int4 { int32_t x, y, z, w; };
 inline long long __double2ll_rd(double x) { return (long long)std::floor(x); }
 inline double __ll2double_rn(long long x) { return (double)x; }
 inline uint32_t __umulhi(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) >> 32); }
@@ -37,5 +38,6 @@ void __syncthreads();
 void emu_syncwarp();
 inline uint2 make_uint2(uint32_t x, uint32_t y) { return uint2{ x, y }; }
 inline uint4 make_uint4(uint32_t x, uint32_t y, uint32_t z, uint32_t w) { return uint4{ x, y, z, w }; }
+inline int4 make_int4(int32_t x, int32_t y, int32_t z, int32_t w) { return int4{ x, y, z, w }; }
 uint32_t *emu_smem();
 unsigned long long emu_timer_ns();

@@ -35,8 +35,9 @@ BUILD = os.path.join(EMU, "_build")
 CSRC = os.path.join(ROOT, "ctwin_gb300", "csrc")
 # (lg, primes, lm) shapes compiled: 2^16 on 64 CTAs of 1024 (the single-test
 # default), 2^16 on 32 CTAs of 2048 with three primes, 2^17 on 32 CTAs of 4096,
-# 2^18 on 128 CTAs of 2048 with three primes (the 2^18 default)
-SHAPES = [(6, 2, 10), (5, 3, 11), (5, 2, 12), (7, 3, 11)]
+# 2^18 on 128 CTAs of 2048 with three primes (the 2^18 default), 2^17 on 64 CTAs
+# of 2048 (the 2^17 default)
+SHAPES = [(6, 2, 10), (5, 3, 11), (5, 2, 12), (7, 3, 11), (6, 2, 11)]
 MARK = "size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np)"
 
 
@@ -88,6 +89,7 @@ def grid_emu():
     (16, 10, 2, 8, 1330358, 64, 3),      # the same with CSIZE 8 (the unrolled carry chain)
     (16, 11, 3, 32, 2000000003, 64, 2),  # three primes, b near 2^31 (128-bit carries)
     (17, 12, 2, 8, 1330358, 32, 2),      # 4096-coefficient CTAs
+    (17, 11, 2, 16, 1330358, 64, 2),     # the 2^17 default: 64 CTAs of 2048, runs of 32 columns
     (18, 11, 3, 16, 1330358, 32, 3),     # 128 CTAs
 ])
 def test_grid_kernel_emulated_bit_exact(grid_emu, ln, lm, primes, csize, b, threads, mult):
