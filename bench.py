@@ -78,9 +78,9 @@ def workload(rank: int):
     return b, E, i0, B_GL, words
 
 
-TRAFFIC_PER_LAUNCH = 1.50e6     # ncu dram read+write bytes of one 651-squaring launch at 2^16 (64-CTA grid)
+TRAFFIC_PER_LAUNCH = 2.58e6     # ncu dram read+write bytes of one 651-squaring launch at 2^16 (64-CTA grid)
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one 651-squaring launch of the "
-                  "default split (profiles/prp_kernel_d65536_full.md)")
+                  "default split (profiles/prp_kernel_grid2_d65536_full.md)")
 
 
 def hbm_line(traffic: float, seconds: float) -> dict:
