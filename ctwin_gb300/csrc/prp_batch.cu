@@ -46,8 +46,10 @@ __global__ void __launch_bounds__(BatchBounds<NP>::threads, OCC)
 {
 	extern __shared__ __align__(16) uint32_t sm[];
 	// class and index of the current item, written into every CTA by rank 0 of
-	// the cluster, after the words the launch bodies use
+	// the cluster, after the words the launch bodies use; then the class's
+	// launch arguments, copied into shared memory for the item's bodies
 	int *item = reinterpret_cast<int *>(sm + item_off);
+	PrpKernelArgs *sa = reinterpret_cast<PrpKernelArgs *>(sm + item_off + 4);
 	cg::cluster_group cl = cg::this_cluster();
 	const int rank = (int)cl.block_rank();
 	for (;;)
@@ -77,15 +79,21 @@ __global__ void __launch_bounds__(BatchBounds<NP>::threads, OCC)
 		const int c = item[0], idx = item[1];
 		if (c < 0) break;
 		const PrpBatchClass &C = cls[c];
+		{
+			const uint32_t *src = reinterpret_cast<const uint32_t *>(&C.a);
+			uint32_t *dst = reinterpret_cast<uint32_t *>(sa);
+			for (int i = threadIdx.x; i < (int)(sizeof(PrpKernelArgs) / 4); i += blockDim.x) dst[i] = src[i];
+		}
+		__syncthreads();
 		const int lg = C.lg;
 		const int sub = rank >> lg, g = rank & ((1 << lg) - 1);
 		const int lane = idx * (BATCH_CLUSTER >> lg) + sub;
 		switch (lg)
 		{
-		case 0: batch_item<NP, 0>(C.a, sm, lane, 0, 0); break;
-		case 1: batch_item<NP, 1>(C.a, sm, lane, g, sub << 1); break;
-		case 2: batch_item<NP, 2>(C.a, sm, lane, g, sub << 2); break;
-		default: batch_item<NP, 3>(C.a, sm, lane, g, 0); break;
+		case 0: batch_item<NP, 0>(*sa, sm, lane, 0, 0); break;
+		case 1: batch_item<NP, 1>(*sa, sm, lane, g, sub << 1); break;
+		case 2: batch_item<NP, 2>(*sa, sm, lane, g, sub << 2); break;
+		default: batch_item<NP, 3>(*sa, sm, lane, g, 0); break;
 		}
 		cl.sync();                                   // every CTA done before the next item is posted
 	}
@@ -99,7 +107,7 @@ size_t batch_body_smem()
 	for (int lg = 0; lg <= 3; ++lg) m = std::max(m, prp_smem_bytes(12, lg, 0, NP));
 	return NP == 3 ? m - prp_shoup_words(12, 3) * 4 : m;    // the three-prime build reads its Shoup roots from L2
 }
-template <int NP> size_t batch_smem() { return batch_body_smem<NP>() + 16; }
+template <int NP> size_t batch_smem() { return batch_body_smem<NP>() + 16 + (sizeof(PrpKernelArgs) + 15) / 16 * 16; }
 
 template <int NP, int OCC>
 cudaError_t batch_launch_t(const PrpBatchClass *d_cls, int ncls, int total_items, unsigned *d_heads,
