@@ -83,18 +83,32 @@ __device__ __forceinline__ long long ld_l2_ll(const long long *p)
 #endif
 }
 
+// Release increment (red.release.gpu): the CTA's writes, ordered before it by
+// the __syncthreads of grid_arrive, become visible to a CTA whose acquire load
+// reads the new count.
+__device__ __forceinline__ void grid_add_release(unsigned *p)
+{
+#if defined(CTW_EMU)
+	__atomic_fetch_add(p, 1u, __ATOMIC_RELEASE);
+#elif defined(__CUDA_ARCH__)
+	asm volatile("red.release.gpu.global.add.u32 [%0], 1;" :: "l"(p) : "memory");
+#else
+	++*p;
+#endif
+}
+
 // Barrier k of the launch over the G CTAs of one lane, in two halves: arrive
 // (after every thread's global writes), then wait until k * G arrivals.  A CTA
 // whose wait ran out (*dead) no longer waits.  The same pair on a per-CTA count
-// (target k) waits for the k-th publication of one other CTA.
+// (target k) waits for the k-th publication of one other CTA.  Thread 0's
+// release increment and acquire load pair up across CTAs, the __syncthreads on
+// either side carry the order to the other threads of each CTA (the PTX
+// memory model's causality order is transitive through bar.sync), so neither
+// half needs a full fence.
 __device__ __forceinline__ void grid_arrive(unsigned *cnt)
 {
 	__syncthreads();
-	if (threadIdx.x == 0)
-	{
-		__threadfence();
-		atomicAdd(cnt, 1u);
-	}
+	if (threadIdx.x == 0) grid_add_release(cnt);
 }
 __device__ __forceinline__ void grid_wait(unsigned *cnt, unsigned target, uint32_t &err, int *dead)
 {
@@ -111,7 +125,6 @@ __device__ __forceinline__ void grid_wait(unsigned *cnt, unsigned target, uint32
 					break;
 				}
 		}
-		__threadfence();
 	}
 	__syncthreads();
 }
@@ -466,12 +479,14 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 //   Y1  gather of the columns fused with the first inverse cross pass
 //   Y2  the last inverse cross pass (with the final scale) fused with Garner,
 //       one item per column group holding every prime
-//   N   normalize1 with the chunk loaded ahead of its carry chain, then the
-//       run-end carries are published by one otherwise idle thread while the
-//       others carry into the chunks that need no remote carry.
+//   N   normalize1 with the chunk loaded ahead of its carry chain; each CTA
+//       also gathers and transforms the last chunk of its left neighbour's
+//       runs and takes that chunk's carry itself, so the carries need no
+//       exchange between CTAs and no third wait.
 // Shared memory: XC [NP][G][MG] column runs (natural order, Garner words in
 // place), XR [NP][M] row block (sub-block swizzle sbx), XD [M] digits at rest
-// (column-run order), chunk and run-end carries, cross and local roots.
+// (column-run order), chunk carries and the left neighbour's run-end carries,
+// cross and local roots, XN the neighbour's last chunk of every run.
 // ---------------------------------------------------------------------------
 
 // word of position p (0..255) inside a sub-block: 4-word groups XOR-permuted
@@ -525,8 +540,8 @@ __host__ __device__ __forceinline__ size_t grid2_words(int lg, int lm, int np)
 {
 	const size_t M = (size_t)1 << lm, G = (size_t)1 << lg;
 	// XC (with a 16-word pad every 8 rows), XR, XD, chunk carries (M/8 int64),
-	// run-end carries (G int64), cross roots, TF + TI (pairs)
-	return 2 * np * M + np * (G / 8) * 16 + M + M / 4 + 2 * G + 2 * np * G + 4 * np * M;
+	// the left neighbour's carries (G int64), cross roots, TF + TI (pairs), XN, XDN
+	return 2 * np * M + np * (G / 8) * 16 + M + M / 4 + 2 * G + 2 * np * G + 4 * np * M + np * M + M;
 }
 
 // Normalize1 of one chunk of CSZ Garner words (64-bit, two primes or narrow
@@ -585,6 +600,9 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	uint32_t *XRT = reinterpret_cast<uint32_t *>(xch + G);      // [NP][2][G]
 	uint32_t *TF = XRT + NP * 2 * G;                            // [NP][M][2] Shoup pairs
 	uint32_t *TI = TF + NP * 2 * M;
+	uint32_t *XN = TI + NP * 2 * M;                             // [NP][G][MG] the left neighbour's last chunk
+	int32_t *XDN = reinterpret_cast<int32_t *>(XN + NP * M);   // [G][MG] its digits (discarded)
+	const int gl = (g + G - 1) % G;                             // the left neighbour in natural order
 	if (tid == 0) dead = 0;
 
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
@@ -600,10 +618,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 
 	uint32_t *gx = ga.gx + (size_t)lane * G * 3 * M;
 	uint32_t *gr = ga.gr + (size_t)lane * G * 3 * M;
-	long long *gc = ga.gc + (size_t)lane * G * G;
 	unsigned *bar = ga.bar + (size_t)lane * GRID_BAR_WORDS;
-	unsigned *cpub = bar + 32;
-	unsigned nbar = 0, ncar = 0;
+	unsigned nbar = 0;
 	auto gsync = [&]() {
 		++nbar;
 		grid_arrive(bar);
@@ -621,15 +637,17 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	};
 
 	// cross pass P over XC (or from the digits / to L2), direction dir
-	auto xpass = [&](auto PC, int dir, auto load, auto store) {
+	// columns tt < MG are this CTA's (XC), MG <= tt < ncols the left neighbour's
+	// last chunk (XN)
+	auto xpass = [&](auto PC, int dir, int ncols, auto load, auto store) {
 		constexpr int P = decltype(PC)::value;
 		constexpr int R = XPass<LG, P>::R, r = Log2<R>::v, l0 = XPass<LG, P>::l0, NGR = G >> r;
 		constexpr int lsh = LG - l0 - r, stride = 1 << lsh;
-		for (int it = tid; it < NP * NGR * MG; it += nt)
+		for (int it = tid; it < NP * NGR * ncols; it += nt)
 		{
-			const int pi = it / (NGR * MG);
-			const int rem = it - pi * NGR * MG;
-			const int gam = rem / MG, tt = rem - gam * MG;
+			const int pi = it / (NGR * ncols);
+			const int rem = it - pi * NGR * ncols;
+			const int gam = rem / ncols, tt = rem - gam * ncols;
 			const int jblk = gam >> lsh, i = gam & (stride - 1);
 			const int hbase = (jblk << (LG - l0)) + i;
 			const uint32_t q = qv(pi), qi = qiv(pi);
@@ -644,8 +662,11 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 			for (int k = 0; k < R; ++k) store(pi, hbase + k * stride, tt, u[k]);
 		}
 	};
-	auto ld_xc = [&](int pi, int h, int tt, uint32_t) { return XC[pi * MP + xcp(h, tt)]; };
-	auto st_xc = [&](int pi, int h, int tt, uint32_t v) { XC[pi * MP + xcp(h, tt)] = v; };
+	auto xw = [&](int pi, int h, int tt) -> uint32_t & {
+		return tt < MG ? XC[pi * MP + xcp(h, tt)] : XN[pi * M + h * MG + (tt - MG)];
+	};
+	auto ld_xc = [&](int pi, int h, int tt, uint32_t) { return xw(pi, h, tt); };
+	auto st_xc = [&](int pi, int h, int tt, uint32_t v) { xw(pi, h, tt) = v; };
 
 	// W: local levels C .. LM-1 of sub-block (pi, sb), pointwise, inverse
 	auto wphase = [&](int pi, int sb, int mode) {
@@ -740,16 +761,16 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	auto transform_and_normalize = [&](int mode, int mult) {
 		__syncthreads();
 		// X1: digits -> residues, first forward cross pass
-		xpass(std::integral_constant<int, 0>{}, 0,
+		xpass(std::integral_constant<int, 0>{}, 0, MG,
 		      [&](int, int h, int tt, uint32_t q) { return modq_i32(XD[h * MG + tt], q); }, st_xc);
 		__syncthreads();
 		if constexpr (NPASS == 3)
 		{
-			xpass(std::integral_constant<int, 1>{}, 0, ld_xc, st_xc);
+			xpass(std::integral_constant<int, 1>{}, 0, MG, ld_xc, st_xc);
 			__syncthreads();
 		}
 		// X3: last forward cross pass, columns published to L2
-		xpass(std::integral_constant<int, PL>{}, 0, ld_xc, [&](int pi, int h, int tt, uint32_t v) {
+		xpass(std::integral_constant<int, PL>{}, 0, MG, ld_xc, [&](int pi, int h, int tt, uint32_t v) {
 			st_l2_u1(gx + (size_t)g * 3 * M + pi * M + h * MG + tt, v);
 		});
 		gsync();
@@ -799,23 +820,55 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 				st_l2_u2(gr + (size_t)g * 3 * M + pi * M + j * 256 + m0, make_uint2(v0[j], v1[j]));
 		}
 		gsync();
-		// Y1: gather the columns, first inverse cross pass
-		xpass(std::integral_constant<int, PL>{}, 1, [&](int pi, int h, int tt, uint32_t) {
-			return ld_l2_u1(gr + (size_t)h * 3 * M + pi * M + g * MG + tt);
-		}, st_xc);
+		// Y1: gather the columns — this CTA's and the left neighbour's last chunk —
+		// in pairs, first inverse cross pass
+		const int ncols = MG + csz;
+		{
+			constexpr int R = XPass<LG, PL>::R, r = Log2<R>::v, l0 = XPass<LG, PL>::l0, NGR = G >> r;
+			constexpr int lsh = LG - l0 - r, stride = 1 << lsh;
+			const int ncp = ncols / 2;
+			for (int it = tid; it < NP * NGR * ncp; it += nt)
+			{
+				const int pi = it / (NGR * ncp);
+				const int rem = it - pi * NGR * ncp;
+				const int gam = rem / ncp, tt = 2 * (rem - gam * ncp);
+				const int jblk = gam >> lsh, i = gam & (stride - 1);
+				const int hbase = (jblk << (LG - l0)) + i;
+				const uint32_t q = qv(pi), qi = qiv(pi);
+				const uint32_t *tw = XRT + (pi * 2 + 1) * G;
+				auto idx = [&](int t, int kk) { return (1 << (l0 + t)) + (jblk << t) + kk; };
+				const uint32_t *src = gr + pi * M + (tt < MG ? g * MG + tt : gl * MG + (MG - csz) + (tt - MG));
+				uint32_t u0[R], u1[R];
+#pragma unroll
+				for (int k = 0; k < R; ++k)
+				{
+					const uint2 w = ld_l2_u2(src + (size_t)(hbase + k * stride) * 3 * M);
+					u0[k] = w.x;
+					u1[k] = w.y;
+				}
+				group_inv<R>(u0, tw, idx, q, qi, l0 == 0, a.omega[pi], a.k1[pi], a.sc[pi]);
+				group_inv<R>(u1, tw, idx, q, qi, l0 == 0, a.omega[pi], a.k1[pi], a.sc[pi]);
+#pragma unroll
+				for (int k = 0; k < R; ++k)
+				{
+					xw(pi, hbase + k * stride, tt) = u0[k];
+					xw(pi, hbase + k * stride, tt + 1) = u1[k];
+				}
+			}
+		}
 		__syncthreads();
 		if constexpr (NPASS == 3)
 		{
-			xpass(std::integral_constant<int, 1>{}, 1, ld_xc, st_xc);
+			xpass(std::integral_constant<int, 1>{}, 1, ncols, ld_xc, st_xc);
 			__syncthreads();
 		}
 		// Y2: last inverse cross pass (levels of pass 0, with the final scale) and
 		// Garner, one item per (column, row group) holding every prime
 		{
 			constexpr int R = XPass<LG, 0>::R, r = Log2<R>::v, NGR = G >> r, lsh = LG - r, stride = 1 << lsh;
-			for (int it = tid; it < NGR * MG; it += nt)
+			for (int it = tid; it < NGR * ncols; it += nt)
 			{
-				const int gam = it / MG, tt = it - gam * MG;
+				const int gam = it / ncols, tt = it - gam * ncols;
 				const int hbase = gam;                          // pass 0: jblk = 0, i = gam
 				uint32_t u[NP][R];
 #pragma unroll
@@ -823,68 +876,93 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 				{
 					const uint32_t q = qv(pi), qi = qiv(pi);
 #pragma unroll
-					for (int k = 0; k < R; ++k) u[pi][k] = XC[pi * MP + xcp(hbase + k * stride, tt)];
+					for (int k = 0; k < R; ++k) u[pi][k] = xw(pi, hbase + k * stride, tt);
 					group_inv<R>(u[pi], XRT + (pi * 2 + 1) * G, [&](int t, int kk) { return (1 << t) + kk; }, q, qi,
 					             true, a.omega[pi], a.k1[pi], a.sc[pi]);
 				}
 #pragma unroll
 				for (int k = 0; k < R; ++k)
 				{
-					const int pos = xcp(hbase + k * stride, tt);
+					const int h = hbase + k * stride;
 					uint32_t w0, w1;
 					if constexpr (NP == 3)
 					{
 						uint32_t w2;
 						garner3(u[0][k], u[1][k], u[2][k], a, narrow, w0, w1, w2);
-						XC[2 * MP + pos] = w2;
+						xw(2, h, tt) = w2;
 					}
 					else garner2(u[0][k], u[1][k], a, w0, w1);
-					XC[pos] = w0;
-					XC[MP + pos] = w1;
+					xw(0, h, tt) = w0;
+					xw(1, h, tt) = w1;
 				}
 			}
 		}
 		__syncthreads();
-		// N: normalize1 over the runs; the last chunk of run h keeps its carry in xch
-		for (int c = tid; c < ncl; c += nt)
-		{
-			const int h = c / runc, j = c - h * runc;
-			const int base = h * MG + j * csz, xb = xcp(h, j * csz);
-			int64_t f;
-			if (narrow && csz == 8) f = norm1_chunk64<8>(XC + xb, XC + MP + xb, XD + base, mult, b, b_inv, b_s, err);
-			else if (narrow && csz == 16)
-				f = norm1_chunk64<16>(XC + xb, XC + MP + xb, XD + base, mult, b, b_inv, b_s, err);
-			else if (narrow)
+		// N: normalize1 over this CTA's chunks and, per row, over the left
+		// neighbour's last chunk, whose carry is the run-end carry that
+		// neighbour computes for itself (normalize1 of a chunk starts from zero,
+		// so it needs that chunk's Garner words only)
+		auto norm1 = [&](const uint32_t *W, int stride_pl, int32_t *XDo) -> int64_t {
+			if (narrow && csz == 8) return norm1_chunk64<8>(W, W + stride_pl, XDo, mult, b, b_inv, b_s, err);
+			if (narrow && csz == 16) return norm1_chunk64<16>(W, W + stride_pl, XDo, mult, b, b_inv, b_s, err);
+			if (narrow)
 			{
 				int64_t acc = 0;
 				for (int i = 0; i < csz; ++i)
 				{
-					acc += load64(XC + xb, MP, i) * (int64_t)mult;
-					XD[base + i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+					acc += load64(W, stride_pl, i) * (int64_t)mult;
+					XDo[i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
 				}
-				f = acc;
+				return acc;
+			}
+			i128 acc = 0;
+			if constexpr (NP == 3)
+			{
+				for (int i = 0; i < csz; ++i)
+				{
+					acc += load96(W, stride_pl, i) * (i128)mult;
+					XDo[i] = reduce_b<i128>(acc, b, b_inv, b_s, err);
+				}
+			}
+			int64_t carry = static_cast<int64_t>(acc);
+			if (static_cast<i128>(carry) != acc) err |= ST_DIGIT_RANGE;
+			return carry;
+		};
+		for (int c = tid; c < ncl + G; c += nt)
+		{
+			if (c < ncl)
+			{
+				const int h = c / runc, j = c - h * runc;
+				fch[c] = norm1(XC + xcp(h, j * csz), MP, XD + h * MG + j * csz);
 			}
 			else
 			{
-				i128 acc = 0;
-				if constexpr (NP == 3)
-					for (int i = 0; i < csz; ++i)
-					{
-						acc += load96(XC + xb, MP, i) * (i128)mult;
-						XD[base + i] = reduce_b<i128>(acc, b, b_inv, b_s, err);
-					}
-				f = (int64_t)acc;
-				if ((i128)f != acc) err |= ST_DIGIT_RANGE;
+				const int h = c - ncl;
+				xch[h] = norm1(XN + h * MG, M, XDN + h * MG);
 			}
-			fch[c] = f;
-			if (j == runc - 1) xch[h] = f;
 		}
 		__syncthreads();
-		// normalize2 (as prp_kernel_grid): the run-end carries are published by the
-		// last thread (fence and count) while threads 0 .. ncl - G - 1 carry into the
-		// chunks j > 0, which need no remote carry
-		for (int h = tid; h < G; h += nt) gc[(size_t)g * G + h] = xch[h];
-		auto carry_in = [&](int h, int j, int64_t acc) {
+		// normalize2: chunk j of run (h, g) takes the carry of the chunk before it
+		// in natural order — for j = 0 the left neighbour's run-end carry, from
+		// the row before for CTA 0, whose run 0 takes -f and run G/2 +f of the
+		// last run (X^D = X^{D/2} - 1)
+		for (int c = tid; c < ncl; c += nt)
+		{
+			const int h = c / runc, j = c - h * runc;
+			int64_t acc;
+			if (j > 0) acc = fch[c - 1];
+			else if (g > 0) acc = xch[h];
+			else
+			{
+				const int64_t last = xch[G - 1];
+				if (h == 0) acc = -last;
+				else
+				{
+					acc = xch[h - 1];
+					if (h == G / 2) acc += last;
+				}
+			}
+			// a chunk carry plus digits: 64-bit arithmetic is exact
 			int32_t *Xh = XD + h * MG + j * csz;
 			int i = 0;
 			bool done = false;
@@ -900,37 +978,6 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 				if (s != (int32_t)s) err |= ST_DIGIT_RANGE;
 				Xh[csz - 1] = (int32_t)s;
 			}
-		};
-		++ncar;
-		__syncthreads();
-		if (tid == nt - 1)
-		{
-			__threadfence();
-			atomicAdd(cpub + g, 1u);
-		}
-		const int nin = ncl - G;                                 // chunks j > 0
-		const int nw = nin < nt - 1 ? nin : nt - 1;              // threads that carry (not the publisher)
-		for (int k = tid; k < nin && tid < nw; k += nw)
-		{
-			const int h = k / (runc - 1), j = k - h * (runc - 1) + 1;
-			carry_in(h, j, fch[h * runc + j - 1]);
-		}
-		grid_wait(cpub + (g + G - 1) % G, ncar, err, &dead);
-		for (int h = tid; h < G; h += nt)
-		{
-			int64_t acc;
-			if (g > 0) acc = ld_l2_ll(gc + (size_t)(g - 1) * G + h);
-			else
-			{
-				const int64_t last = ld_l2_ll(gc + (size_t)(G - 1) * G + (G - 1));
-				if (h == 0) acc = -last;
-				else
-				{
-					acc = ld_l2_ll(gc + (size_t)(G - 1) * G + (h - 1));
-					if (h == G / 2) acc += last;
-				}
-			}
-			carry_in(h, 0, acc);
 		}
 	};
 
