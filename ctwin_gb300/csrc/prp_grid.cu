@@ -618,8 +618,14 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 
 	uint32_t *gx = ga.gx + (size_t)lane * G * 3 * M;
 	uint32_t *gr = ga.gr + (size_t)lane * G * 3 * M;
+	long long *gc = ga.gc + (size_t)lane * G * G;                // [G][G]: run-end carries of CTA c at c*G
 	unsigned *bar = ga.bar + (size_t)lane * GRID_BAR_WORDS;
-	unsigned nbar = 0;
+	unsigned *cpub = bar + 32;                                  // [G] carry publications of each CTA
+	unsigned nbar = 0, ncar = 0;
+	// the left neighbour's last chunk is recomputed here when it is at most half
+	// a run; otherwise (runs of 16 words with CSIZE 16 at degree 2^18) the
+	// neighbour publishes its run-end carries and this CTA waits for them
+	const bool nbr = 2 * csz <= MG;
 	auto gsync = [&]() {
 		++nbar;
 		grid_arrive(bar);
@@ -822,7 +828,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		gsync();
 		// Y1: gather the columns — this CTA's and the left neighbour's last chunk —
 		// in pairs, first inverse cross pass
-		const int ncols = MG + csz;
+		const int ncols = nbr ? MG + csz : MG;
 		{
 			constexpr int R = XPass<LG, PL>::R, r = Log2<R>::v, l0 = XPass<LG, PL>::l0, NGR = G >> r;
 			constexpr int lsh = LG - l0 - r, stride = 1 << lsh;
@@ -928,12 +934,14 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 			if (static_cast<i128>(carry) != acc) err |= ST_DIGIT_RANGE;
 			return carry;
 		};
-		for (int c = tid; c < ncl + G; c += nt)
+		for (int c = tid; c < ncl + (nbr ? G : 0); c += nt)
 		{
 			if (c < ncl)
 			{
 				const int h = c / runc, j = c - h * runc;
-				fch[c] = norm1(XC + xcp(h, j * csz), MP, XD + h * MG + j * csz);
+				const int64_t f = norm1(XC + xcp(h, j * csz), MP, XD + h * MG + j * csz);
+				fch[c] = f;
+				if (!nbr && j == runc - 1) xch[h] = f;
 			}
 			else
 			{
@@ -945,24 +953,9 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		// normalize2: chunk j of run (h, g) takes the carry of the chunk before it
 		// in natural order — for j = 0 the left neighbour's run-end carry, from
 		// the row before for CTA 0, whose run 0 takes -f and run G/2 +f of the
-		// last run (X^D = X^{D/2} - 1)
-		for (int c = tid; c < ncl; c += nt)
-		{
-			const int h = c / runc, j = c - h * runc;
-			int64_t acc;
-			if (j > 0) acc = fch[c - 1];
-			else if (g > 0) acc = xch[h];
-			else
-			{
-				const int64_t last = xch[G - 1];
-				if (h == 0) acc = -last;
-				else
-				{
-					acc = xch[h - 1];
-					if (h == G / 2) acc += last;
-				}
-			}
-			// a chunk carry plus digits: 64-bit arithmetic is exact
+		// last run (X^D = X^{D/2} - 1).  A chunk carry plus digits: 64-bit
+		// arithmetic is exact.
+		auto carry_in = [&](int h, int j, int64_t acc) {
 			int32_t *Xh = XD + h * MG + j * csz;
 			int i = 0;
 			bool done = false;
@@ -978,7 +971,39 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 				if (s != (int32_t)s) err |= ST_DIGIT_RANGE;
 				Xh[csz - 1] = (int32_t)s;
 			}
+		};
+		auto first_carry = [&](int h, auto run_end) -> int64_t {
+			if (g > 0) return run_end(h);
+			const int64_t last = run_end(G - 1);
+			if (h == 0) return -last;
+			return h == G / 2 ? run_end(h - 1) + last : run_end(h - 1);
+		};
+		if (nbr)
+		{
+			for (int c = tid; c < ncl; c += nt)
+			{
+				const int h = c / runc, j = c - h * runc;
+				carry_in(h, j, j > 0 ? fch[c - 1] : first_carry(h, [&](int hh) { return xch[hh]; }));
+			}
+			return;
 		}
+		// the run-end carries are published (the last thread releases the count)
+		// while threads 0 .. ncl - G - 1 carry into the chunks j > 0, which need
+		// no remote carry; then the chunks j = 0 wait for the left neighbour's
+		for (int h = tid; h < G; h += nt) gc[(size_t)g * G + h] = xch[h];
+		++ncar;
+		__syncthreads();
+		if (tid == nt - 1) grid_add_release(cpub + g);
+		const int nin = ncl - G;                                 // chunks j > 0
+		const int nw = nin < nt - 1 ? nin : nt - 1;              // threads that carry (not the publisher)
+		for (int k = tid; k < nin && tid < nw; k += nw)
+		{
+			const int h = k / (runc - 1), j = k - h * (runc - 1) + 1;
+			carry_in(h, j, fch[h * runc + j - 1]);
+		}
+		grid_wait(cpub + gl, ncar, err, &dead);
+		for (int h = tid; h < G; h += nt)
+			carry_in(h, 0, first_carry(h, [&](int hh) { return (int64_t)ld_l2_ll(gc + (size_t)gl * G + hh); }));
 	};
 
 	if (a.op == OP_MUL)
