@@ -970,6 +970,8 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
+        "step_ms": {"min": min(times), "median": statistics.median(times), "max": max(times),
+                    "first": times[0], "last": times[-1]},
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": single_config(world),
         "launch": {"ctas_per_candidate": geo["ctas_per_lane"], "threads_per_cta": geo["threads"],

@@ -351,16 +351,22 @@ int launch(ctw_prp *h, const PrpKernelArgs &a)
 	cudaError_t e;
 	if (h->grid)
 	{
-		// barrier counters start at zero in every launch
+		// barrier counters and the published columns and rows (whose words carry
+		// the parity of their publication in the launch) start at zero
+		const size_t xw = (size_t)h->lanes * 3 * h->D;
 		e = cudaMemsetAsync(h->d_bar, 0, (size_t)h->lanes * GRID_BAR_WORDS * sizeof(unsigned), h->stream);
+		if (e == cudaSuccess) e = cudaMemsetAsync(h->d_gx, 0, xw * 4, h->stream);
+		if (e == cudaSuccess) e = cudaMemsetAsync(h->d_gr, 0, xw * 4, h->stream);
 		// testing only (ctw_prp_test_unreachable_barrier): word 0 of every lane
-		// starts at 0x80808080, 2^31 arrivals short of any target this launch sets
+		// starts at 0x80808080, 2^31 arrivals short of any target this launch
+		// sets, and CTA 0 skips its first publication of columns
 		for (int l = 0; e == cudaSuccess && h->bar_unreachable && l < h->lanes; ++l)
 			e = cudaMemsetAsync(h->d_bar + (size_t)l * GRID_BAR_WORDS, 0x80, sizeof(unsigned), h->stream);
+		const int mute = h->bar_unreachable ? 1 : 0;
 		h->bar_unreachable = 0;
 		if (e == cudaSuccess)
 		{
-			const PrpGridArgs ga{ h->d_gx, h->d_gr, h->d_gc, h->d_bar, h->d_xr };
+			const PrpGridArgs ga{ h->d_gx, h->d_gr, h->d_gc, h->d_bar, h->d_xr, mute };
 			e = prp_grid_launch(a, ga, h->lg, h->lanes, h->stream);
 		}
 	}
@@ -391,7 +397,9 @@ int check_status(ctw_prp *h)
 	{
 		cudaMemsetAsync(h->d_status, 0, sizeof(uint32_t), h->stream);
 		if (st & ST_GRID_WAIT)
-			return fail(CTW_E_COMPUTE, "grid kernel: a barrier wait ran out, the launch's results are void (status 0x%x)", st);
+			return fail(CTW_E_COMPUTE,
+			            "grid kernel: a wait for other CTAs (grid barrier or published words) ran out, the launch's "
+			            "results are void (status 0x%x)", st);
 		return fail(CTW_E_COMPUTE, "device arithmetic range check failed (status 0x%x)", st);
 	}
 	return CTW_OK;

@@ -468,21 +468,27 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 // coefficients): the same squaring as prp_kernel_grid (registers equal), with
 // fewer CTA-wide steps per squaring:
 //   X1  digits -> residues fused into the first forward cross pass
-//   X3  the last forward cross pass stores straight to L2 (no shared copy)
-//   A   gather of row block g fused with local levels 0 .. C-1 (radix 2^C,
-//       C = LM - 8) across the CTA
+//   X3  the last forward cross pass stores straight to L2 (no shared copy),
+//       each word with its publication's parity bit
+//   A   gather of row block g, polling each word for the parity of this
+//       publication (no grid barrier), fused with local levels 0 .. C-1
+//       (radix 2^C, C = LM - 8) across the CTA
 //   W   local levels C .. LM-1, the pointwise step and their inverse on
 //       sub-blocks of 256 coefficients, one warp each: three register passes
 //       (radix 8, 8, 4) with warp-synchronous exchanges through shared memory;
 //       local roots as Shoup pairs (one high and two low products each)
 //   A'  inverse local levels C-1 .. 0 fused with the publication of the row
-//   Y1  gather of the columns fused with the first inverse cross pass
+//   Y1  gather of the columns (polling, as A) fused with the first inverse
+//       cross pass
 //   Y2  the last inverse cross pass (with the final scale) fused with Garner,
 //       one item per column group holding every prime
 //   N   normalize1 with the chunk loaded ahead of its carry chain; each CTA
 //       also gathers and transforms the last chunk of its left neighbour's
 //       runs and takes that chunk's carry itself, so the carries need no
-//       exchange between CTAs and no third wait.
+//       exchange between CTAs (when that chunk is at most half a run; else
+//       the neighbour publishes its run-end carries).
+// A squaring has no grid barrier: a multiply keeps one between the transform
+// of y and that of x.
 // Shared memory: XC [NP][G][MG] column runs (natural order, Garner words in
 // place), XR [NP][M] row block (sub-block swizzle sbx), XD [M] digits at rest
 // (column-run order), chunk carries and the left neighbour's run-end carries,
@@ -526,6 +532,105 @@ __device__ __forceinline__ void st_l2_u1(uint32_t *p, uint32_t v)
 #else
 	*p = v;
 #endif
+}
+
+// Published words (the columns of X3, the rows of A'): a residue below 2^31
+// (in [0, 2q)) with bit 31 holding the parity of its publication within the
+// launch.  The buffers are zeroed before every launch and publication k = 1,
+// 2, ... of a buffer sets parity k & 1; every publication rewrites every word
+// of its buffer for the launch's primes, so a word that shows the expected
+// parity is this publication's, never the one before.  A reader therefore
+// needs no grid barrier: it polls the words it gathers.  Stores and loads are
+// relaxed at GPU scope, so each 32-bit word is single-copy atomic.
+// Overwriting is safe without a barrier too: a CTA publishes a buffer again
+// only after it has gathered the other buffer's next publication from every
+// CTA, which each of them makes after its own gather of this one.
+constexpr uint32_t PUB_BIT = 0x80000000u;
+__device__ __forceinline__ void st_pub_u1(uint32_t *p, uint32_t v)
+{
+#if defined(CTW_EMU)
+	__atomic_store_n(p, v, __ATOMIC_RELAXED);
+#elif defined(__CUDA_ARCH__)
+	asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+#else
+	*p = v;
+#endif
+}
+__device__ __forceinline__ void st_pub_u2(uint32_t *p, uint2 v)
+{
+#if defined(CTW_EMU)
+	__atomic_store_n(p, v.x, __ATOMIC_RELAXED);
+	__atomic_store_n(p + 1, v.y, __ATOMIC_RELAXED);
+#elif defined(__CUDA_ARCH__)
+	asm volatile("st.relaxed.gpu.global.v2.u32 [%0], {%1, %2};" :: "l"(p), "r"(v.x), "r"(v.y) : "memory");
+#else
+	p[0] = v.x;
+	p[1] = v.y;
+#endif
+}
+__device__ __forceinline__ uint2 ld_pub_u2(const uint32_t *p)
+{
+	uint2 v;
+#if defined(CTW_EMU)
+	v.x = __atomic_load_n(p, __ATOMIC_RELAXED);
+	v.y = __atomic_load_n(p + 1, __ATOMIC_RELAXED);
+#elif defined(__CUDA_ARCH__)
+	asm volatile("ld.relaxed.gpu.global.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+#else
+	v = *reinterpret_cast<const uint2 *>(p);
+#endif
+	return v;
+}
+__device__ __forceinline__ void grid_pause()
+{
+#if defined(CTW_EMU)
+	emu_yield();
+#endif
+}
+
+// Gather K published pairs (addr(k)), polling each until both words carry the
+// parity bit `want` (PUB_BIT or 0), and strip the bit.  A wait that runs out
+// (GRID_WAIT_NS of %globaltimer) marks the launch (ST_GRID_WAIT) and ends every
+// later wait of the CTA (*dead).
+template <int K, class Addr>
+__device__ __forceinline__ void pub_gather(uint2 (&w)[K], Addr addr, uint32_t want, uint32_t &err,
+                                           volatile int *dead)
+{
+#pragma unroll
+	for (int k = 0; k < K; ++k) w[k] = ld_pub_u2(addr(k));
+	auto stale = [&](int k) { return ((w[k].x ^ want) | (w[k].y ^ want)) & PUB_BIT; };
+	uint32_t bad = 0;
+#pragma unroll
+	for (int k = 0; k < K; ++k) bad |= stale(k);
+	if (bad && !*dead)
+	{
+		const unsigned long long t0 = grid_timer();
+		for (;;)
+		{
+			grid_pause();
+			bad = 0;
+#pragma unroll
+			for (int k = 0; k < K; ++k)
+				if (stale(k))
+				{
+					w[k] = ld_pub_u2(addr(k));
+					bad |= stale(k);
+				}
+			if (!bad || *dead) break;
+			if (grid_timer() - t0 > GRID_WAIT_NS)
+			{
+				err |= ST_GRID_WAIT;
+				*dead = 1;
+				break;
+			}
+		}
+	}
+#pragma unroll
+	for (int k = 0; k < K; ++k)
+	{
+		w[k].x &= ~PUB_BIT;
+		w[k].y &= ~PUB_BIT;
+	}
 }
 __device__ __forceinline__ void warp_sync()
 {
@@ -622,10 +727,13 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	unsigned *bar = ga.bar + (size_t)lane * GRID_BAR_WORDS;
 	unsigned *cpub = bar + 32;                                  // [G] carry publications of each CTA
 	unsigned nbar = 0, ncar = 0;
-	// the left neighbour's last chunk is recomputed here when it is at most half
-	// a run; otherwise (runs of 16 words with CSIZE 16 at degree 2^18) the
-	// neighbour publishes its run-end carries and this CTA waits for them
-	const bool nbr = 2 * csz <= MG;
+	unsigned npx = 0, npr = 0;                                  // publications of gx / gr in this launch
+	volatile int *vdead = &dead;
+	// on two primes the left neighbour's last chunk is recomputed here when it
+	// is at most half a run; otherwise (three primes, whose Garner step costs
+	// more than the wait, or a chunk of more than half a run) the neighbour
+	// publishes its run-end carries and this CTA waits for them
+	const bool nbr = NP == 2 && 2 * csz <= MG;
 	auto gsync = [&]() {
 		++nbar;
 		grid_arrive(bar);
@@ -775,11 +883,13 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 			xpass(std::integral_constant<int, 1>{}, 0, MG, ld_xc, st_xc);
 			__syncthreads();
 		}
-		// X3: last forward cross pass, columns published to L2
+		// X3: last forward cross pass, columns published to L2 (reduced to
+		// [0, 2q), with the parity bit)
+		const uint32_t bx = (++npx & 1) ? PUB_BIT : 0u;
+		const bool pub = ga.test_mute != g + 1 || npx > 1;       // testing: one CTA skips its first publication
 		xpass(std::integral_constant<int, PL>{}, 0, MG, ld_xc, [&](int pi, int h, int tt, uint32_t v) {
-			st_l2_u1(gx + (size_t)g * 3 * M + pi * M + h * MG + tt, v);
+			if (pub) st_pub_u1(gx + (size_t)g * 3 * M + pi * M + h * MG + tt, red(v, 2 * qv(pi)) | bx);
 		});
-		gsync();
 		// A: gather row block g (pairs of coefficients m0, m0 + 1 of every sub-block j),
 		// local levels 0 .. C-1
 		for (int it = tid; it < NP * 128; it += nt)
@@ -787,13 +897,16 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 			const int pi = it >> 7, m0 = 2 * (it & 127);
 			const uint32_t q = qv(pi);
 			uint32_t v0[NSB], v1[NSB];
+			uint2 w[NSB];
+			pub_gather<NSB>(w, [&](int j) {
+				const int m = j * 256 + m0, c = m / MG, tt = m - c * MG;
+				return gx + (size_t)c * 3 * M + pi * M + g * MG + tt;
+			}, bx, err, vdead);
 #pragma unroll
 			for (int j = 0; j < NSB; ++j)
 			{
-				const int m = j * 256 + m0, c = m / MG, tt = m - c * MG;
-				const uint2 w = ld_l2_u2(gx + (size_t)c * 3 * M + pi * M + g * MG + tt);
-				v0[j] = w.x;
-				v1[j] = w.y;
+				v0[j] = w[j].x;
+				v1[j] = w[j].y;
 			}
 			group_fwd_s<NSB>(v0, reinterpret_cast<const uint2 *>(TF) + pi * M, aidx, q);
 			group_fwd_s<NSB>(v1, reinterpret_cast<const uint2 *>(TF) + pi * M, aidx, q);
@@ -806,7 +919,9 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		for (int wt = warp; wt < NP * NSB; wt += nwarps) wphase(wt / NSB, wt % NSB, mode);
 		if (mode == LM_FWD_ONLY) return;
 		__syncthreads();
-		// A': inverse local levels C-1 .. 0, row published to L2 (natural order)
+		// A': inverse local levels C-1 .. 0, row published to L2 (natural order,
+		// values in [0, 2q), with the parity bit)
+		const uint32_t br = (++npr & 1) ? PUB_BIT : 0u;
 		for (int it = tid; it < NP * 128; it += nt)
 		{
 			const int pi = it >> 7, m0 = 2 * (it & 127);
@@ -823,9 +938,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 			group_inv_s<NSB>(v1, reinterpret_cast<const uint2 *>(TI) + pi * M, aidx, q);
 #pragma unroll
 			for (int j = 0; j < NSB; ++j)
-				st_l2_u2(gr + (size_t)g * 3 * M + pi * M + j * 256 + m0, make_uint2(v0[j], v1[j]));
+				st_pub_u2(gr + (size_t)g * 3 * M + pi * M + j * 256 + m0, make_uint2(v0[j] | br, v1[j] | br));
 		}
-		gsync();
 		// Y1: gather the columns — this CTA's and the left neighbour's last chunk —
 		// in pairs, first inverse cross pass
 		const int ncols = nbr ? MG + csz : MG;
@@ -845,12 +959,13 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 				auto idx = [&](int t, int kk) { return (1 << (l0 + t)) + (jblk << t) + kk; };
 				const uint32_t *src = gr + pi * M + (tt < MG ? g * MG + tt : gl * MG + (MG - csz) + (tt - MG));
 				uint32_t u0[R], u1[R];
+				uint2 w[R];
+				pub_gather<R>(w, [&](int k) { return src + (size_t)(hbase + k * stride) * 3 * M; }, br, err, vdead);
 #pragma unroll
 				for (int k = 0; k < R; ++k)
 				{
-					const uint2 w = ld_l2_u2(src + (size_t)(hbase + k * stride) * 3 * M);
-					u0[k] = w.x;
-					u1[k] = w.y;
+					u0[k] = w[k].x;
+					u1[k] = w[k].y;
 				}
 				group_inv<R>(u0, tw, idx, q, qi, l0 == 0, a.omega[pi], a.k1[pi], a.sc[pi]);
 				group_inv<R>(u1, tw, idx, q, qi, l0 == 0, a.omega[pi], a.k1[pi], a.sc[pi]);

@@ -80,12 +80,14 @@ constexpr int GRID_BAR_WORDS = 32 + 128;
 // Buffers of the grid kernel (prp_grid.cu): one candidate on G = 2^lg CTAs of a
 // cooperative launch, transposes and run-end carries through L2.
 struct PrpGridArgs {
-	uint32_t *gx;               // [lanes][G][3][M] published column planes
-	uint32_t *gr;               // [lanes][G][3][M] published row planes
+	uint32_t *gx;               // [lanes][G][3][M] published column planes } zero at launch (their
+	uint32_t *gr;               // [lanes][G][3][M] published row planes    } words carry a parity bit)
 	long long *gc;              // [lanes][G][G] run-end carries
 	unsigned *bar;              // [lanes][GRID_BAR_WORDS], zero at launch: word 0 the grid barrier
 	                            // count, words 32 + g the carry publications of CTA g
 	const uint32_t *xr;         // [3][2][128] cross-level roots (Montgomery): forward, inverse
+	int test_mute;              // testing only: 1 + a CTA whose first publication of the launch is
+	                            // skipped (its readers' waits run out); 0 in every normal launch
 };
 // Grid splits with a kernel: 2^lg CTAs of 2^lm coefficients for (lg, lm) =
 // (5, 12), (6, 12) (D = 2^17, 2^18), (5, 11), (6, 11), (7, 11) (D = 2^16..2^18)

@@ -182,11 +182,13 @@ int ctw_prp_geometry(ctw_prp *h, int *ctas_per_lane, int *threads, int *smem_byt
 long long ctw_prp_launches(ctw_prp *h);
 /* Degree of the tested numbers (log2), lanes, and 1 for an N- engine. */
 int ctw_prp_shape(ctw_prp *h, int *log2_degree, int *lanes, int *minus);
-/* Testing only, no counterpart in the reference: the next launch of a grid
- * handle starts its grid-barrier counter out of reach, so that every CTA's
- * bounded wait (50 ms of %globaltimer) runs out.  That launch ends with
- * CTW_E_COMPUTE (status ST_GRID_WAIT, results void) and the handle stays
- * usable; later launches are unaffected.  CTW_E_ARG for a non-grid split. */
+/* Testing only, no counterpart in the reference: in the next launch of a grid
+ * handle the grid-barrier counter starts out of reach and CTA 0 skips its first
+ * publication of columns, so that the other CTAs' bounded waits (50 ms of
+ * %globaltimer each, on the barrier or on the published words) run out.  That
+ * launch ends with CTW_E_COMPUTE (status ST_GRID_WAIT, results void) and the
+ * handle stays usable; later launches are unaffected.  CTW_E_ARG for a
+ * non-grid split. */
 int ctw_prp_test_unreachable_barrier(ctw_prp *h);
 
 /* z = x * y for `lanes` candidates of degree D = 2^log2_degree (8..14), with

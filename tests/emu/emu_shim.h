@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <sched.h>
 struct dim3 {
 	unsigned x, y, z;
 	dim3(unsigned a = 1, unsigned b = 1, unsigned c = 1) : x(a), y(b), z(c) {}
@@ -42,3 +43,5 @@ inline uint4 make_uint4(uint32_t x, uint32_t y, uint32_t z, uint32_t w) { return
 inline int4 make_int4(int32_t x, int32_t y, int32_t z, int32_t w) { return int4{ x, y, z, w }; }
 uint32_t *emu_smem();
 unsigned long long emu_timer_ns();
+// a thread that polls another CTA's words lets the host threads of that CTA run
+inline void emu_yield() { sched_yield(); }

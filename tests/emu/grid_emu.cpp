@@ -81,7 +81,8 @@ static void *run(void *p)
 	return nullptr;
 }
 
-static int launch(Kern k, const PrpKernelArgs &a, const PrpGridArgs &ga, int G, int threads, size_t smem_words)
+static int launch(Kern k, const PrpKernelArgs &a, const PrpGridArgs &ga, int G, int threads, size_t smem_words,
+                  size_t pub_words)
 {
 	gridDim = dim3(G);
 	blockDim = dim3(threads);
@@ -92,6 +93,8 @@ static int launch(Kern k, const PrpKernelArgs &a, const PrpGridArgs &ga, int G, 
 	g_wbar.clear();
 	for (int w = 0; w < G * g_warps; ++w) g_wbar.push_back(new std::barrier<>(32));
 	memset(ga.bar, 0, GRID_BAR_WORDS * sizeof(unsigned));
+	memset(ga.gx, 0, pub_words * sizeof(uint32_t));      // as the engine zeroes them before every launch
+	memset(ga.gr, 0, pub_words * sizeof(uint32_t));
 	std::vector<Job> jobs((size_t)G * threads);
 	std::vector<pthread_t> th((size_t)G * threads);
 	pthread_attr_t attr;
@@ -154,14 +157,14 @@ int main(int argc, char **argv)
 	a.status = status.data(); a.lm = lm; a.csize = csize; a.mult = mult; a.scratch = scratch.data(); a.nprime = np;
 	a.tw_smem = grid_words(lg, lm, 1, np) * 4 <= 227 * 1024 ? 1 : 0;
 	if (lm <= 11 && ((1 << lm) >> lg) < 32) a.swz_b = 20;   // the launch's swizzle for 16-word runs
-	PrpGridArgs ga{ gx.data(), gr.data(), gc.data(), bar.data(), xr.data() };
+	PrpGridArgs ga{ gx.data(), gr.data(), gc.data(), bar.data(), xr.data(), 0 };
 	const size_t words = grid_words(lg, lm, a.tw_smem, np);
 	uint32_t bits[2] = { 3u, 3u };
 	std::vector<int32_t> x0 = x;
 	a.op = OP_SQUARE; a.reg_in = x.data(); a.reg_out = x.data(); a.bits = bits; a.nwords = 1; a.i_hi = 1; a.count = 2;
-	launch(k, a, ga, G, nth, words);
+	launch(k, a, ga, G, nth, words, gx.size());
 	a.op = OP_MUL; a.reg_in = x.data(); a.reg_y = y.data(); a.reg_out = out.data(); a.count = 1;
-	launch(k, a, ga, G, nth, words);
+	launch(k, a, ga, G, nth, words, gx.size());
 	orc_prp_tables *t = orc_prp_tables_create(ln);
 	std::vector<int32_t> r = x0;
 	orc_square_dup(t, r.data(), bs, mult, csize);
