@@ -484,6 +484,29 @@ __device__ __forceinline__ int32_t reduce_b<int64_t>(int64_t &f, uint32_t b, uin
 	return s ? -(int32_t)r_l : (int32_t)r_l;
 }
 
+// The same truncated division of a 64-bit f in one step, for the grid
+// kernel's carry chains: with m = floor((2^64 - 1) / b), q = hi64(|f| m) is
+// floor(|f| / b) or one less (|f| < 2^63) and the remainder fits 32 bits, so
+// one correction ends it.  For b >= 64 and |f| < 2^63 the two Barrett steps of
+// reduce_b<int64_t> are exact (the first step's estimate is low by less than
+// 2^(2 - b_s) + 1/2 < 1, the second's by less than 1, and the range check
+// needs |f| >= 2^(b_s + 61)), so both give the same quotient and remainder;
+// this one has the shorter dependent chain.
+__device__ __forceinline__ int32_t reduce_b64(int64_t &f, uint32_t b, uint64_t m)
+{
+	const bool s = f < 0;
+	const uint64_t t = s ? 0 - (uint64_t)f : (uint64_t)f;
+	uint64_t q = __umul64hi(t, m);
+	uint32_t r = (uint32_t)t - (uint32_t)q * b;
+	if (r >= b)
+	{
+		r -= b;
+		++q;
+	}
+	f = s ? -(int64_t)q : (int64_t)q;
+	return s ? -(int32_t)r : (int32_t)r;
+}
+
 constexpr uint64_t Q21 = (uint64_t)Q2 * Q1;
 
 // Balanced CRT value of residues r0, r1, r2 (each in [0, q)) as 96-bit two's

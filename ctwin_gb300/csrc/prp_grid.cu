@@ -655,7 +655,7 @@ __host__ __device__ __forceinline__ size_t grid2_words(int lg, int lm, int np)
 // W0, W1 and XDo are 16-byte aligned: the words move in 16-byte pieces.
 template <int CSZ>
 __device__ __forceinline__ int64_t norm1_chunk64(const uint32_t *W0, const uint32_t *W1, int32_t *XDo, int mult,
-                                                  uint32_t b, uint32_t b_inv, int b_s, uint32_t &err)
+                                                  uint32_t b, uint64_t b_m)
 {
 	uint32_t lo[CSZ], hi[CSZ];
 #pragma unroll
@@ -671,7 +671,7 @@ __device__ __forceinline__ int64_t norm1_chunk64(const uint32_t *W0, const uint3
 	for (int i = 0; i < CSZ; ++i)
 	{
 		acc += (int64_t)((uint64_t)lo[i] | ((uint64_t)hi[i] << 32)) * (int64_t)mult;
-		d[i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+		d[i] = reduce_b64(acc, b, b_m);
 	}
 #pragma unroll
 	for (int i = 0; i < CSZ; i += 4) *reinterpret_cast<int4 *>(XDo + i) = make_int4(d[i], d[i + 1], d[i + 2], d[i + 3]);
@@ -712,6 +712,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
 	const int b_s = (int)a.lane_b[4 * lane + 2];
+	const uint64_t b_m = ~0ull / b;                             // reciprocal of the one-step carry division
 	const bool narrow = NP == 2 || (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;
 	uint32_t err = 0;
 
@@ -1024,15 +1025,15 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		// neighbour computes for itself (normalize1 of a chunk starts from zero,
 		// so it needs that chunk's Garner words only)
 		auto norm1 = [&](const uint32_t *W, int stride_pl, int32_t *XDo) -> int64_t {
-			if (narrow && csz == 8) return norm1_chunk64<8>(W, W + stride_pl, XDo, mult, b, b_inv, b_s, err);
-			if (narrow && csz == 16) return norm1_chunk64<16>(W, W + stride_pl, XDo, mult, b, b_inv, b_s, err);
+			if (narrow && csz == 8) return norm1_chunk64<8>(W, W + stride_pl, XDo, mult, b, b_m);
+			if (narrow && csz == 16) return norm1_chunk64<16>(W, W + stride_pl, XDo, mult, b, b_m);
 			if (narrow)
 			{
 				int64_t acc = 0;
 				for (int i = 0; i < csz; ++i)
 				{
 					acc += load64(W, stride_pl, i) * (int64_t)mult;
-					XDo[i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+					XDo[i] = reduce_b64(acc, b, b_m);
 				}
 				return acc;
 			}
@@ -1077,7 +1078,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 			for (; i < csz - 1; ++i)
 			{
 				acc += Xh[i];
-				Xh[i] = reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+				Xh[i] = reduce_b64(acc, b, b_m);
 				if (acc == 0) { done = true; break; }
 			}
 			if (!done)
