@@ -723,6 +723,21 @@ __device__ __forceinline__ void csync()
 	else __syncthreads();
 }
 
+// normalize1 over chunk c of 64-bit Garner integers (x mult): the one-step
+// division of reduce_b64, b_m = floor((2^64 - 1) / b).
+__device__ __forceinline__ int64_t carry_chunk64(uint32_t *X, int M, int c, int csize, int sb, int mult, uint32_t b,
+                                                 uint64_t b_m)
+{
+	int64_t acc = 0;
+	for (int i = 0; i < csize; ++i)
+	{
+		const int p = swz(c * csize + i, sb);
+		acc += load64(X, M, p) * (int64_t)mult;
+		X[p] = (uint32_t)reduce_b64(acc, b, b_m);
+	}
+	return acc;
+}
+
 // normalize1 over chunk c: carry of the Garner integers (x mult) into digits.
 template <class T>
 __device__ __forceinline__ int64_t carry_chunk(uint32_t *X, int M, int c, int csize, int sb, int mult, uint32_t b,

@@ -239,6 +239,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
 	const int b_s = (int)a.lane_b[4 * lane + 2];
+	const uint64_t b_m = ~0ull / b;                             // reciprocal of the one-step carry division
 	const bool narrow = NP == 2 || (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;
 	uint32_t err = 0;
 
@@ -358,7 +359,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 				{
 					const int p = swz(base + i, sb) - cb;
 					acc += load64(Xh, M, p) * (int64_t)mult;
-					Xh[p] = (uint32_t)reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+					Xh[p] = (uint32_t)reduce_b64(acc, b, b_m);
 				}
 				acc_f = acc;
 			}
@@ -396,7 +397,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid(c
 			{
 				const int p = swz(base + i, sb) - cb;
 				acc += (int32_t)Xh[p];
-				Xh[p] = (uint32_t)reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+				Xh[p] = (uint32_t)reduce_b64(acc, b, b_m);
 				if (acc == 0) { done = true; break; }
 			}
 			if (!done)

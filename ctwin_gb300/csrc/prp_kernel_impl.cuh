@@ -50,6 +50,7 @@ __device__ __forceinline__ void prp_body(const PrpKernelArgs &a, uint32_t *sm, c
 
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
 	const int b_s = (int)a.lane_b[4 * lane + 2];
+	const uint64_t b_m = ~0ull / b;                 // reciprocal of the one-step carry division
 	// 64-bit carries: always with two primes, else launch-wide or per lane
 	const bool narrow = NP == 2 || (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;
 	uint32_t err = 0;
@@ -154,8 +155,8 @@ __device__ __forceinline__ void prp_body(const PrpKernelArgs &a, uint32_t *sm, c
 		for (int c = tid; c < ncu; c += nt)
 		{
 			int64_t f;
-			if constexpr (NP == 2) f = carry_chunk<int64_t>(X, M, c, a.csize, sb, mult, b, b_inv, b_s, err);
-			else f = narrow ? carry_chunk<int64_t>(X, M, c, a.csize, sb, mult, b, b_inv, b_s, err)
+			if constexpr (NP == 2) f = carry_chunk64(X, M, c, a.csize, sb, mult, b, b_m);
+			else f = narrow ? carry_chunk64(X, M, c, a.csize, sb, mult, b, b_m)
 			                : carry_chunk<i128>(X, M, c, a.csize, sb, mult, b, b_inv, b_s, err);
 			fch[c] = f;
 			if (c == ncu - 1) xch[0] = f;
@@ -189,7 +190,7 @@ __device__ __forceinline__ void prp_body(const PrpKernelArgs &a, uint32_t *sm, c
 			{
 				const int p = swz(c * a.csize + i, sb);
 				acc += (int32_t)X[p];
-				X[p] = (uint32_t)reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+				X[p] = (uint32_t)reduce_b64(acc, b, b_m);
 				if (acc == 0) { done = true; break; }
 			}
 			if (!done)
@@ -289,6 +290,7 @@ __device__ __forceinline__ void cols_body(const PrpKernelArgs &a, uint32_t *sm, 
 
 	const uint32_t b = a.lane_b[4 * lane + 0], b_inv = a.lane_b[4 * lane + 1];
 	const int b_s = (int)a.lane_b[4 * lane + 2];
+	const uint64_t b_m = ~0ull / b;                 // reciprocal of the one-step carry division
 	// 64-bit carries: always with two primes, else launch-wide or per lane
 	const bool narrow = NP == 2 || (a.narrow | (int)a.lane_b[4 * lane + 3]) != 0;
 	uint32_t err = 0;
@@ -489,7 +491,7 @@ __device__ __forceinline__ void cols_body(const PrpKernelArgs &a, uint32_t *sm, 
 					auto step = [&](int i) {
 						const int p = swz(base + i, sb) - cb;
 						acc += load64(Xh, M, p) * (int64_t)mult;
-						Xh[p] = (uint32_t)reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+						Xh[p] = (uint32_t)reduce_b64(acc, b, b_m);
 					};
 					if (csz == 8)
 					{
@@ -546,7 +548,7 @@ __device__ __forceinline__ void cols_body(const PrpKernelArgs &a, uint32_t *sm, 
 			{
 				const int p = swz(base + i, sb) - cb;
 				acc += (int32_t)Xh[p];
-				Xh[p] = (uint32_t)reduce_b<int64_t>(acc, b, b_inv, b_s, err);
+				Xh[p] = (uint32_t)reduce_b64(acc, b, b_m);
 				if (acc == 0) { done = true; break; }
 			}
 			if (!done)
