@@ -609,14 +609,14 @@ __device__ __forceinline__ void pub_gather(uint2 (&w)[K], Addr addr, uint32_t wa
 		for (;;)
 		{
 			grid_pause();
-			bad = 0;
+			// every stale pair is loaded again before any result is looked at,
+			// so that one round costs one L2 round trip
 #pragma unroll
 			for (int k = 0; k < K; ++k)
-				if (stale(k))
-				{
-					w[k] = ld_pub_u2(addr(k));
-					bad |= stale(k);
-				}
+				if (stale(k)) w[k] = ld_pub_u2(addr(k));
+			bad = 0;
+#pragma unroll
+			for (int k = 0; k < K; ++k) bad |= stale(k);
 			if (!bad || *dead) break;
 			if (grid_timer() - t0 > GRID_WAIT_NS)
 			{
