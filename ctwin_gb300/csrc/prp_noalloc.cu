@@ -115,6 +115,19 @@ extern "C" int ctw_prp_mul_noalloc(int log2_degree, int lanes, const uint32_t *b
 		            "(lanes * 12 * D bytes <= %zu, lanes <= %d)", lanes, log2_degree, NA_SCRATCH_BYTES, NA_MAX_LANES);
 	if (csize != 8 && csize != 16 && csize != 32 && csize != 64) return fail(CTW_E_ARG, "csize %d not in {8,16,32,64}", csize);
 	if (!b || !x_dev || !y_dev || !z_dev) return fail(CTW_E_ARG, "ctw_prp_mul_noalloc: null pointer");
+	{
+		// the call copies from this stack frame and synchronises its stream: it
+		// cannot be recorded into a graph
+		cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+		const cudaError_t e = cudaStreamIsCapturing((cudaStream_t)stream, &cs);
+		if (e != cudaSuccess)
+		{
+			cudaGetLastError();
+			return fail(CTW_E_ARG, "ctw_prp_mul_noalloc: capture status of the stream: %s", cudaGetErrorString(e));
+		}
+		if (cs != cudaStreamCaptureStatusNone)
+			return fail(CTW_E_ARG, "ctw_prp_mul_noalloc: the stream is being captured (the call synchronises it)");
+	}
 	uint32_t lb[NA_MAX_LANES * 4];
 	uint32_t bmax = 0;
 	for (int l = 0; l < lanes; ++l)

@@ -210,7 +210,8 @@ int ctw_prp_test_unreachable_barrier(ctw_prp *h);
  * z may be x or y, or both (x == y squares): each CTA reads the words of x
  * and y that it later writes in z, and reads them before it writes.
  * Runs on `stream` (a cudaStream_t, NULL = default) and returns after it has
- * synchronised the stream. */
+ * synchronised the stream; CTW_E_ARG when `stream` is being captured into a
+ * graph. */
 int ctw_prp_mul_noalloc(int log2_degree, int lanes, const uint32_t *b, const int32_t *x_dev,
                         const int32_t *y_dev, int32_t *z_dev, int csize, void *stream);
 

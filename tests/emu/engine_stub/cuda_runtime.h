@@ -28,6 +28,7 @@ struct EmuGraph {
 typedef EmuGraph *cudaGraph_t;
 typedef EmuGraph *cudaGraphExec_t;
 enum cudaStreamCaptureMode { cudaStreamCaptureModeRelaxed = 2 };
+enum cudaStreamCaptureStatus { cudaStreamCaptureStatusNone = 0, cudaStreamCaptureStatusActive = 1 };
 enum { cudaEventDisableTiming = 2 };
 
 typedef int cudaError_t;
@@ -126,6 +127,11 @@ inline cudaError_t cudaStreamBeginCapture(cudaStream_t, cudaStreamCaptureMode)
 {
 	if (emu_capture) return cudaErrorInvalidValue;
 	emu_capture = new std::vector<std::function<void()>>();
+	return cudaSuccess;
+}
+inline cudaError_t cudaStreamIsCapturing(cudaStream_t, cudaStreamCaptureStatus *st)
+{
+	*st = emu_capture ? cudaStreamCaptureStatusActive : cudaStreamCaptureStatusNone;
 	return cudaSuccess;
 }
 inline cudaError_t cudaStreamEndCapture(cudaStream_t, cudaGraph_t *g)

@@ -65,3 +65,28 @@ def test_mul_noalloc_rejects_oversize(native):
     assert L.ctw_prp_mul_noalloc(14, 64, ctypes.c_void_p(b.ctypes.data), null, null, null, 16, None) == -1
     assert b"exceed the fixed scratch" in L.ctw_last_error()
     assert L.ctw_prp_mul_noalloc(15, 1, ctypes.c_void_p(b.ctypes.data), null, null, null, 16, None) == -1
+
+
+def test_mul_noalloc_rejects_stream_capture(native):
+    """The call synchronises its stream, so it refuses a stream under capture
+    (CTW_E_ARG) instead of recording a copy from its own stack frame."""
+    import torch
+
+    from ctwin_gb300._native import lib
+    L = lib()
+    b = np.full(1, 1000003, dtype=np.uint32)
+    x = torch.zeros(1 << 11, dtype=torch.int32, device="cuda")
+    keep = torch.zeros(16, device="cuda")
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        keep.add_(1.0)                     # the graph holds one node of its own
+        st = torch.cuda.current_stream().cuda_stream
+        rc = L.ctw_prp_mul_noalloc(11, 1, ctypes.c_void_p(b.ctypes.data), ctypes.c_void_p(x.data_ptr()),
+                                   ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(x.data_ptr()), 16,
+                                   ctypes.c_void_p(st))
+    assert rc == -1
+    assert b"being captured" in L.ctw_last_error()
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(keep[0]) == 2.0
