@@ -1,9 +1,10 @@
 """Benchmark: single large PRP test, degree D = 2^16, b uniform in [2^20, 2^21).
 
 One step = one Gerbicz-Li block of the Fermat test: B_GL squarings of the real
-exponent bits (one resident-kernel launch, the residue stays in shared memory of
-a 16-CTA cluster) followed by the Gerbicz-Li multiply d <- d * x, exactly the
-work cyclo::check does between two checkpoints (cyclo/src/cyclo.h:277-308).
+exponent bits (one resident-kernel launch: the residue stays in the shared
+memory of a 64-CTA cooperative grid) followed by the Gerbicz-Li multiply
+d <- d * x, exactly the work cyclo::check does between two checkpoints
+(cyclo/src/cyclo.h:277-308).
 
   value  squarings/s with the residue and exponent resident in HBM (CUDA events
          on the engine's stream, per step, L2 flushed between steps)
@@ -30,9 +31,9 @@ Two more workloads print their own line (not the default):
          2^32 (both forms), then base-3 PRP of every survivor and of its twin partner N-
   --workload serve  a seeded Poisson stream of full PRP tests, degree 2^k with k
          log-uniform in [12, --serve-max-degree], b uniform in [2^16, 2^24), through the
-         server (continuous batching by degree, admission by pool bytes); tests/s and
-         p50/p99 latency per degree, beside the plain path run for real on the first
-         arrivals (one test at a time)
+         server (continuous batching by degree, admission by pool bytes; degrees 2^16
+         and up in its grid lane); tests/s and p50/p99 latency per degree, beside the
+         plain path run for real on the first arrivals (one test at a time)
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload single|batch|serve]
 """
@@ -78,7 +79,7 @@ def workload(rank: int):
     return b, E, i0, B_GL, words
 
 
-TRAFFIC_PER_LAUNCH = 2.58e6     # ncu dram read+write bytes of one 651-squaring launch at 2^16 (64-CTA grid)
+TRAFFIC_PER_LAUNCH = 2.53e6     # ncu dram read+write bytes of one 651-squaring launch at 2^16 (64-CTA grid)
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one 651-squaring launch of the "
                   "default split (profiles/prp_kernel_grid2_d65536_full.md)")
 
@@ -515,21 +516,40 @@ def pct(v, q):
 
 def run_serve(args):
     import torch  # noqa: F401  (CUDA context for the library)
-    from ctwin_gb300 import Pool, Server, autotune, two_primes
+    from ctwin_gb300 import Pool, PrpEngine, Server, autotune, two_primes
     rng = random.Random(11)
     kmax = args.serve_max_degree
     degrees = tuple(range(12, kmax + 1))
     lo, hi = math.log(12), math.log(kmax + 1)
+    lane = 16                             # the server's grid lane: degrees 2^16 and up
     # capacity from the pools themselves: device time per lane-squaring of a
     # pool tick of each degree and prime class (squarings, multiply, register
-    # moves, graph launch); 64 slots up to 2^15, 8 above
+    # moves, graph launch), 64 slots; for the grid lane's degrees the device
+    # time per squaring of one test on the one-lane engine (the lane runs one
+    # test at a time and takes turns with the pools)
     us, frac2 = {}, {}
+    words = np.array([rng.getrandbits(32) for _ in range(64)], dtype=np.uint32)
     for k in degrees:
-        slots = 64 if k <= 15 else 8
+        slots = 64
         lim = max([b for b in range(1 << 16, 1 << 24, 1 << 12) if two_primes(k, b)] or [(1 << 16) - 1])
         frac2[k] = max(0.0, (lim - (1 << 16)) / ((1 << 24) - (1 << 16)))
         for primes, (b_lo, b_hi) in ((2, (1 << 16, lim)), (3, (lim + (1 << 12), 1 << 24))):
             if b_hi <= b_lo:
+                continue
+            if k >= lane:
+                with PrpEngine(k, 1) as eng:
+                    eng.set_b([rng.randrange(b_lo, b_hi)])
+                    assert eng.prime_count == primes
+                    eng.set(1)
+                    eng.square_bits(words, 2047, 256)
+                    eng.sync()
+                    st = torch.cuda.ExternalStream(eng.stream)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(st)
+                    eng.square_bits(words, 2047, 1024)
+                    e1.record(st)
+                    e1.synchronize()
+                    us[(k, primes)] = e0.elapsed_time(e1) * 1e3 / 1024
                 continue
             lg, cs, _ = autotune(k, slots, primes)
             with Pool(k, slots, log2_ctas=lg, csize=cs) as p:
@@ -557,9 +577,11 @@ def run_serve(args):
         t += rng.expovariate(lam)
         k = int(math.exp(rng.uniform(lo, hi)))
         reqs.append((t, k, rng.randrange(1 << 16, 1 << 24)))
-    srv = Server(hbm_budget_bytes=args.hbm_budget << 30, max_slots=256, ticks_per_launch=1, autotune=True)
+    srv = Server(hbm_budget_bytes=args.hbm_budget << 30, max_slots=256, ticks_per_launch=1, autotune=True,
+                 grid_lane=lane)
     for k in degrees:
-        srv.prepare(k, 0)
+        if k < lane:
+            srv.prepare(k, 0)
     last, still = -1, 0
     while still < 10:                     # pools created and tuned: bytes stable for 1 s
         nb = srv.stats()["pool_bytes"]
@@ -594,8 +616,10 @@ def run_serve(args):
         "n_gpus": 1, "steps": n, "warmup": 0, "ms_per_step": 1000.0 * span / max(1, len(res)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": f"{n} Poisson arrivals (seed 11, rate {lam:.3f}/s = {args.load:.0%} of the capacity "
-                               f"measured on pool ticks), degree 2^k, k log-uniform in [12, {kmax}], "
-                               "b uniform in [2^16, 2^24)",
+                               f"measured on pool ticks and on the grid lane's engine), degree 2^k, k log-uniform "
+                               f"in [12, {kmax}], b uniform in [2^16, 2^24); degrees 2^{lane} and up in the "
+                               "server's grid lane (one test at a time on the cooperative grid kernel, taking "
+                               "turns with the pools)",
                    "us_per_lane_squaring": {f"{k}" + ("" if c == 2 else "w"): v for (k, c), v in us.items()},
                    "two_prime_fraction": {str(k): v for k, v in frac2.items()},
                    "hbm_budget_gib": args.hbm_budget, "ticks_per_launch": 1},

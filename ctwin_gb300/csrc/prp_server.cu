@@ -12,6 +12,14 @@
 // where the degree has a two-prime kernel, whether b lies within the two-prime
 // bound: tests above it get pools of their own, so that they never hold the
 // others' launches at three primes.
+//
+// Grid lane: a test of degree >= grid_min (2^16 by default) runs instead on a
+// one-lane engine, i.e. on the cooperative grid kernel that spreads one test
+// over 64-128 SMs, one test at a time, on a thread of its own.  A cooperative
+// grid needs all of its CTAs resident at once, so the lane and the pools take
+// turns on the device: at every Gerbicz-Li checkpoint of the lane's test the
+// lane hands the device back, the worker issues one round of pool launches,
+// waits for the pools' streams and hands it over again.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -25,6 +33,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/ctwin_gb300.h"
+#include "bignum.h"
 #include "prp_host.h"
 #include "prp_pool.h"
 #include "prp_tables.h"
@@ -64,7 +73,13 @@ struct ctw_server {
 	long long submitted = 0, finished = 0, active = 0, pending = 0;
 	size_t bytes = 0;
 
-	std::thread prep, worker;
+	std::thread prep, worker, grid;
+	// grid lane (guarded by mu): queue, turn flags, the test on the device
+	int grid_min = 16;
+	std::deque<Request> grid_q;
+	std::condition_variable cv_grid, cv_turn;
+	bool grid_wants = false, grid_has = false;
+	int grid_running = 0;
 	// worker-owned
 	std::map<int, std::vector<ctw_pool *>> pools;   // class -> pools
 	std::map<int, std::pair<int, int>> split;      // class -> (log2 CTAs, csize)
@@ -160,8 +175,11 @@ void worker_loop(ctw_server *s)
 				for (ctw_pool *p : kv.second)
 					if (pool_active(p) > 0 || pool_in_flight(p) > 0) busy = true;
 			if (!busy)
-				s->cv_ready.wait_for(lk, std::chrono::milliseconds(2),
-				                     [&] { return s->stop || !s->ready.empty() || !s->prepare_req.empty(); });
+				s->cv_ready.wait_for(lk, std::chrono::milliseconds(2), [&] {
+					return s->stop || !s->ready.empty() || !s->prepare_req.empty() || s->grid_wants;
+				});
+			// no pool work is issued while the grid lane holds the device
+			s->cv_turn.wait(lk, [&] { return s->stop || !s->grid_has; });
 			if (s->stop) break;
 			while (!s->ready.empty())
 			{
@@ -283,15 +301,141 @@ void worker_loop(ctw_server *s)
 				s->done.push_back(r);
 			}
 			s->finished += (long long)out.size();
-			s->active = act;
-			s->pending = (long long)s->waiting.size() + (long long)s->ready.size() + (long long)s->incoming.size();
+			s->active = act + s->grid_running;
+			s->pending = (long long)s->waiting.size() + (long long)s->ready.size() + (long long)s->incoming.size() +
+			             (long long)s->grid_q.size();
 		}
 		if (!out.empty()) s->cv_done.notify_all();
+		// the grid lane asks for the device: let this round of pool launches
+		// finish, then hand it over
+		bool grant;
+		{
+			std::lock_guard<std::mutex> lk(s->mu);
+			grant = s->grid_wants && !s->grid_has;
+		}
+		if (grant)
+		{
+			for (auto &kv : s->pools)
+				for (ctw_pool *p : kv.second)
+					if (cudaStreamSynchronize((cudaStream_t)ctw_pool_stream(p)) != cudaSuccess) set_error(s, "sync");
+			{
+				std::lock_guard<std::mutex> lk(s->mu);
+				s->grid_has = true;
+			}
+			s->cv_turn.notify_all();
+			continue;
+		}
 		if (admitted == 0 && out.empty()) std::this_thread::sleep_for(std::chrono::microseconds(100));
 	}
 	for (auto &kv : s->pools)
 		for (ctw_pool *p : kv.second) ctw_pool_destroy(p);
 	s->pools.clear();
+}
+
+// The grid lane's turn: ask the worker for the device and wait until it is
+// handed over (false when the server stops).
+bool grid_take(ctw_server *s)
+{
+	std::unique_lock<std::mutex> lk(s->mu);
+	s->grid_wants = true;
+	s->cv_ready.notify_all();
+	s->cv_turn.wait(lk, [&] { return s->stop || s->grid_has; });
+	s->grid_wants = false;
+	return !s->stop;
+}
+void grid_give(ctw_server *s)
+{
+	{
+		std::lock_guard<std::mutex> lk(s->mu);
+		s->grid_has = false;
+	}
+	s->cv_turn.notify_all();
+}
+int grid_checkpoint(void *user, long long)
+{
+	ctw_server *s = static_cast<ctw_server *>(user);
+	grid_give(s);
+	return grid_take(s) ? 0 : 1;
+}
+
+// Squarings and multiplies of ctw_prp_run_ex for one test of b at degree 2^ln.
+long long grid_squarings(uint32_t b, int ln)
+{
+	const Big E = prp_exponent(b, ln);
+	const long long i0 = (long long)big_bitlen(E) - 1;
+	const int L = 2 << ((31 - __builtin_clz((uint32_t)i0)) / 2);
+	const long long B = (i0 - 1) / L + 1;
+	const long long j0 = (long long)big_bitlen(big_block_sum(E, (int)B)) - 1;
+	return (i0 + 1) + (i0 / B) + (j0 >= B ? j0 - B + 1 : 0) + B + 2;
+}
+
+void grid_loop(ctw_server *s)
+{
+	cudaSetDevice(s->device);
+	std::map<int, ctw_prp *> eng;
+	for (;;)
+	{
+		Request r;
+		{
+			std::unique_lock<std::mutex> lk(s->mu);
+			s->cv_grid.wait(lk, [&] { return s->stop || !s->grid_q.empty(); });
+			if (s->stop) break;
+			r = s->grid_q.front();
+			s->grid_q.pop_front();
+			s->grid_running = 1;
+		}
+		ctw_result res{};
+		res.tag = r.tag;
+		res.b = r.b;
+		res.log2_degree = r.ln;
+		res.slot = -2;
+		res.t_submit = r.t_submit;
+		ctw_prp *&h = eng[r.ln];
+		int rc = CTW_OK;
+		if (!h && (rc = ctw_prp_create(r.ln, 1, &h)) == CTW_OK) rc = ctw_prp_set_base(h, s->base);
+		if (rc != CTW_OK && h)
+		{
+			ctw_prp_destroy(h);
+			h = nullptr;
+		}
+		bool stopped = false;
+		if (rc == CTW_OK)
+		{
+			if (!grid_take(s)) break;
+			res.t_admit = mono_seconds();
+			uint8_t prp = 0, gl = 0;
+			uint64_t r64 = 0;
+			rc = ctw_prp_run_ex(h, &r.b, 1, -1, grid_checkpoint, s, &prp, &r64, &gl);
+			stopped = rc == CTW_STOPPED;
+			{
+				std::lock_guard<std::mutex> lk(s->mu);
+				if (s->grid_has) s->grid_has = false;
+			}
+			s->cv_turn.notify_all();
+			res.is_prp = prp;
+			res.res64 = r64;
+			res.gl_ok = gl;
+			res.squarings = grid_squarings(r.b, r.ln);
+		}
+		else
+			res.t_admit = mono_seconds();
+		if (stopped) break;
+		res.t_done = mono_seconds();
+		res.status = (int8_t)rc;
+		if (rc == CTW_E_CUDA) set_error(s, "grid lane");
+		{
+			std::lock_guard<std::mutex> lk(s->mu);
+			res.t_submit -= s->t0;
+			res.t_admit -= s->t0;
+			res.t_done -= s->t0;
+			s->done.push_back(res);
+			++s->finished;
+			s->grid_running = 0;
+		}
+		s->cv_done.notify_all();
+	}
+	for (auto &kv : eng)
+		if (kv.second) ctw_prp_destroy(kv.second);
 }
 
 }  // namespace
@@ -328,6 +472,7 @@ int ctw_server_create(size_t hbm_budget_bytes, int max_slots, uint32_t base, int
 	s->t0 = mono_seconds();
 	s->prep = std::thread(prep_loop, s);
 	s->worker = std::thread(worker_loop, s);
+	s->grid = std::thread(grid_loop, s);
 	*out = s;
 	return CTW_OK;
 }
@@ -345,11 +490,27 @@ int ctw_server_submit(ctw_server *s, int log2_degree, uint32_t b, uint64_t tag)
 		r.b = b;
 		r.tag = tag;
 		r.t_submit = mono_seconds();
-		s->incoming.push_back(r);
 		++s->submitted;
 		++s->pending;
+		if (s->grid_min > 0 && log2_degree >= s->grid_min)
+		{
+			s->grid_q.push_back(r);
+			s->cv_grid.notify_one();
+			return CTW_OK;
+		}
+		s->incoming.push_back(r);
 	}
 	s->cv_in.notify_one();
+	return CTW_OK;
+}
+
+int ctw_server_set_grid_lane(ctw_server *s, int min_log2_degree)
+{
+	if (!s) return fail(CTW_E_ARG, "null server");
+	if (min_log2_degree != 0 && (min_log2_degree < 8 || min_log2_degree > 18))
+		return fail(CTW_E_ARG, "grid lane degree %d not 0 or in [8, 18]", min_log2_degree);
+	std::lock_guard<std::mutex> lk(s->mu);
+	s->grid_min = min_log2_degree;
 	return CTW_OK;
 }
 
@@ -408,8 +569,11 @@ int ctw_server_destroy(ctw_server *s)
 	}
 	s->cv_in.notify_all();
 	s->cv_ready.notify_all();
+	s->cv_grid.notify_all();
+	s->cv_turn.notify_all();
 	if (s->prep.joinable()) s->prep.join();
 	if (s->worker.joinable()) s->worker.join();
+	if (s->grid.joinable()) s->grid.join();
 	delete s;
 	return CTW_OK;
 }

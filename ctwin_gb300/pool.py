@@ -232,11 +232,18 @@ class Server:
     """Request loop over pools of every degree (continuous batching by size class)."""
 
     def __init__(self, hbm_budget_bytes: int = 0, max_slots: int = 256, base: int = 2, ticks_per_launch: int = 2,
-                 autotune: bool = False):
+                 autotune: bool = False, grid_lane: int = 16):
+        """grid_lane: tests of degree >= 2^grid_lane run one at a time on the
+        cooperative grid kernel, taking turns with the pools (0: pools only)."""
         h = ctypes.c_void_p()
         check(lib().ctw_server_create(hbm_budget_bytes, max_slots, base, ticks_per_launch, 1 if autotune else 0,
                                       ctypes.byref(h)))
         self._h = h
+        try:
+            check(lib().ctw_server_set_grid_lane(h, grid_lane))
+        except Exception:
+            self.close()
+            raise
 
     def close(self):
         if self._h:

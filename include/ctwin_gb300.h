@@ -246,7 +246,7 @@ typedef struct ctw_result {
 	uint8_t gl_ok;            /* Gerbicz-Li check passed */
 	int8_t status;            /* 0, or the CTW_E_* code of a failed test */
 	uint8_t reserved;
-	int32_t slot;
+	int32_t slot;             /* pool slot; -1: never admitted; -2: the server's grid lane */
 	double t_submit, t_admit, t_done;
 	long long squarings;      /* squarings and multiplies run for this test */
 } ctw_result;
@@ -346,6 +346,13 @@ int ctw_server_create(size_t hbm_budget_bytes, int max_slots, uint32_t base, int
                       ctw_server **out);
 /* Queue a test (thread-safe).  8 <= log2_degree <= 18. */
 int ctw_server_submit(ctw_server *s, int log2_degree, uint32_t b, uint64_t tag);
+/* Grid lane: tests of degree >= 2^min_log2_degree (8..18; 0 turns the lane
+ * off) run one at a time on a one-lane engine instead of in pools; at 2^16..
+ * 2^18 the engine's default split is the cooperative grid kernel (one test
+ * over 64-128 SMs).  The lane and the pools take turns on the device at every
+ * Gerbicz-Li checkpoint of the lane's test.  Its results carry slot -2.
+ * Default 16.  Applies to requests submitted afterwards. */
+int ctw_server_set_grid_lane(ctw_server *s, int min_log2_degree);
 /* Create (and tune) the pools of a degree (one per prime class where the degree
  * has a two-prime kernel) ahead of its first request. */
 int ctw_server_prepare(ctw_server *s, int log2_degree, int slots);

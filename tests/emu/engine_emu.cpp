@@ -179,7 +179,18 @@ static int run_server(int argc, char **argv)
 	for (int i = 5; i < argc; ++i) bs.push_back((uint32_t)strtoul(argv[i], nullptr, 10));
 	ctw_server *s = nullptr;
 	int rc = ctw_server_create((size_t)1 << 30, max_slots, (uint32_t)base, 1, 0, &s);
-	for (size_t i = 0; i < bs.size() && !rc; ++i) rc = ctw_server_submit(s, ln, bs[i], i);
+	// CTW_EMU_GRID_LANE=<ln>:<b>: one more request of degree 2^ln, served by the
+	// server's grid lane (threshold ln), while the others run in pools
+	const char *gl = getenv("CTW_EMU_GRID_LANE");
+	int gln = 0;
+	uint32_t gb = 0;
+	if (gl && sscanf(gl, "%d:%u", &gln, &gb) == 2 && !rc)
+	{
+		rc = ctw_server_set_grid_lane(s, gln);
+		if (!rc) rc = ctw_server_submit(s, gln, gb, bs.size());
+		bs.push_back(gb);
+	}
+	for (size_t i = 0; i + (gb ? 1 : 0) < bs.size() && !rc; ++i) rc = ctw_server_submit(s, ln, bs[i], i);
 	size_t done = 0;
 	std::vector<ctw_result> res(16);
 	const auto t0 = std::chrono::steady_clock::now();
@@ -188,8 +199,9 @@ static int run_server(int argc, char **argv)
 		const int got = ctw_server_poll(s, res.data(), (int)res.size(), 1000);
 		if (got < 0) { rc = got; break; }
 		for (int i = 0; i < got; ++i, ++done)
-			printf("%u %d %016llX %d %d\n", res[(size_t)i].b, res[(size_t)i].is_prp,
-			       (unsigned long long)res[(size_t)i].res64, res[(size_t)i].gl_ok, res[(size_t)i].status);
+			printf("%u %d %016llX %d %d %d\n", res[(size_t)i].b, res[(size_t)i].is_prp,
+			       (unsigned long long)res[(size_t)i].res64, res[(size_t)i].gl_ok, res[(size_t)i].status,
+			       res[(size_t)i].slot);
 		if (std::chrono::steady_clock::now() - t0 > std::chrono::minutes(10)) { rc = -100; break; }
 	}
 	if (rc) fprintf(stderr, "error %d: %s\n", rc, ctw_last_error());

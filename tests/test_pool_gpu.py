@@ -222,3 +222,40 @@ def test_server_admits_arrivals_while_others_run(native):
             s.submit(ln, b, tag=t)
             r = s.drain(1, timeout_s=120)[0]
             assert (r["is_prp"], r["res64"], r["gl_ok"]) == (res[t]["is_prp"], res[t]["res64"], res[t]["gl_ok"])
+
+
+def test_server_grid_lane_beside_pools(native):
+    """The grid lane: a request of degree 2^16 runs on the one-lane engine (the
+    64-CTA cooperative grid) while requests of 2^10..2^12 run in pools; the two
+    take turns on the device at the lane test's Gerbicz-Li checkpoints, so pool
+    tests are admitted and finish while the lane test runs.  The lane's result
+    equals PrpEngine.run's for the same b, the pools' equal GMP's (tolerance 0)."""
+    import time
+
+    from ctwin_gb300 import PrpEngine, Server
+    big = (16, 1330358)                                     # about 1.33 M squarings
+    small = [(10, server_cases(10)[0]), (11, server_cases(11)[1]), (12, server_cases(12)[0]),
+             (12, server_cases(12)[1])]
+    with Server(hbm_budget_bytes=1 << 30, max_slots=8, ticks_per_launch=1) as s:
+        for ln in (10, 11, 12):
+            s.prepare(ln, 4)
+        s.submit(*big, tag=0)
+        t0 = time.time()
+        while s.stats()["active"] < 1:                      # the lane test is on the device
+            assert time.time() - t0 < 60
+            time.sleep(0.001)
+        for i, (ln, b) in enumerate(small):
+            s.submit(ln, b, tag=i + 1)
+        res = {r["tag"]: r for r in s.drain(1 + len(small), timeout_s=600)}
+    assert sorted(res) == list(range(1 + len(small)))
+    lane = res[0]
+    assert lane["slot"] == -2 and lane["status"] == 0 and lane["gl_ok"]
+    with PrpEngine(16, 1) as eng:
+        assert eng.geometry()["ctas_per_lane"] == 64
+        prp, r64, gl = eng.run([big[1]])
+    assert gl[0] and (lane["is_prp"], lane["res64"]) == (bool(prp[0]), int(r64[0]))
+    for t in range(1, 1 + len(small)):
+        r = res[t]
+        assert r["slot"] >= 0
+        check_results([r], small[t - 1][0])
+        assert lane["t_admit"] < r["t_admit"] and r["t_done"] < lane["t_done"], (lane, r)
