@@ -642,12 +642,23 @@ __device__ __forceinline__ void warp_sync()
 #endif
 }
 
+// Pad words of a column plane: when a row is 16 words, 16 words after every
+// 2^r rows, r the radix exponent of the last cross pass (the rows that one
+// half-warp of that pass covers: 8 for 64 CTAs, 4 for 128), so that the
+// half-warps of a cross pass fall in different banks; none otherwise.
+__host__ __device__ constexpr int grid2_pad_words(int lg, int lm)
+{
+	return ((1 << lm) >> lg) == 16
+	           ? ((1 << lg) >> (lg / ((lg + 2) / 3) + ((lg + 2) / 3 - 1 < lg % ((lg + 2) / 3) ? 1 : 0))) * 16
+	           : 0;
+}
+
 __host__ __device__ __forceinline__ size_t grid2_words(int lg, int lm, int np)
 {
 	const size_t M = (size_t)1 << lm, G = (size_t)1 << lg;
-	// XC (with a 16-word pad every 8 rows), XR, XD, chunk carries (M/8 int64),
-	// the left neighbour's carries (G int64), cross roots, TF + TI (pairs), XN, XDN
-	return 2 * np * M + np * (G / 8) * 16 + M + M / 4 + 2 * G + 2 * np * G + 4 * np * M + np * M + M;
+	// XC (with its pads), XR, XD, chunk carries (M/8 int64), the left
+	// neighbour's carries (G int64), cross roots, TF + TI (pairs), XN, XDN
+	return 2 * np * M + np * (size_t)grid2_pad_words(lg, lm) + M + M / 4 + 2 * G + 2 * np * G + 4 * np * M + np * M + M;
 }
 
 // Normalize1 of one chunk of CSZ Garner words (64-bit, two primes or narrow
@@ -697,8 +708,9 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	// column planes of MP words: row h at h * MG, plus a 16-word pad after every
 	// 8 rows when a row is 16 words, so that the half-warps of a cross pass whose
 	// rows are 8 apart fall in different banks
-	constexpr int MP = M + (G / 8) * 16;
-	auto xcp = [](int h, int tt) { return h * MG + (MG == 16 ? (h >> 3) * 16 : 0) + tt; };
+	constexpr int MP = M + grid2_pad_words(LG, LM), PADSH = XPass<LG, PL>::r;
+	static_assert(MG != 16 || (G >> PADSH) * 16 == MP - M, "pad layout");
+	auto xcp = [](int h, int tt) { return h * MG + (MG == 16 ? (h >> PADSH) * 16 : 0) + tt; };
 	uint32_t *XR = XC + NP * MP;                                // [NP][M] (sub-block swizzle)
 	int32_t *XD = reinterpret_cast<int32_t *>(XR + NP * M);     // [G][MG] digits
 	int64_t *fch = reinterpret_cast<int64_t *>(XD + M);         // [M/8]

@@ -382,7 +382,6 @@ void grid_loop(ctw_server *s)
 			if (s->stop) break;
 			r = s->grid_q.front();
 			s->grid_q.pop_front();
-			s->grid_running = 1;
 		}
 		ctw_result res{};
 		res.tag = r.tag;
@@ -403,6 +402,10 @@ void grid_loop(ctw_server *s)
 		{
 			if (!grid_take(s)) break;
 			res.t_admit = mono_seconds();
+			{
+				std::lock_guard<std::mutex> lk(s->mu);
+				s->grid_running = 1;                 // counted as active from its first turn on
+			}
 			uint8_t prp = 0, gl = 0;
 			uint64_t r64 = 0;
 			rc = ctw_prp_run_ex(h, &r.b, 1, -1, grid_checkpoint, s, &prp, &r64, &gl);

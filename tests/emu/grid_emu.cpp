@@ -66,7 +66,14 @@ static Kern pick(int lg, int lm, int np)
 static size_t grid_words(int lg, int lm, int tw, int np)
 {
 	const size_t M = (size_t)1 << lm, G = (size_t)1 << lg;
-	if (lm <= 11) return 2 * np * M + np * (G / 8) * 16 + M + M / 4 + 2 * G + 2 * np * G + 4 * np * M + np * M + M;
+	if (lm <= 11)
+	{
+		// the column planes' pads: 16 words after every 2^r rows of 16 words, r
+		// the radix exponent of the last cross pass
+		const int npass = (lg + 2) / 3, r = lg / npass + (npass - 1 < lg % npass ? 1 : 0);
+		const size_t pad = (M >> lg) == 16 ? (G >> r) * 16 : 0;
+		return 2 * np * M + np * pad + M + M / 4 + 2 * G + 2 * np * G + 4 * np * M + np * M + M;
+	}
 	return 2 * np * M + M / 4 + 2 * G + 2 * np * G + (tw ? 2 * np * M : 0) + (lm == 12 ? 2 * (size_t)np * 512 : 0);
 }
 
