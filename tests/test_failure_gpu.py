@@ -6,10 +6,12 @@
   ctw_prp_read_regs, written back with ctw_prp_write_regs at a checkpoint);
   the run must end with the check failed.  Run on the 64-CTA grid of degree
   2^16 and on a one-CTA engine of degree 2^12.
-* Grid barrier: every wait of the grid kernel is bounded (50 ms of
-  %globaltimer).  A test hook starts the barrier counter of one launch out of
-  reach; the launch must end within about one wait budget with CTW_E_COMPUTE,
-  and the same handle must then square bit-exactly again.
+* Grid waits: every wait of the grid kernel (barrier, carry count, poll of a
+  published word) is bounded (50 ms of %globaltimer).  A test hook starts the
+  barrier counter of one launch out of reach and has CTA 0 skip its first
+  publication of columns, so that the other CTAs' polls run out; the launch
+  must end within a few wait budgets with CTW_E_COMPUTE, and the same handle
+  must then square bit-exactly again.
 """
 import time
 
