@@ -705,9 +705,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	const int csz = a.csize, runc = MG / csz, ncl = G * runc, cb = g * MG;
 
 	uint32_t *XC = sm;                                          // [NP][G][MG]
-	// column planes of MP words: row h at h * MG, plus a 16-word pad after every
-	// 8 rows when a row is 16 words, so that the half-warps of a cross pass whose
-	// rows are 8 apart fall in different banks
+	// column planes of MP words: row h at h * MG, plus the pads of
+	// grid2_pad_words (after every 2^PADSH rows when a row is 16 words)
 	constexpr int MP = M + grid2_pad_words(LG, LM), PADSH = XPass<LG, PL>::r;
 	static_assert(MG != 16 || (G >> PADSH) * 16 == MP - M, "pad layout");
 	auto xcp = [](int h, int tt) { return h * MG + (MG == 16 ? (h >> PADSH) * 16 : 0) + tt; };
@@ -718,8 +717,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 	uint32_t *XRT = reinterpret_cast<uint32_t *>(xch + G);      // [NP][2][G]
 	uint32_t *TF = XRT + NP * 2 * G;                            // [NP][M][2] Shoup pairs
 	uint32_t *TI = TF + NP * 2 * M;
-	uint32_t *XN = TI + NP * 2 * M;                             // [NP][G][csz] the left neighbour's last chunk
-	int32_t *XDN = reinterpret_cast<int32_t *>(XN + NP * M);   // [G][csz] its digits (discarded)
+	uint32_t *XN = TI + NP * 2 * M;                             // [NP][G][MG] the left neighbour's last chunk
+	int32_t *XDN = reinterpret_cast<int32_t *>(XN + NP * M);   // [G][MG] its digits (discarded)
 	const int gl = (g + G - 1) % G;                             // the left neighbour in natural order
 	if (tid == 0) dead = 0;
 
@@ -791,7 +790,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		}
 	};
 	auto xw = [&](int pi, int h, int tt) -> uint32_t & {
-		return tt < MG ? XC[pi * MP + xcp(h, tt)] : XN[pi * G * csz + h * csz + (tt - MG)];
+		return tt < MG ? XC[pi * MP + xcp(h, tt)] : XN[pi * M + h * MG + (tt - MG)];
 	};
 	auto ld_xc = [&](int pi, int h, int tt, uint32_t) { return xw(pi, h, tt); };
 	auto st_xc = [&](int pi, int h, int tt, uint32_t v) { xw(pi, h, tt) = v; };
@@ -960,22 +959,18 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		{
 			constexpr int R = XPass<LG, PL>::R, r = Log2<R>::v, l0 = XPass<LG, PL>::l0, NGR = G >> r;
 			constexpr int lsh = LG - l0 - r, stride = 1 << lsh;
-			// pair items of this CTA's columns first, then of the neighbour's last
-			// chunk, so that a warp's stores stay in one array (bank-conflict free)
-			const int nown = NP * NGR * (MG / 2), nnb = nbr ? NP * NGR * (csz / 2) : 0;
-			for (int it = tid; it < nown + nnb; it += nt)
+			const int ncp = ncols / 2;
+			for (int it = tid; it < NP * NGR * ncp; it += nt)
 			{
-				const bool own = it < nown;
-				const int cp = own ? MG / 2 : csz / 2, i2 = own ? it : it - nown;
-				const int pi = i2 / (NGR * cp);
-				const int rem = i2 - pi * NGR * cp;
-				const int gam = rem / cp, t2 = 2 * (rem - gam * cp);
+				const int pi = it / (NGR * ncp);
+				const int rem = it - pi * NGR * ncp;
+				const int gam = rem / ncp, tt = 2 * (rem - gam * ncp);
 				const int jblk = gam >> lsh, i = gam & (stride - 1);
 				const int hbase = (jblk << (LG - l0)) + i;
 				const uint32_t q = qv(pi), qi = qiv(pi);
 				const uint32_t *tw = XRT + (pi * 2 + 1) * G;
 				auto idx = [&](int t, int kk) { return (1 << (l0 + t)) + (jblk << t) + kk; };
-				const uint32_t *src = gr + pi * M + (own ? g * MG + t2 : gl * MG + (MG - csz) + t2);
+				const uint32_t *src = gr + pi * M + (tt < MG ? g * MG + tt : gl * MG + (MG - csz) + (tt - MG));
 				uint32_t u0[R], u1[R];
 				uint2 w[R];
 				pub_gather<R>(w, [&](int k) { return src + (size_t)(hbase + k * stride) * 3 * M; }, br, err, vdead);
@@ -990,9 +985,8 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 #pragma unroll
 				for (int k = 0; k < R; ++k)
 				{
-					const int h = hbase + k * stride;
-					uint32_t *dst = own ? XC + pi * MP + xcp(h, t2) : XN + pi * G * csz + h * csz + t2;
-					*reinterpret_cast<uint2 *>(dst) = make_uint2(u0[k], u1[k]);
+					xw(pi, hbase + k * stride, tt) = u0[k];
+					xw(pi, hbase + k * stride, tt + 1) = u1[k];
 				}
 			}
 		}
@@ -1006,13 +1000,9 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 		// Garner, one item per (column, row group) holding every prime
 		{
 			constexpr int R = XPass<LG, 0>::R, r = Log2<R>::v, NGR = G >> r, lsh = LG - r, stride = 1 << lsh;
-			// items of this CTA's columns first, then of the neighbour's chunk
-			const int nown = NGR * MG, nnb = nbr ? NGR * csz : 0;
-			for (int it = tid; it < nown + nnb; it += nt)
+			for (int it = tid; it < NGR * ncols; it += nt)
 			{
-				const bool own = it < nown;
-				const int cw = own ? MG : csz, i2 = own ? it : it - nown;
-				const int gam = i2 / cw, tt = (own ? 0 : MG) + (i2 - gam * cw);
+				const int gam = it / ncols, tt = it - gam * ncols;
 				const int hbase = gam;                          // pass 0: jblk = 0, i = gam
 				uint32_t u[NP][R];
 #pragma unroll
@@ -1084,7 +1074,7 @@ __global__ void __launch_bounds__(prp_grid_threads(LM, NP), 1) prp_kernel_grid2(
 			else
 			{
 				const int h = c - ncl;
-				xch[h] = norm1(XN + h * csz, G * csz, XDN + h * csz);
+				xch[h] = norm1(XN + h * MG, M, XDN + h * MG);
 			}
 		}
 		__syncthreads();
