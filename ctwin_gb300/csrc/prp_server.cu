@@ -18,8 +18,9 @@
 // over 64-128 SMs, one test at a time, on a thread of its own.  A cooperative
 // grid needs all of its CTAs resident at once, so the lane and the pools take
 // turns on the device: at every Gerbicz-Li checkpoint of the lane's test the
-// lane hands the device back, the worker issues one round of pool launches,
-// waits for the pools' streams and hands it over again.
+// lane hands the device back; the worker keeps busy pools running for as long
+// as the lane held it (an even share while both have work), waits for the
+// pools' streams and hands it over again.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -165,6 +166,9 @@ void worker_loop(ctw_server *s)
 {
 	cudaSetDevice(s->device);
 	std::vector<ctw_result> buf(256);
+	// device-time share with the grid lane: after the lane held the device for
+	// a time t, busy pools get the device for at least t before the next turn
+	double granted_at = -1.0, pools_until = 0.0;
 	for (;;)
 	{
 		std::vector<std::pair<int, int>> ahead;
@@ -181,6 +185,12 @@ void worker_loop(ctw_server *s)
 			// no pool work is issued while the grid lane holds the device
 			s->cv_turn.wait(lk, [&] { return s->stop || !s->grid_has; });
 			if (s->stop) break;
+			if (granted_at >= 0)
+			{
+				const double now = mono_seconds();
+				pools_until = now + (now - granted_at);
+				granted_at = -1.0;
+			}
 			while (!s->ready.empty())
 			{
 				s->waiting.push_back(std::move(s->ready.front()));
@@ -306,12 +316,17 @@ void worker_loop(ctw_server *s)
 			             (long long)s->grid_q.size();
 		}
 		if (!out.empty()) s->cv_done.notify_all();
-		// the grid lane asks for the device: let this round of pool launches
-		// finish, then hand it over
+		// the grid lane asks for the device: once the pools have had their share
+		// (or have nothing to do), let the queued pool launches finish and hand
+		// the device over
 		bool grant;
 		{
 			std::lock_guard<std::mutex> lk(s->mu);
-			grant = s->grid_wants && !s->grid_has;
+			bool pools_busy = !s->waiting.empty();
+			for (auto &kv : s->pools)
+				for (ctw_pool *p : kv.second)
+					if (pool_active(p) > 0 || pool_in_flight(p) > 0) pools_busy = true;
+			grant = s->grid_wants && !s->grid_has && (!pools_busy || mono_seconds() >= pools_until);
 		}
 		if (grant)
 		{
@@ -322,6 +337,7 @@ void worker_loop(ctw_server *s)
 				std::lock_guard<std::mutex> lk(s->mu);
 				s->grid_has = true;
 			}
+			granted_at = mono_seconds();
 			s->cv_turn.notify_all();
 			continue;
 		}
