@@ -7,19 +7,20 @@
 // kernel: CTA g keeps, for every row block h < G, the run of coefficients
 // [h*M + g*MG, h*M + (g+1)*MG), MG = M/G.  Per squaring:
 //   digits -> residues; the LG cross levels of every column (radix-8/4 passes
-//   in shared memory); publish the columns to L2; grid barrier A; gather row
-//   block g (16-byte loads that bypass L1); the M-coefficient local
-//   transform, pointwise square and inverse; publish the row; grid barrier B;
-//   gather the columns; inverse cross levels; Garner; carry over the runs;
-//   publish the run-end carries; wait for those of the preceding CTA only;
-//   chunk carries.
+//   in shared memory); publish the columns to L2; gather row block g (loads
+//   that bypass L1); the M-coefficient local transform, pointwise square and
+//   inverse; publish the row; gather the columns; inverse cross levels;
+//   Garner; carry over the runs; chunk carries.
 // Registers after every squaring equal the cluster kernel's (and the
 // reference's) for the same CSIZE: the same transform, carry and wrap rules.
 //
-// Grid barriers are counters in global memory (zeroed by the host before each
-// launch).  The cooperative launch guarantees that all CTAs are resident; every
-// wait is still bounded by a %globaltimer budget, after which the CTA records
-// ST_GRID_WAIT and stops waiting, so a launch always ends.
+// prp_kernel_grid (CTAs of 4096) orders the exchanges with grid barriers and a
+// per-CTA carry count, counters in global memory zeroed by the host before each
+// launch; prp_kernel_grid2 (CTAs of 1024 / 2048) needs no barrier in a
+// squaring: its published words carry a parity bit that the readers poll (see
+// the comment at st_pub_u1).  The cooperative launch guarantees that all CTAs
+// are resident; every wait is still bounded by a %globaltimer budget, after
+// which the CTA records ST_GRID_WAIT and stops waiting, so a launch always ends.
 #include <type_traits>
 
 #include "prp_device.cuh"
