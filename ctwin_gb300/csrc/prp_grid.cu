@@ -1200,7 +1200,7 @@ static cudaError_t grid_launch_t(const PrpKernelArgs &a, const PrpGridArgs &ga, 
 	cfg.dynamicSmemBytes = smem;
 	cfg.stream = stream;
 	cudaLaunchAttribute at[1];
-	at[0].id = cudaLaunchAttributeCooperative;   // all CTAs resident: the grid barriers can complete
+	at[0].id = cudaLaunchAttributeCooperative;   // all CTAs resident: every wait for another CTA can end
 	at[0].val.cooperative = 1;
 	cfg.attrs = at;
 	cfg.numAttrs = 1;

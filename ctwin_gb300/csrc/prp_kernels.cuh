@@ -72,7 +72,7 @@ enum PrpStatus : uint32_t {
 	ST_OK = 0,
 	ST_BARRETT_RANGE = 1,       // quotient outside the two-step Barrett range
 	ST_DIGIT_RANGE = 2,         // a digit left the int32 range
-	ST_GRID_WAIT = 4,           // a grid barrier wait ran out (the launch's results are void)
+	ST_GRID_WAIT = 4,           // a grid wait (barrier, carry count, published word) ran out: results void
 };
 
 constexpr int GRID_BAR_WORDS = 32 + 128;

@@ -1,8 +1,9 @@
 """The PRP kernels' own source compiled for the host and run with one host
 thread per GPU thread (tests/emu/), under AddressSanitizer and UBSan:
 
-* the grid kernel (ctwin_gb300/csrc/prp_grid.cu): every CTA of a lane at once,
-  the grid barriers and the neighbour carry publications on host atomics;
+* the grid kernels (ctwin_gb300/csrc/prp_grid.cu): every CTA of a lane at
+  once, the grid barriers, carry counts and polled published words on host
+  atomics;
 * the one-CTA and cluster kernels (prp_kernel_impl.cuh): the CTAs of a
   cluster at once, cluster barriers and distributed shared memory emulated;
 * the whole sieve path (sieve.cu: host driver and kernels, ctw_sieve_run) on
