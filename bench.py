@@ -79,7 +79,7 @@ def workload(rank: int):
     return b, E, i0, B_GL, words
 
 
-TRAFFIC_PER_LAUNCH = 2.53e6     # ncu dram read+write bytes of one 651-squaring launch at 2^16 (64-CTA grid)
+TRAFFIC_PER_LAUNCH = 2.62e6     # ncu dram read+write bytes of one 651-squaring launch at 2^16 (64-CTA grid)
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one 651-squaring launch of the "
                   "default split (profiles/prp_kernel_grid2_d65536_full.md)")
 
