@@ -480,15 +480,26 @@ __global__ void pos_roots(int n, int lchunk, const PosPrime *pr, const uint32_t 
 		const uint64_t c2 = mp_mul(m, c, c), c4 = mp_mul(m, c2, c2), c6 = mp_mul(m, c4, c2);
 		uint64_t x = mp_toint(m, mp_mul(m, mp_pow(m, c6, t0), c));   // c^(6 t0 + 1), plain
 		const bool small_p = p <= bspan;
+		// for p > b_max a root r strikes at most r itself, when b_min <= r <= b_max,
+		// and its negative p - r, when p - b_max <= r <= p - b_min: one unsigned
+		// range test each
+		const uint64_t span = T.b_max - T.b_min, neg_lo = p - T.b_max;
 		for (uint64_t t = 0; t < (1ull << lc); ++t)
 		{
 			const uint64_t y = shoup64(x, gv.c4, gv.c4q, p);   // c^(6t+5)
-			const uint64_t r4[4] = { x, p - x, y, p - y };
-#pragma unroll
-			for (int j = 0; j < 4; ++j)
+			if (small_p)
 			{
-				const uint64_t r = r4[j];
-				if (small_p || (r >= T.b_min && r <= T.b_max)) strike_root(T, sb, r, p);
+				strike_root(T, sb, x, p);
+				strike_root(T, sb, p - x, p);
+				strike_root(T, sb, y, p);
+				strike_root(T, sb, p - y, p);
+			}
+			else
+			{
+				if (x - T.b_min <= span) strike_root(T, sb, x, p);
+				if (x - neg_lo <= span) strike_root(T, sb, p - x, p);
+				if (y - T.b_min <= span) strike_root(T, sb, y, p);
+				if (y - neg_lo <= span) strike_root(T, sb, p - y, p);
 			}
 			x = shoup64(y, gv.c2, gv.c2q, p);                  // c^(6t+7)
 		}
