@@ -119,6 +119,7 @@ def lib() -> ctypes.CDLL:
             "ctw_server_submit": ([H, i32, u32, ctypes.c_uint64], i32),
             "ctw_server_prepare": ([H, i32, i32], i32),
             "ctw_server_set_grid_lane": ([H, i32], i32),
+            "ctw_server_set_grid_lanes": ([H, i32], i32),
             "ctw_server_poll": ([H, vp, i32, i32], i32),
             "ctw_server_stats": ([H, vp, vp, vp, vp, vp], i32),
             "ctw_server_clock": ([H], ctypes.c_double),

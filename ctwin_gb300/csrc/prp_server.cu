@@ -13,13 +13,15 @@
 // bound: tests above it get pools of their own, so that they never hold the
 // others' launches at three primes.
 //
-// Grid lane: a test of degree >= grid_min (2^16 by default) runs instead on a
+// Grid lanes: a test of degree >= grid_min (2^16 by default) runs instead on a
 // one-lane engine, i.e. on the cooperative grid kernel that spreads one test
-// over 64-128 SMs, one test at a time, on a thread of its own.  A cooperative
-// grid needs all of its CTAs resident at once, so the lane and the pools take
-// turns on the device: at every Gerbicz-Li checkpoint of the lane's test the
-// lane hands the device back; the worker keeps busy pools running for as long
-// as the lane held it (an even share while both have work), waits for the
+// over 64-128 SMs, each lane a thread of its own running one test at a time
+// (GRID_LANES threads).  A cooperative grid needs all of its CTAs resident at
+// once, so the lanes and the pools take turns on the device: the worker hands
+// the device to the waiting lanes whose CTAs fit on the SMs together (two
+// tests of 64 CTAs, one of 128); at every Gerbicz-Li checkpoint a lane hands
+// it back; once all have, the worker keeps busy pools running for as long as
+// the lanes held it (an even share while both have work), waits for the
 // pools' streams and hands it over again.
 #include <algorithm>
 #include <chrono>
@@ -42,6 +44,8 @@
 using namespace ctw;
 
 namespace {
+
+constexpr int GRID_LANES = 2;
 
 struct Request {
 	int ln = 0;
@@ -74,13 +78,33 @@ struct ctw_server {
 	long long submitted = 0, finished = 0, active = 0, pending = 0;
 	size_t bytes = 0;
 
-	std::thread prep, worker, grid;
-	// grid lane (guarded by mu): queue, turn flags, the test on the device
-	int grid_min = 16;
+	std::thread prep, worker, grid[GRID_LANES];
+	// grid lanes (guarded by mu): queue, per-lane turn flags and CTA counts
+	int grid_min = 16, grid_lanes = GRID_LANES, sms = 0, grid_next = 0;
 	std::deque<Request> grid_q;
 	std::condition_variable cv_grid, cv_turn;
-	bool grid_wants = false, grid_has = false;
-	int grid_running = 0;
+	struct Lane {
+		bool wants = false, has = false;
+		int ctas = 0, running = 0;
+	} lane[GRID_LANES];
+	bool lanes_want() const
+	{
+		for (const Lane &l : lane)
+			if (l.wants && !l.has) return true;
+		return false;
+	}
+	bool lanes_have() const
+	{
+		for (const Lane &l : lane)
+			if (l.has) return true;
+		return false;
+	}
+	int lanes_running() const
+	{
+		int n = 0;
+		for (const Lane &l : lane) n += l.running;
+		return n;
+	}
 	// worker-owned
 	std::map<int, std::vector<ctw_pool *>> pools;   // class -> pools
 	std::map<int, std::pair<int, int>> split;      // class -> (log2 CTAs, csize)
@@ -180,10 +204,10 @@ void worker_loop(ctw_server *s)
 					if (pool_active(p) > 0 || pool_in_flight(p) > 0) busy = true;
 			if (!busy)
 				s->cv_ready.wait_for(lk, std::chrono::milliseconds(2), [&] {
-					return s->stop || !s->ready.empty() || !s->prepare_req.empty() || s->grid_wants;
+					return s->stop || !s->ready.empty() || !s->prepare_req.empty() || s->lanes_want();
 				});
-			// no pool work is issued while the grid lane holds the device
-			s->cv_turn.wait(lk, [&] { return s->stop || !s->grid_has; });
+			// no pool work is issued while a grid lane holds the device
+			s->cv_turn.wait(lk, [&] { return s->stop || !s->lanes_have(); });
 			if (s->stop) break;
 			if (granted_at >= 0)
 			{
@@ -311,14 +335,14 @@ void worker_loop(ctw_server *s)
 				s->done.push_back(r);
 			}
 			s->finished += (long long)out.size();
-			s->active = act + s->grid_running;
+			s->active = act + s->lanes_running();
 			s->pending = (long long)s->waiting.size() + (long long)s->ready.size() + (long long)s->incoming.size() +
 			             (long long)s->grid_q.size();
 		}
 		if (!out.empty()) s->cv_done.notify_all();
-		// the grid lane asks for the device: once the pools have had their share
-		// (or have nothing to do), let the queued pool launches finish and hand
-		// the device over
+		// grid lanes ask for the device: once the pools have had their share (or
+		// have nothing to do), let the queued pool launches finish and hand the
+		// device over
 		bool grant;
 		{
 			std::lock_guard<std::mutex> lk(s->mu);
@@ -326,7 +350,7 @@ void worker_loop(ctw_server *s)
 			for (auto &kv : s->pools)
 				for (ctw_pool *p : kv.second)
 					if (pool_active(p) > 0 || pool_in_flight(p) > 0) pools_busy = true;
-			grant = s->grid_wants && !s->grid_has && (!pools_busy || mono_seconds() >= pools_until);
+			grant = s->lanes_want() && !s->lanes_have() && (!pools_busy || mono_seconds() >= pools_until);
 		}
 		if (grant)
 		{
@@ -334,8 +358,20 @@ void worker_loop(ctw_server *s)
 				for (ctw_pool *p : kv.second)
 					if (cudaStreamSynchronize((cudaStream_t)ctw_pool_stream(p)) != cudaSuccess) set_error(s, "sync");
 			{
+				// the waiting lanes whose CTAs fit on the SMs together, taken in
+				// turn from the one after the lane served first last time
 				std::lock_guard<std::mutex> lk(s->mu);
-				s->grid_has = true;
+				int used = 0, granted = 0;
+				for (int k = 0; k < GRID_LANES && granted < s->grid_lanes; ++k)
+				{
+					const int i = (s->grid_next + k) % GRID_LANES;
+					ctw_server::Lane &l = s->lane[i];
+					if (!l.wants || (granted > 0 && used + l.ctas > s->sms)) continue;
+					if (granted == 0) s->grid_next = (i + 1) % GRID_LANES;
+					l.has = true;
+					used += l.ctas;
+					++granted;
+				}
 			}
 			granted_at = mono_seconds();
 			s->cv_turn.notify_all();
@@ -348,30 +384,35 @@ void worker_loop(ctw_server *s)
 	s->pools.clear();
 }
 
-// The grid lane's turn: ask the worker for the device and wait until it is
-// handed over (false when the server stops).
-bool grid_take(ctw_server *s)
+// A lane's turn: ask the worker for the device for `ctas` CTAs and wait until
+// it is handed over (false when the server stops).
+bool grid_take(ctw_server *s, int i, int ctas)
 {
 	std::unique_lock<std::mutex> lk(s->mu);
-	s->grid_wants = true;
+	s->lane[i].wants = true;
+	s->lane[i].ctas = ctas;
 	s->cv_ready.notify_all();
-	s->cv_turn.wait(lk, [&] { return s->stop || s->grid_has; });
-	s->grid_wants = false;
+	s->cv_turn.wait(lk, [&] { return s->stop || s->lane[i].has; });
+	s->lane[i].wants = false;
 	return !s->stop;
 }
-void grid_give(ctw_server *s)
+void grid_give(ctw_server *s, int i)
 {
 	{
 		std::lock_guard<std::mutex> lk(s->mu);
-		s->grid_has = false;
+		s->lane[i].has = false;
 	}
 	s->cv_turn.notify_all();
 }
+struct LaneCtx {
+	ctw_server *s;
+	int i, ctas;
+};
 int grid_checkpoint(void *user, long long)
 {
-	ctw_server *s = static_cast<ctw_server *>(user);
-	grid_give(s);
-	return grid_take(s) ? 0 : 1;
+	LaneCtx *c = static_cast<LaneCtx *>(user);
+	grid_give(c->s, c->i);
+	return grid_take(c->s, c->i, c->ctas) ? 0 : 1;
 }
 
 // Squarings and multiplies of ctw_prp_run_ex for one test of b at degree 2^ln.
@@ -385,7 +426,7 @@ long long grid_squarings(uint32_t b, int ln)
 	return (i0 + 1) + (i0 / B) + (j0 >= B ? j0 - B + 1 : 0) + B + 2;
 }
 
-void grid_loop(ctw_server *s)
+void grid_loop(ctw_server *s, int lane)
 {
 	cudaSetDevice(s->device);
 	std::map<int, ctw_prp *> eng;
@@ -414,21 +455,24 @@ void grid_loop(ctw_server *s)
 			h = nullptr;
 		}
 		bool stopped = false;
+		int ctas = 0;
+		if (rc == CTW_OK) rc = ctw_prp_geometry(h, &ctas, nullptr, nullptr);
 		if (rc == CTW_OK)
 		{
-			if (!grid_take(s)) break;
+			LaneCtx ctx{ s, lane, ctas };
+			if (!grid_take(s, lane, ctas)) break;
 			res.t_admit = mono_seconds();
 			{
 				std::lock_guard<std::mutex> lk(s->mu);
-				s->grid_running = 1;                 // counted as active from its first turn on
+				s->lane[lane].running = 1;           // counted as active from its first turn on
 			}
 			uint8_t prp = 0, gl = 0;
 			uint64_t r64 = 0;
-			rc = ctw_prp_run_ex(h, &r.b, 1, -1, grid_checkpoint, s, &prp, &r64, &gl);
+			rc = ctw_prp_run_ex(h, &r.b, 1, -1, grid_checkpoint, &ctx, &prp, &r64, &gl);
 			stopped = rc == CTW_STOPPED;
 			{
 				std::lock_guard<std::mutex> lk(s->mu);
-				if (s->grid_has) s->grid_has = false;
+				s->lane[lane].has = false;
 			}
 			s->cv_turn.notify_all();
 			res.is_prp = prp;
@@ -449,7 +493,7 @@ void grid_loop(ctw_server *s)
 			res.t_done -= s->t0;
 			s->done.push_back(res);
 			++s->finished;
-			s->grid_running = 0;
+			s->lane[lane].running = 0;
 		}
 		s->cv_done.notify_all();
 	}
@@ -491,7 +535,8 @@ int ctw_server_create(size_t hbm_budget_bytes, int max_slots, uint32_t base, int
 	s->t0 = mono_seconds();
 	s->prep = std::thread(prep_loop, s);
 	s->worker = std::thread(worker_loop, s);
-	s->grid = std::thread(grid_loop, s);
+	cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
+	for (int i = 0; i < GRID_LANES; ++i) s->grid[i] = std::thread(grid_loop, s, i);
 	*out = s;
 	return CTW_OK;
 }
@@ -530,6 +575,15 @@ int ctw_server_set_grid_lane(ctw_server *s, int min_log2_degree)
 		return fail(CTW_E_ARG, "grid lane degree %d not 0 or in [8, 18]", min_log2_degree);
 	std::lock_guard<std::mutex> lk(s->mu);
 	s->grid_min = min_log2_degree;
+	return CTW_OK;
+}
+
+int ctw_server_set_grid_lanes(ctw_server *s, int lanes)
+{
+	if (!s) return fail(CTW_E_ARG, "null server");
+	if (lanes < 1 || lanes > GRID_LANES) return fail(CTW_E_ARG, "grid lanes %d outside [1, %d]", lanes, GRID_LANES);
+	std::lock_guard<std::mutex> lk(s->mu);
+	s->grid_lanes = lanes;
 	return CTW_OK;
 }
 
@@ -592,7 +646,8 @@ int ctw_server_destroy(ctw_server *s)
 	s->cv_turn.notify_all();
 	if (s->prep.joinable()) s->prep.join();
 	if (s->worker.joinable()) s->worker.join();
-	if (s->grid.joinable()) s->grid.join();
+	for (std::thread &t : s->grid)
+		if (t.joinable()) t.join();
 	delete s;
 	return CTW_OK;
 }

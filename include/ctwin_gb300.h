@@ -346,13 +346,16 @@ int ctw_server_create(size_t hbm_budget_bytes, int max_slots, uint32_t base, int
                       ctw_server **out);
 /* Queue a test (thread-safe).  8 <= log2_degree <= 18. */
 int ctw_server_submit(ctw_server *s, int log2_degree, uint32_t b, uint64_t tag);
-/* Grid lane: tests of degree >= 2^min_log2_degree (8..18; 0 turns the lane
- * off) run one at a time on a one-lane engine instead of in pools; at 2^16..
- * 2^18 the engine's default split is the cooperative grid kernel (one test
- * over 64-128 SMs).  The lane and the pools take turns on the device at every
- * Gerbicz-Li checkpoint of the lane's test.  Its results carry slot -2.
- * Default 16.  Applies to requests submitted afterwards. */
+/* Grid lanes: tests of degree >= 2^min_log2_degree (8..18; 0 turns the lanes
+ * off) run on one-lane engines instead of in pools, one test per lane at a
+ * time; at 2^16..2^18 the engine's default split is the cooperative grid
+ * kernel (one test over 64-128 SMs).  The lanes whose CTAs fit on the SMs
+ * together hold the device at once (two tests of 64 CTAs, one of 128); lanes
+ * and pools take turns at every Gerbicz-Li checkpoint.  Lane results carry
+ * slot -2.  Default 16.  Applies to requests submitted afterwards. */
 int ctw_server_set_grid_lane(ctw_server *s, int min_log2_degree);
+/* How many grid lanes may hold the device at once: 1 or 2 (the default). */
+int ctw_server_set_grid_lanes(ctw_server *s, int lanes);
 /* Create (and tune) the pools of a degree (one per prime class where the degree
  * has a two-prime kernel) ahead of its first request. */
 int ctw_server_prepare(ctw_server *s, int log2_degree, int slots);

@@ -179,18 +179,22 @@ static int run_server(int argc, char **argv)
 	for (int i = 5; i < argc; ++i) bs.push_back((uint32_t)strtoul(argv[i], nullptr, 10));
 	ctw_server *s = nullptr;
 	int rc = ctw_server_create((size_t)1 << 30, max_slots, (uint32_t)base, 1, 0, &s);
-	// CTW_EMU_GRID_LANE=<ln>:<b>: one more request of degree 2^ln, served by the
-	// server's grid lane (threshold ln), while the others run in pools
+	// CTW_EMU_GRID_LANE=<ln>:<b>[,<b>...]: more requests of degree 2^ln, served
+	// by the server's grid lanes (threshold ln), while the others run in pools
 	const char *gl = getenv("CTW_EMU_GRID_LANE");
+	const size_t npool = bs.size();
 	int gln = 0;
-	uint32_t gb = 0;
-	if (gl && sscanf(gl, "%d:%u", &gln, &gb) == 2 && !rc)
+	if (gl && sscanf(gl, "%d:", &gln) == 1 && !rc)
 	{
 		rc = ctw_server_set_grid_lane(s, gln);
-		if (!rc) rc = ctw_server_submit(s, gln, gb, bs.size());
-		bs.push_back(gb);
+		for (const char *q = strchr(gl, ':'); q && !rc; q = strchr(q + 1, ','))
+		{
+			const uint32_t gb = (uint32_t)strtoul(q + 1, nullptr, 10);
+			rc = ctw_server_submit(s, gln, gb, bs.size());
+			bs.push_back(gb);
+		}
 	}
-	for (size_t i = 0; i + (gb ? 1 : 0) < bs.size() && !rc; ++i) rc = ctw_server_submit(s, ln, bs[i], i);
+	for (size_t i = 0; i < npool && !rc; ++i) rc = ctw_server_submit(s, ln, bs[i], i);
 	size_t done = 0;
 	std::vector<ctw_result> res(16);
 	const auto t0 = std::chrono::steady_clock::now();

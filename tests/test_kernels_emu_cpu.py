@@ -336,16 +336,15 @@ def test_server_grid_lane_emulated_matches_gmp(engine_emu, golden_dir):
     """The server's grid lane (a thread running one test at a time on a
     one-lane engine, taking turns on the device with the pools at every
     Gerbicz-Li checkpoint), threshold 2^9 for the emulation (2^16 by default):
-    one request of degree 2^9 in the lane while two of 2^8 share a one-slot
-    pool.  PRP flags and RES64 equal GMP's on both paths; the lane's result
-    carries slot -2."""
+    two requests of degree 2^9 in the two lanes (their one-CTA grids fit the
+    device together) while two of 2^8 share a one-slot pool.  PRP flags and
+    RES64 equal GMP's on both paths; the lanes' results carry slot -2."""
     import json
     gold = {x["b"]: x for x in json.load(open(os.path.join(golden_dir, "prp_gmp.json")))
             if x["n"] == 8 and x["base"] == 3 and x["form"] == "+"}
     bs = [68, 298]
-    lane_b = 71
-    _, r64, prp = O.fermat(lane_b, 9, 3)
-    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0", CTW_EMU_GRID_LANE=f"9:{lane_b}")
+    lane_bs = [71, 79]
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0", CTW_EMU_GRID_LANE="9:" + ",".join(map(str, lane_bs)))
     r = subprocess.run([engine_emu, "server", "8", "1", "3", *map(str, bs)], capture_output=True, text=True,
                        timeout=900, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
@@ -353,11 +352,13 @@ def test_server_grid_lane_emulated_matches_gmp(engine_emu, golden_dir):
     for line in r.stdout.strip().splitlines():
         b, p, res64, gl, status, slot = line.split()
         got[int(b)] = (p == "1", res64, gl, status, int(slot))
-    assert sorted(got) == sorted(bs + [lane_b])
+    assert sorted(got) == sorted(bs + lane_bs)
     for b in bs:
         assert got[b][:4] == (gold[b]["prp"], gold[b]["res64"], "1", "0"), b
         assert got[b][4] >= 0
-    assert got[lane_b] == (prp, f"{r64:016X}", "1", "0", -2)
+    for b in lane_bs:
+        _, r64, prp = O.fermat(b, 9, 3)
+        assert got[b] == (prp, f"{r64:016X}", "1", "0", -2), b
 
 
 def test_batch_emulated_equals_pools(engine_emu):

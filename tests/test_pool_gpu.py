@@ -259,3 +259,25 @@ def test_server_grid_lane_beside_pools(native):
         assert r["slot"] >= 0
         check_results([r], small[t - 1][0])
         assert lane["t_admit"] < r["t_admit"] and r["t_done"] < lane["t_done"], (lane, r)
+
+
+def test_server_two_grid_lanes_run_together(native):
+    """Two requests of degree 2^16 (64 CTAs each) hold the device together in
+    the two grid lanes: their admit-done intervals overlap and each result
+    equals PrpEngine.run's for its b."""
+    from ctwin_gb300 import PrpEngine, Server
+    bs = [65, 127]                                          # about 0.4 M squarings each
+    with Server(hbm_budget_bytes=1 << 30, max_slots=8) as s:
+        for i, b in enumerate(bs):
+            s.submit(16, b, tag=i)
+        res = {r["tag"]: r for r in s.drain(len(bs), timeout_s=600)}
+    assert sorted(res) == [0, 1]
+    a, c = res[0], res[1]
+    assert a["slot"] == c["slot"] == -2
+    assert a["t_admit"] < c["t_done"] and c["t_admit"] < a["t_done"], (a, c)   # both on the device at once
+    with PrpEngine(16, 1) as eng:
+        for i, b in enumerate(bs):
+            prp, r64, gl = eng.run([b])
+            r = res[i]
+            assert r["status"] == 0 and r["gl_ok"] and gl[0]
+            assert (r["is_prp"], r["res64"]) == (bool(prp[0]), int(r64[0]))
