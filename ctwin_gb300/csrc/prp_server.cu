@@ -16,13 +16,13 @@
 // Grid lanes: a test of degree >= grid_min (2^16 by default) runs instead on a
 // one-lane engine, i.e. on the cooperative grid kernel that spreads one test
 // over 64-128 SMs, each lane a thread of its own running one test at a time
-// (GRID_LANES threads).  A cooperative grid needs all of its CTAs resident at
-// once, so the lanes and the pools take turns on the device: the worker hands
-// the device to the waiting lanes whose CTAs fit on the SMs together (two
-// tests of 64 CTAs, one of 128); at every Gerbicz-Li checkpoint a lane hands
-// it back; once all have, the worker keeps busy pools running for as long as
-// the lanes held it (an even share while both have work), waits for the
-// pools' streams and hands it over again.
+// (one lane by default, up to GRID_LANES).  A cooperative grid needs all of
+// its CTAs resident at once, so the lanes and the pools take turns on the
+// device: the worker hands the device to the waiting lanes whose CTAs fit on
+// the SMs together (two tests of 64 CTAs, one of 128); at every Gerbicz-Li
+// checkpoint a lane hands it back; once all have, the worker keeps busy pools
+// running for as long as the lanes held it (an even share while both have
+// work), waits for the pools' streams and hands it over again.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -80,7 +80,7 @@ struct ctw_server {
 
 	std::thread prep, worker, grid[GRID_LANES];
 	// grid lanes (guarded by mu): queue, per-lane turn flags and CTA counts
-	int grid_min = 16, grid_lanes = GRID_LANES, sms = 0, grid_next = 0;
+	int grid_min = 16, grid_lanes = 1, sms = 0, grid_next = 0;
 	std::deque<Request> grid_q;
 	std::condition_variable cv_grid, cv_turn;
 	struct Lane {
@@ -435,7 +435,9 @@ void grid_loop(ctw_server *s, int lane)
 		Request r;
 		{
 			std::unique_lock<std::mutex> lk(s->mu);
-			s->cv_grid.wait(lk, [&] { return s->stop || !s->grid_q.empty(); });
+			// lanes beyond grid_lanes take no requests: with one lane the large
+			// tests run first come, first served
+			s->cv_grid.wait(lk, [&] { return s->stop || (lane < s->grid_lanes && !s->grid_q.empty()); });
 			if (s->stop) break;
 			r = s->grid_q.front();
 			s->grid_q.pop_front();
@@ -582,8 +584,11 @@ int ctw_server_set_grid_lanes(ctw_server *s, int lanes)
 {
 	if (!s) return fail(CTW_E_ARG, "null server");
 	if (lanes < 1 || lanes > GRID_LANES) return fail(CTW_E_ARG, "grid lanes %d outside [1, %d]", lanes, GRID_LANES);
-	std::lock_guard<std::mutex> lk(s->mu);
-	s->grid_lanes = lanes;
+	{
+		std::lock_guard<std::mutex> lk(s->mu);
+		s->grid_lanes = lanes;
+	}
+	s->cv_grid.notify_all();
 	return CTW_OK;
 }
 

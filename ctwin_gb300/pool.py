@@ -232,10 +232,11 @@ class Server:
     """Request loop over pools of every degree (continuous batching by size class)."""
 
     def __init__(self, hbm_budget_bytes: int = 0, max_slots: int = 256, base: int = 2, ticks_per_launch: int = 2,
-                 autotune: bool = False, grid_lane: int = 16, grid_lanes: int = 2):
+                 autotune: bool = False, grid_lane: int = 16, grid_lanes: int = 1):
         """grid_lane: tests of degree >= 2^grid_lane run on the cooperative grid
         kernel, one per lane at a time, taking turns with the pools (0: pools
-        only); grid_lanes: lanes that may hold the device at once (1 or 2)."""
+        only); grid_lanes: lanes taking requests (1: first come, first served;
+        2: two large tests in flight)."""
         h = ctypes.c_void_p()
         check(lib().ctw_server_create(hbm_budget_bytes, max_slots, base, ticks_per_launch, 1 if autotune else 0,
                                       ctypes.byref(h)))

@@ -354,7 +354,9 @@ int ctw_server_submit(ctw_server *s, int log2_degree, uint32_t b, uint64_t tag);
  * and pools take turns at every Gerbicz-Li checkpoint.  Lane results carry
  * slot -2.  Default 16.  Applies to requests submitted afterwards. */
 int ctw_server_set_grid_lane(ctw_server *s, int min_log2_degree);
-/* How many grid lanes may hold the device at once: 1 or 2 (the default). */
+/* Grid lanes that take requests: 1 (the default: large tests first come, first
+ * served) or 2 (two tests in flight; they hold the device together when their
+ * CTAs fit on the SMs, else in turns). */
 int ctw_server_set_grid_lanes(ctw_server *s, int lanes);
 /* Create (and tune) the pools of a degree (one per prime class where the degree
  * has a two-prime kernel) ahead of its first request. */

@@ -187,6 +187,8 @@ static int run_server(int argc, char **argv)
 	if (gl && sscanf(gl, "%d:", &gln) == 1 && !rc)
 	{
 		rc = ctw_server_set_grid_lane(s, gln);
+		const char *nl = getenv("CTW_EMU_GRID_LANES");
+		if (!rc) rc = ctw_server_set_grid_lanes(s, nl ? atoi(nl) : 2);
 		for (const char *q = strchr(gl, ':'); q && !rc; q = strchr(q + 1, ','))
 		{
 			const uint32_t gb = (uint32_t)strtoul(q + 1, nullptr, 10);

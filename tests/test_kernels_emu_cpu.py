@@ -332,19 +332,22 @@ def test_server_emulated_matches_gmp(engine_emu, golden_dir):
     assert any(gold[b]["prp"] for b in bs)
 
 
-def test_server_grid_lane_emulated_matches_gmp(engine_emu, golden_dir):
+@pytest.mark.parametrize("lanes", [1, 2])
+def test_server_grid_lane_emulated_matches_gmp(engine_emu, golden_dir, lanes):
     """The server's grid lane (a thread running one test at a time on a
     one-lane engine, taking turns on the device with the pools at every
     Gerbicz-Li checkpoint), threshold 2^9 for the emulation (2^16 by default):
-    two requests of degree 2^9 in the two lanes (their one-CTA grids fit the
-    device together) while two of 2^8 share a one-slot pool.  PRP flags and
-    RES64 equal GMP's on both paths; the lanes' results carry slot -2."""
+    two requests of degree 2^9 in one lane (first come, first served) or in
+    two (their one-CTA grids fit the device together) while two of 2^8 share
+    a one-slot pool.  PRP flags and RES64 equal GMP's on both paths; the
+    lanes' results carry slot -2."""
     import json
     gold = {x["b"]: x for x in json.load(open(os.path.join(golden_dir, "prp_gmp.json")))
             if x["n"] == 8 and x["base"] == 3 and x["form"] == "+"}
     bs = [68, 298]
     lane_bs = [71, 79]
-    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0", CTW_EMU_GRID_LANE="9:" + ",".join(map(str, lane_bs)))
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0", CTW_EMU_GRID_LANE="9:" + ",".join(map(str, lane_bs)),
+               CTW_EMU_GRID_LANES=str(lanes))
     r = subprocess.run([engine_emu, "server", "8", "1", "3", *map(str, bs)], capture_output=True, text=True,
                        timeout=900, env=env)
     assert r.returncode == 0, r.stderr[-2000:]

@@ -267,7 +267,7 @@ def test_server_two_grid_lanes_run_together(native):
     equals PrpEngine.run's for its b."""
     from ctwin_gb300 import PrpEngine, Server
     bs = [65, 127]                                          # about 0.4 M squarings each
-    with Server(hbm_budget_bytes=1 << 30, max_slots=8) as s:
+    with Server(hbm_budget_bytes=1 << 30, max_slots=8, grid_lanes=2) as s:
         for i, b in enumerate(bs):
             s.submit(16, b, tag=i)
         res = {r["tag"]: r for r in s.drain(len(bs), timeout_s=600)}
