@@ -38,7 +38,7 @@ CSRC = os.path.join(ROOT, "ctwin_gb300", "csrc")
 # default), 2^16 on 32 CTAs of 2048 with three primes, 2^17 on 32 CTAs of 4096,
 # 2^18 on 128 CTAs of 2048 with three primes (the 2^18 default), 2^17 on 64 CTAs
 # of 2048 (the 2^17 default)
-SHAPES = [(6, 2, 10), (5, 3, 11), (5, 2, 12), (7, 3, 11), (6, 2, 11)]
+SHAPES = [(6, 2, 10), (5, 3, 11), (5, 2, 12), (7, 3, 11), (6, 2, 11), (7, 2, 11)]
 MARK = "size_t prp_grid_smem_bytes(int lg, int lm, int tw_smem, int np)"
 
 
@@ -92,6 +92,7 @@ def grid_emu():
     (17, 12, 2, 8, 1330358, 32, 2),      # 4096-coefficient CTAs
     (17, 11, 2, 16, 1330358, 64, 2),     # the 2^17 default: 64 CTAs of 2048, runs of 32 columns
     (18, 11, 3, 16, 1330358, 32, 3),     # 128 CTAs
+    (18, 11, 2, 8, 1330358, 32, 2),      # 128 CTAs on two primes: the neighbour's chunk through three cross passes
 ])
 def test_grid_kernel_emulated_bit_exact(grid_emu, ln, lm, primes, csize, b, threads, mult):
     _run([grid_emu, ln, lm, primes, csize, b, threads, mult])
