@@ -457,6 +457,20 @@ def run_batch(args):
                                "tests_per_s_projected": alone / bits, "plain_tests_per_s_projected": plain / bits}
     for p in plist:
         p.close()
+    # residues: the first candidate of every class of degree 2^12 and 2^13 run
+    # to completion in a batch of its own, against the same test on the plain
+    # engine (PrpEngine.run, another launch path); tolerance 0
+    from ctwin_gb300 import PrpEngine
+    vpools = batch_pools({c: bl[:1] for c, bl in groups.items() if c[0] <= 13}, csize)
+    with Batch(list(vpools.values()), ctas_per_sm=occ) as bv:
+        vres = bv.run_to_completion()
+    for p in vpools.values():
+        p.close()
+    for r in vres:
+        with PrpEngine(r["log2_degree"], 1) as eng:
+            prp, r64, gl = eng.run([r["b"]])
+        if not (r["status"] == 0 and r["gl_ok"] and gl[0] and (r["is_prp"], r["res64"]) == (bool(prp[0]), int(r64[0]))):
+            raise SystemExit(f"batch result differs from the engine's for b={r['b']} at 2^{r['log2_degree']}")
     line = {
         "metric": "PRP squarings/s (batched, uneven degrees)", "value": value, "unit": "squarings/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
@@ -479,6 +493,8 @@ def run_batch(args):
                      "peak_source": "32-bit IMAD probe kernel run on this GPU in this process"},
         "cpu_baseline": None, "gpu_launches": persistent + 2 * len(plist) * args.steps,
         "persistent_launches": persistent, "clocks": clk.summary(),
+        "verified": {"tests": len(vres), "against": "PrpEngine.run (RES64, PRP flag, Gerbicz-Li)",
+                     "b": sorted(r["b"] for r in vres)},
     }
     print(json.dumps(line))
     return 0
